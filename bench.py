@@ -1,0 +1,419 @@
+"""Benchmark of the J-VIE solve path on one or more GPUs.
+
+Workload (single body, mixed precision): a 128^3 grid at 2 mm holding a seeded
+phantom of 12 random ellipsoids (eps_r ~ U[5,80], sigma ~ U[0.02,2] S/m) inside
+a 20 x 15 x 25 cm outer ellipsoid, 298 MHz, x-polarised plane wave travelling
++z; J-VIE form 2, GMRES restart 50, tolerance 1e-6 on the true FP64 relative
+residual.  A step is one full solve: RHS set-up on the device, the solve, and
+the scatter of J back onto the grid (the operator fN is assembled once per
+frequency, outside the timed region, and reported separately).
+
+Arms:
+  default          FP32 circulant matvec inside FP64 GMRES + FP64 refinement
+                   (inputs resident in HBM for `value`; host buffers through the
+                   C ABI for `e2e`); the plain FP64 solve and the matvec times
+                   are measured beside it.
+  --impl reference the reference's CPU path (the numpy/scipy restatement of
+                   mv_AN + pgmres, complex128, scipy.fft on all host cores),
+                   one GMRES iteration per step, reported as solves/s.
+
+Multi-GPU: each rank solves its own body (seed = rank); no data-path
+collective ("weak" scaling, replicas of independent objects).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "VIE solves/s & matvec ms @128^3, FP32+FP64-refined vs FP64 on GB300, 1e-6 residual"
+FREQ = 298e6
+L = M = N = 128
+DX = 2e-3
+N_ELL = 12
+TOL = 1e-6
+RESTART = 50
+# FP64 GMRES iterations of this workload (seed 0), measured by the FP64 arm on
+# GB300 (the CPU restatement takes the same iterations by parity); used only to
+# scale the CPU arm's per-iteration time to solves/s.
+FP64_ITERATIONS_C2 = None
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_problem(seed):
+    from marie_gb300 import phantoms
+
+    r, er, scale = phantoms.ellipsoids(L, M, N, DX, N_ELL, seed, FREQ)
+    return r, er
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if os.environ.get("MARIE_BENCH_GLOO") is None else "gloo")
+    return world, rank, local
+
+
+def reduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args, world, rank, local):
+    import ctypes as C
+
+    import torch
+
+    import marie_gb300 as mg
+    from marie_gb300 import _lib, vie
+
+    torch.cuda.set_device(local)
+    lib = _lib.load()
+    r, er = make_problem(seed=rank)
+    em = mg.EMconstants(FREQ)
+    E, _ = mg.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
+    dev = torch.device("cuda", local)
+    t_asm0 = time.perf_counter()
+    op = mg.Operator.assemble(L, M, N, DX, FREQ, precision="mixed")
+    torch.cuda.synchronize()
+    t_asm = time.perf_counter() - t_asm0
+
+    def colmajor(a):
+        t = torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose(*range(a.ndim - 1, -1, -1))))
+        return t.to(dev).permute(*range(a.ndim - 1, -1, -1))
+
+    Ed, erd = colmajor(E), colmajor(er)
+    stream = torch.cuda.ExternalStream(lib.marie_plan_stream(op.plan))
+
+    def solve(opr, Ein, e_r, rr):
+        return mg.JVIE_Solver(Ein, e_r, rr, FREQ, opr, tol=TOL, form=2, inner_it=RESTART, outer_it=200)
+
+    # --- timed region: mixed-precision solves, inputs resident in HBM --------
+    for _ in range(args.warmup):
+        res = solve(op, Ed, erd, r)
+    barrier(world)
+    torch.cuda.synchronize()
+    n0 = lib.marie_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            res = solve(op, Ed, erd, r)
+        ev1.record(stream)
+        ev1.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    launches = lib.marie_launch_count() - n0
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    elapsed_max = reduce_max(elapsed, world)
+    Jm, flag_m, relres_m, iter_m, resvec_m, _ = res
+    ms_per_step = elapsed_max / args.steps * 1e3
+    value = world * args.steps / elapsed_max
+
+    out = {}
+    if rank == 0:
+        # --- FP64 arm (the reference arithmetic on the GPU) -------------------
+        op64 = mg.Operator.from_array(op.to_array(), precision="fp64")
+        t0 = time.perf_counter()
+        J64, flag64, relres64, it64, resvec64, _ = solve(op64, Ed, erd, r)
+        torch.cuda.synchronize()
+        t64 = time.perf_counter() - t0
+        n_it64 = len(resvec64) - 1
+        field_err = float((torch.linalg.norm(Jm - J64) / torch.linalg.norm(J64)).item())
+
+        # --- matvec times on the solver's DOFs ------------------------------
+        mv = matvec_times(mg, op, op64, er, lib)
+
+        # --- e2e through the C ABI with host buffers ------------------------
+        Eh, erh = np.asfortranarray(E), np.asfortranarray(er)
+        solve(op, Eh, erh, r)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ne2e = max(1, min(args.steps, 3))
+        for _ in range(ne2e):
+            Jh = solve(op, Eh, erh, r)[0]
+        t_e2e = (time.perf_counter() - t0) / ne2e
+        V = L * M * N
+        hbm, kind = peaks()
+        dom = mv["dominant"]
+        out = {
+            "metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64 matvec / c128 krylov",
+            "data": "synthetic (seeded ellipsoid phantom, plane wave)",
+            "config": {"workload": "single body 128^3 @2mm, 12-ellipsoid phantom, 298 MHz plane wave, "
+                                   "J-VIE form 2, GMRES(50), FP32 matvec + FP64 refinement to 1e-6",
+                       "grid": [L, M, N], "fft_grid": [2 * L, 2 * M, 2 * N], "dofs": int(3 * np.count_nonzero(
+                           np.abs(er - 1) > 1e-12)), "l2": "working set (fN 0.8 GB + spectra 0.3 GB) > L2",
+                       "parallelism": f"replicas x{world}"},
+            "solve": {"mixed": {"flag": flag_m, "relres": relres_m, "iter": iter_m,
+                                "matvecs": len(resvec_m) - 1, "solves_per_s": round(value / world, 4)},
+                      "fp64": {"flag": flag64, "relres": relres64, "iter": it64, "iterations": n_it64,
+                               "seconds": round(t64, 4), "solves_per_s": round(1 / t64, 4)},
+                      "speedup_mixed_vs_fp64": round(t64 / (ms_per_step / 1e3), 3),
+                      "field_rel_err_mixed_vs_fp64": field_err},
+            "matvec_ms": {"fp32": mv["fp32_ms"], "fp64": mv["fp64_ms"], "fp32_passes_ms": mv["fp32_passes"],
+                          "fp64_passes_ms": mv["fp64_passes"]},
+            "assembly_s": round(t_asm, 3),
+            "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": round(dom["gbs"], 1), "peak": hbm,
+                         "unit": "GB/s", "frac": round(dom["gbs"] / hbm, 4), "traffic": None,
+                         "peak_kind": kind, "alg_bytes_per_launch": dom["bytes"]},
+            "matvec_roofline": {"alg_bytes": mv["alg_bytes"], "gbs": round(mv["alg_bytes"] / (mv["fp32_ms"] / 1e3) / 1e9, 1),
+                                "frac": round(mv["alg_bytes"] / (mv["fp32_ms"] / 1e3) / 1e9 / hbm, 4)},
+            "e2e": {"value": round(1.0 / t_e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": 4 * V * 16,
+                    "d2h_bytes_per_step": 3 * V * 16},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        }
+        if world == 1 and not args.no_cpu:
+            out["cpu_baseline"] = cpu_baseline(n_it64, budget_s=args.cpu_budget)
+    return out
+
+
+def matvec_times(mg, op, op64, er, lib):
+    """FP32 and FP64 matvec times (CUDA events, averaged) on the solver's DOFs."""
+    import ctypes as C
+
+    import torch
+
+    V = L * M * N
+    idxS = np.nonzero(np.abs(er.reshape(-1, order="F") - 1) > 1e-12)[0] + 1
+    idx = np.concatenate([idxS, V + idxS, 2 * V + idxS]).astype(np.int64)
+    n = idx.size
+    dev = torch.device("cuda")
+    Mr = torch.ones(V, dtype=torch.complex128, device=dev)
+    erf = torch.from_numpy(er.reshape(-1, order="F")).to(dev)
+    Mc = (erf - 1) / erf
+    idx_d = torch.from_numpy(idx).to(dev)
+    J = torch.randn(n, dtype=torch.complex128, device=dev)
+    out = torch.empty_like(J)
+    res = {}
+    for name, opr, prec in (("fp32", op, 32), ("fp64", op64, 64)):
+        st = torch.cuda.ExternalStream(lib.marie_plan_stream(opr.plan))
+        reps = 20 if prec == 32 else 5
+
+        def call():
+            s = lib.marie_mv_AN(opr.plan, C.c_void_p(J.data_ptr()), C.c_void_p(Mr.data_ptr()),
+                                C.c_void_p(Mc.data_ptr()), 8e-9, 0, C.c_void_p(idx_d.data_ptr()), n,
+                                C.c_void_p(out.data_ptr()), 1, prec)
+            assert s == 0, lib.marie_last_error()
+
+        for _ in range(3):
+            call()
+        # per-pass profile
+        pm = (C.c_double * 5)()
+        cnt = C.c_int64()
+        lib.marie_plan_profile(opr.plan, 1, pm, C.byref(cnt))
+        for _ in range(reps):
+            call()
+        lib.marie_plan_profile(opr.plan, 0, pm, C.byref(cnt))
+        passes = [round(x, 4) for x in pm]
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            call()
+        e1.record(st)
+        e1.synchronize()
+        res[name + "_ms"] = round(e0.elapsed_time(e1) / reps, 4)
+        res[name + "_passes"] = passes
+    # algorithmic bytes (complex64 spectra), per pass and per matvec
+    S = 8
+    Lp, Mp = 2 * L, 2 * M
+    fN_oct = 6 * (L + 1) * (M + 1) * (N + 1) * S
+    x_spec = 3 * Lp * M * N * S     # 3 x N x M x 2L
+    y_spec = 3 * Lp * Mp * N * S    # 3 x N x 2M x 2L
+    vec = n * 16
+    pass_bytes = [vec + x_spec, x_spec + y_spec, 2 * y_spec + fN_oct, y_spec + x_spec, x_spec + 4 * vec]
+    names = ["x_forward", "y_forward", "z_multiply", "y_inverse", "x_inverse"]
+    k = int(np.argmax(res["fp32_passes"]))
+    res["dominant"] = {"name": names[k], "bytes": pass_bytes[k],
+                       "gbs": pass_bytes[k] / (res["fp32_passes"][k] / 1e3) / 1e9}
+    res["alg_bytes"] = S * 56 * V + fN_oct
+    return res
+
+
+# ---------------------------------------------------------------------------
+# CPU arm (the oracle restatement of mv_AN + pgmres)
+# ---------------------------------------------------------------------------
+def cpu_iteration_time(budget_s=20.0):
+    """Seconds per GMRES iteration of the CPU restatement at 128^3 (one mv_AN
+    with scipy.fft on every host core, plus the CGS step at the mean basis size
+    of GMRES(50)).  fN values do not change the FFT cost, so a seeded random
+    operator of the right shape stands in for the assembled one."""
+    from oracle import vie_oracle as vo
+
+    workers = os.cpu_count() or 1
+    r, er = make_problem(0)
+    V = L * M * N
+    rng = np.random.default_rng(0)
+    fN = (rng.standard_normal((2 * L, 2 * M, 2 * N, 6)) + 1j * rng.standard_normal((2 * L, 2 * M, 2 * N, 6)))
+    Mr = np.ones((L, M, N), complex)
+    Mc = (er - 1) / er
+    idxS = np.nonzero(np.abs(er.reshape(-1, order="F") - 1) > 1e-12)[0] + 1
+    idx = np.concatenate([idxS, V + idxS, 2 * V + idxS])
+    n = idx.size
+    J = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    vo.mv_AN(J, fN, Mr, Mc, DX**3, "notransp", idx, workers)  # warm-up / plan
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        vo.mv_AN(J, fN, Mr, Mc, DX**3, "notransp", idx, workers)
+        reps += 1
+        if time.perf_counter() - t0 > budget_s * 0.7 or reps >= 10:
+            break
+    t_mv = (time.perf_counter() - t0) / reps
+    k = RESTART // 2
+    Vb = rng.standard_normal((n, k)) + 1j * rng.standard_normal((n, k))
+    t0 = time.perf_counter()
+    h = Vb.conj().T @ J
+    w = J - Vb @ h
+    np.linalg.norm(w)
+    t_cgs = time.perf_counter() - t0
+    return t_mv + t_cgs, workers, reps, t_mv, t_cgs
+
+
+def cpu_baseline(iterations, budget_s=20.0):
+    t_it, workers, reps, t_mv, t_cgs = cpu_iteration_time(budget_s)
+    solves = 1.0 / (t_it * iterations) if iterations else None
+    return {"value": solves, "unit": "solves/s", "cores": workers, "kind": "port",
+            "sample": f"{reps} oracle mv_AN calls at 128^3 (complex128, scipy.fft workers={workers}) "
+                      f"+ one CGS step at 25 basis vectors = {t_it:.3f} s/iteration, x {iterations} "
+                      f"FP64 GMRES iterations of this workload"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    iters = FP64_ITERATIONS_C2
+    times = []
+    for i in range(args.warmup + args.steps):
+        t_it, workers, reps, t_mv, t_cgs = cpu_iteration_time(budget_s=args.cpu_budget / max(1, args.steps))
+        if i >= args.warmup:
+            times.append(t_it)
+    t = statistics.mean(times)
+    value = 1.0 / (t * iters) if iters else 1.0 / t
+    unit = "solves/s" if iters else "GMRES iterations/s"
+    return {"metric": METRIC, "value": value, "unit": unit, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": "single body 128^3 @2mm, 12-ellipsoid phantom, J-VIE form 2, GMRES(50), "
+                                   "CPU restatement of mv_AN + pgmres", "grid": [L, M, N]},
+            "cpu_baseline": {"value": value, "unit": unit, "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"one GMRES iteration (mv_AN + CGS) per step, scaled by {iters} "
+                                       f"iterations per solve"},
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="marie", choices=["marie", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        out = run_reference(args, world, rank)
+    else:
+        out = run_gpu(args, world, rank, local)
+    if rank == 0 and out:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

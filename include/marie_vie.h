@@ -1,0 +1,158 @@
+/*
+ * marie_vie.h -- C ABI of the GB300 J-VIE solve path.
+ *
+ * Drop-in boundary for the FFT-accelerated current-based volume integral
+ * equation (J-VIE) path of MARIE: operator assembly (getOPERATORS), the
+ * circulant matvec (mv_AN / mv_L) and restarted GMRES (pgmres), plus the
+ * JVIE_Solver driver that strings them together.  Every entry point takes plain
+ * pointers and sizes; no C++ or torch types cross this boundary.
+ *
+ * Conventions (same as the reference MATLAB arrays):
+ *   - complex data is interleaved (re, im) doubles, i.e. double2;
+ *   - grid arrays are column-major: x fastest, then y, then z, then component;
+ *   - idx vectors are 1-based int64 linear indices into an L x M x N x 3 array
+ *     (the MATLAB vector idxS3), translated on the device;
+ *   - a pointer argument may be host memory (copied, as gpuArray/gather do) or
+ *     device memory (used in place); the library tells them apart itself;
+ *   - every call returns MARIE_OK (0) or a negative status; marie_last_error()
+ *     gives the message of the last failure on the calling thread.
+ *
+ * A plan binds one grid size, one CUDA stream and the device memory of the
+ * operator; calls on one plan are serialised on that stream.
+ */
+#ifndef MARIE_VIE_H
+#define MARIE_VIE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MARIE_OK 0
+#define MARIE_EINVAL (-1)      /* bad argument, shape or index                */
+#define MARIE_ENOMEM (-2)      /* device allocation failed                   */
+#define MARIE_ECUDA (-3)       /* CUDA runtime error                         */
+#define MARIE_ENOCONV (-4)     /* reserved: non-convergence is reported by flag */
+#define MARIE_EBREAKDOWN (-5)  /* Arnoldi breakdown with a non-finite residual */
+#define MARIE_ETIMEOUT (-6)    /* a bounded device wait ran out              */
+#define MARIE_EUNSUPPORTED (-7) /* FFT length or configuration not built     */
+#define MARIE_ENOOP (-8)       /* plan has no operator (set or assemble first) */
+
+/* arithmetic of the circulant matvec */
+#define MARIE_FP64 64
+#define MARIE_FP32 32
+#define MARIE_MIXED 96 /* FP32 matvec inside FP64 GMRES with FP64 refinement */
+
+typedef struct marie_plan marie_plan;
+
+/* y = A(x) on device vectors of length n (nrhs = 1).  Returns a status. */
+typedef int (*marie_op_fn)(void* ctx, const double* x, double* y, int64_t n);
+
+const char* marie_last_error(void);
+int marie_version(void);
+
+/* Create a plan for an L x M x N voxel grid (FFT grid 2L x 2M x 2N).
+ * precision: MARIE_FP64, MARIE_FP32 or MARIE_MIXED; nrhs_max bounds batched
+ * calls; stream is a cudaStream_t (NULL = a stream owned by the plan). */
+int marie_plan_create(int64_t L, int64_t M, int64_t N, int precision, int64_t nrhs_max,
+                      void* stream, marie_plan** plan);
+int marie_plan_destroy(marie_plan* plan);
+/* Device stream of the plan (a cudaStream_t). */
+void* marie_plan_stream(marie_plan* plan);
+
+/* Replaces getOPERATORS(r, f, op, type, singular)
+ * (src_vie/src_operators/getOPERATORS.m:1-127) for op = 'N'.
+ *   r:       L x M x N x 3 voxel centres (uniform spacing; dx = r[1]-r[0])
+ *   type:    'F' FFT of the circulant (2L x 2M x 2N x 6, the default 'FFTofC'),
+ *            'C' circulant (2L x 2M x 2N x 6), 'T' Toeplitz (L x M x N x 6)
+ *   singular:'D' computes the weakly singular self/edge/vertex integrals on
+ *            the device (converged 4-D quadrature); 'U' uses the five values
+ *            in singular_values = {ST, EAc, EAo, VAc, VAo} (complex)
+ *   op_out:  complex output, host or device.
+ * Component order [xx, xy, xz, yy, yz, zz] as vector_projection.m:15-22. */
+int marie_get_operators(const double* r, int64_t L, int64_t M, int64_t N, double f, char op,
+                        char type, char singular, const double* singular_values, double* op_out);
+
+/* The five singular integrals {ST, EAc, EAo, VAc, VAo} for voxel size dx and
+ * wavenumber ko (replaces singular_st/ea/va.m with singular='DIRECTFN'). */
+int marie_singular_integrals(double ko, double dx, double* out10);
+
+/* Upload an FFT-of-circulant operator fN (2L x 2M x 2N x 6 complex), as
+ * gpuArray(fN) in JVIE_Solver.m:271.  Converted to the plan's precisions. */
+int marie_set_operator(marie_plan* plan, const double* fN, int64_t Lf, int64_t Mf, int64_t Nf);
+/* Assemble the operator on the device for this plan's grid (no host copy). */
+int marie_plan_assemble(marie_plan* plan, double dx, double freq, char singular,
+                        const double* singular_values);
+/* Copy the plan's FP64 operator out (2L x 2M x 2N x 6 complex, host or device). */
+int marie_get_plan_operator(marie_plan* plan, double* fN_out);
+
+/* Replaces mv_AN(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, GPU_flag)
+ * (src_vie/src_mvp/mv_AN.m:1-146) with the plan's operator.
+ *   JIn0, JOut: n_idx x nrhs complex (columns contiguous)
+ *   Mr, Mc:     L x M x N complex
+ *   transp:     0 = 'notransp', 1 = 'transp' (Hermitian adjoint)
+ *   idx:        n_idx 1-based indices into L x M x N x 3 (no duplicates)
+ *   precision:  MARIE_FP64 or MARIE_FP32 (arithmetic of the circulant part) */
+int marie_mv_AN(marie_plan* plan, const double* JIn0, const double* Mr, const double* Mc,
+                double Gram, int transp, const int64_t* idx, int64_t n_idx, double* JOut,
+                int64_t nrhs, int precision);
+
+/* Replaces mv_L(JIn0, fN, r, Gram, idx, GPU_flag) (src_vie/src_mvp/mv_L.m:1-97):
+ * JOut = crop(N J) - Gram*J on the entries idx. */
+int marie_mv_L(marie_plan* plan, const double* JIn0, double Gram, const int64_t* idx,
+               int64_t n_idx, double* JOut, int64_t nrhs, int precision);
+
+/* Replaces pgmres(A, b, restart, tol, maxit, L1, L2, R1, R2, x0)
+ * (src_numeric/src_iterative/pgmres.m:70-181, pgmres_iter.m:22-150): restarted
+ * GMRES with classical Gram-Schmidt, function-handle preconditioners applied as
+ * products, true residual recomputed at the end.  All vectors are device or
+ * host (n complex); A/L1/L2/R1/R2 receive device vectors.  NULL L1..R2 = none;
+ * NULL x0 = zero start.  Outputs: x, flag (0 converged / 1 not), relres,
+ * iter = {inner, outer}, resvec (relative, length written to *resvec_len). */
+int marie_pgmres(marie_plan* plan, marie_op_fn A, void* A_ctx, const double* b, int64_t n,
+                 int restart, double tol, int maxit, marie_op_fn L1, void* L1_ctx,
+                 marie_op_fn L2, void* L2_ctx, marie_op_fn R1, void* R1_ctx, marie_op_fn R2,
+                 void* R2_ctx, const double* x0, double* x, int* flag, double* relres,
+                 int* iter, double* resvec, int64_t resvec_cap, int64_t* resvec_len);
+
+/* Replaces JVIE_Solver(Einc, e_r, r, freq, fN, tol, form, solver, precond, ...)
+ * (src_vie/src_solver/JVIE_Solver.m:1-521) with solver 'G' (pgmres) using the
+ * plan's operator.  Einc: L x M x N x 3, e_r: L x M x N (complex), dx the voxel
+ * edge.  form 1 or 2; precond 0, 'L' or 'R'.  With a MARIE_MIXED plan the
+ * matvec runs in FP32 inside FP64 GMRES, refined by FP64 true residuals until
+ * relres <= tol.  Je: L x M x N x 3.  iter = {inner, outer}. */
+int marie_jvie_solve(marie_plan* plan, const double* Einc, const double* e_r, double dx,
+                     double freq, int form, char precond, double tol, int inner_it,
+                     int outer_it, double* Je, int* flag, double* relres, int* iter,
+                     double* resvec, int64_t resvec_cap, int64_t* resvec_len, double* solvert);
+
+/* Replaces E_field_Nop(J, fN, Gram, freq, Einc) (src_vie/src_fields/src_op/
+ * E_field_Nop.m:59-84): Etot = Einc + (N J - Gram J)/(Gram*j*omega*eps0).
+ * J, Einc (may be NULL), Etot: L x M x N x 3 complex. */
+int marie_e_field_nop(marie_plan* plan, const double* J, double Gram, double freq,
+                      const double* Einc, double* Etot, int precision);
+
+/* Incident fields on the grid (L x M x N x 3 complex):
+ * PlaneWave_Excitation.m:39-95 (voxel-averaged, k = wavevector, Eo = polarisation)
+ * and Dipole_Excitation.m / E_field_DGF.m:36-99 (point-sampled electric dipoles,
+ * ndip dipoles with moments Jd[ndip][3] complex and positions pos[ndip][3]). */
+int marie_plane_wave(const double* r, int64_t L, int64_t M, int64_t N, const double* k,
+                     const double* Eo, double* E);
+int marie_dipole_field(const double* r, int64_t L, int64_t M, int64_t N, double ko,
+                       const double* Jd, const double* pos, int64_t ndip, double* E);
+
+/* Instrumentation (no counterpart in the reference, which times with tic/toc):
+ * number of kernels this library has launched since load, and per-pass device
+ * times of the matvec.  marie_plan_profile(plan, enable, pass_ms, count)
+ * returns the mean milliseconds of the five matvec passes (x forward, y
+ * forward, z multiply, y inverse, x inverse) over the matvecs run since the
+ * previous call, then resets and switches recording on or off. */
+int64_t marie_launch_count(void);
+int marie_plan_profile(marie_plan* plan, int enable, double* pass_ms, int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MARIE_VIE_H */

@@ -1,0 +1,472 @@
+// C-ABI entry points for plans, operator upload and the matvecs, plus the
+// host-side plumbing they share (pointer staging, workspaces, index maps).
+#include <cmath>
+#include <cstdarg>
+#include <atomic>
+#include <cstring>
+#include <vector>
+
+#include "matvec_launch.cuh"
+#include "plan.h"
+
+namespace marie {
+
+static thread_local char g_err[512] = "";
+static std::atomic<long long> g_launches{0};
+
+void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int DBuf::alloc(size_t bytes, cudaStream_t st) {
+  s = st;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMallocAsync(&p, bytes, st);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    cudaGetLastError();
+    return set_error(MARIE_ENOMEM, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+  }
+  return MARIE_OK;
+}
+
+bool is_device_ptr(const void* ptr) {
+  if (!ptr) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int stage_in(const void* user, size_t bytes, cudaStream_t st, DBuf& tmp, const void** dev) {
+  if (is_device_ptr(user)) {
+    *dev = user;
+    return MARIE_OK;
+  }
+  MARIE_TRY(tmp.alloc(bytes, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(tmp.p, user, bytes, cudaMemcpyHostToDevice, st));
+  *dev = tmp.p;
+  return MARIE_OK;
+}
+
+int stage_out(void* user, size_t bytes, cudaStream_t st, DBuf& tmp, void** dev) {
+  if (is_device_ptr(user)) {
+    *dev = user;
+    return MARIE_OK;
+  }
+  MARIE_TRY(tmp.alloc(bytes, st));
+  *dev = tmp.p;
+  return MARIE_OK;
+}
+
+int finish_out(void* user, const void* dev, size_t bytes, cudaStream_t st) {
+  if (user != dev) {
+    MARIE_CUDA_TRY(cudaMemcpyAsync(user, dev, bytes, cudaMemcpyDeviceToHost, st));
+    MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  return MARIE_OK;
+}
+
+int ensure_workspace(marie_plan* p, int prec, long long nrhs) {
+  const size_t es = (prec == MARIE_FP32) ? sizeof(float2) : sizeof(double2);
+  const size_t need_A = (size_t)p->elems_A() * es * nrhs;
+  const size_t need_B = (size_t)p->elems_B() * es * nrhs;
+  if (need_A > p->ws_bytes_A) {
+    if (p->wsA) cudaFreeAsync(p->wsA, p->stream);
+    p->wsA = nullptr;
+    p->ws_bytes_A = 0;
+    if (cudaMallocAsync(&p->wsA, need_A, p->stream) != cudaSuccess) {
+      cudaGetLastError();
+      p->wsA = nullptr;
+      return set_error(MARIE_ENOMEM, "workspace A (%zu bytes) allocation failed", need_A);
+    }
+    p->ws_bytes_A = need_A;
+  }
+  if (need_B > p->ws_bytes_B) {
+    if (p->wsB) cudaFreeAsync(p->wsB, p->stream);
+    p->wsB = nullptr;
+    p->ws_bytes_B = 0;
+    if (cudaMallocAsync(&p->wsB, need_B, p->stream) != cudaSuccess) {
+      cudaGetLastError();
+      p->wsB = nullptr;
+      return set_error(MARIE_ENOMEM, "workspace B (%zu bytes) allocation failed", need_B);
+    }
+    p->ws_bytes_B = need_B;
+  }
+  return MARIE_OK;
+}
+
+int ensure_pinned(marie_plan* p, size_t n) {
+  if (p->pinned_len >= n) return MARIE_OK;
+  if (p->pinned) cudaFreeHost(p->pinned);
+  p->pinned = nullptr;
+  p->pinned_len = 0;
+  MARIE_CUDA_TRY(cudaMallocHost(&p->pinned, n * sizeof(double)));
+  p->pinned_len = n;
+  return MARIE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// index map and coefficient kernels
+// ---------------------------------------------------------------------------
+__global__ void k_fill_int(int* a, long long n, int v) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+
+__global__ void k_scatter_inverse(const int64_t* idx, long long n, long long n3V, int* inv, int* err) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long g = idx[i] - 1;
+    if (g < 0 || g >= n3V) {
+      atomicOr(err, 1);
+      continue;
+    }
+    const int old = atomicExch(&inv[g], (int)i);
+    if (old != -1) atomicOr(err, 2);
+  }
+}
+
+__global__ void k_coefficients(const int64_t* idx, long long n, long long V, const double2* Mr, const double2* Mc,
+                               double Gram, int mode, double2* a, double2* b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long v = (idx[i] - 1) % V;
+    const double2 mr = Mr[v], mc = Mc[v];
+    if (mode == 0) {
+      a[i] = mk<double2>(Gram * mr.x, Gram * mr.y);
+      b[i] = mc;
+    } else {
+      b[i] = mc;                                      // prologue factor
+      a[i] = mk<double2>(Gram * mr.x, -Gram * mr.y);  // Gram * conj(Mr)
+    }
+  }
+}
+
+static inline int grid_for(long long n, int threads = 256) {
+  long long g = (n + threads - 1) / threads;
+  if (g > 152 * 16) g = 152 * 16;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+int build_inverse_index(marie_plan* p, const int64_t* idx_dev, long long n, int* inv) {
+  const long long n3V = 3 * p->d.V;
+  if (n < 0 || n > n3V) return set_error(MARIE_EINVAL, "n_idx = %lld outside [0, 3*L*M*N = %lld]", n, n3V);
+  DBuf err;
+  MARIE_TRY(err.alloc(sizeof(int), p->stream));
+  MARIE_CUDA_TRY(cudaMemsetAsync(err.p, 0, sizeof(int), p->stream));
+  k_fill_int<<<grid_for(n3V), 256, 0, p->stream>>>(inv, n3V, -1);
+  count_launch();
+  if (n > 0) {
+    k_scatter_inverse<<<grid_for(n), 256, 0, p->stream>>>(idx_dev, n, n3V, inv, err.as<int>());
+    count_launch();
+  }
+  MARIE_CUDA_TRY(cudaGetLastError());
+  int herr = 0;
+  MARIE_CUDA_TRY(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  if (herr & 1) return set_error(MARIE_EINVAL, "idx entry outside [1, 3*L*M*N]");
+  if (herr & 2) return set_error(MARIE_EINVAL, "idx has repeated entries");
+  return MARIE_OK;
+}
+
+int build_coefficients(marie_plan* p, const int64_t* idx_dev, long long n, const double2* Mr, const double2* Mc,
+                       double Gram, int mode, double2* a, double2* b) {
+  if (n == 0) return MARIE_OK;
+  k_coefficients<<<grid_for(n), 256, 0, p->stream>>>(idx_dev, n, p->d.V, Mr, Mc, Gram, mode, a, b);
+  count_launch();
+  MARIE_CUDA_TRY(cudaGetLastError());
+  return MARIE_OK;
+}
+
+template <typename T>
+static int run_matvec_t(marie_plan* p, const double2* J, double2* out, long long n, int nrhs, const int* inv,
+                        const Prologue& pro, const Epilogue& ep, const cplx<T>* fN, cplx<T>* const* tw) {
+  using ML = MatvecLaunch<T>;
+  const Dims& d = p->d;
+  const int prec = sizeof(T) == 4 ? MARIE_FP32 : MARIE_FP64;
+  const long long chunk_max = p->nrhs_max > 0 ? p->nrhs_max : 1;
+  for (long long r0 = 0; r0 < nrhs; r0 += chunk_max) {
+    const int nr = (int)((nrhs - r0) < chunk_max ? (nrhs - r0) : chunk_max);
+    MARIE_TRY(ensure_workspace(p, prec, nr));
+    cplx<T>* A = reinterpret_cast<cplx<T>*>(p->wsA);
+    cplx<T>* B = reinterpret_cast<cplx<T>*>(p->wsB);
+    const long long sA = p->elems_A(), sB = p->elems_B();
+    const double2* Jc = J + r0 * n;
+    double2* oc = out + r0 * n;
+    const bool prof = p->profile;
+    if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[0], p->stream));
+    MARIE_CUDA_TRY(ML::xfwd(Jc, n, inv, pro, A, sA, d, tw[0], nr, p->stream));
+    if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[1], p->stream));
+    MARIE_CUDA_TRY(ML::cols(false, d.Mp, A, (long long)d.Lp * d.M, sA, d.M, B, (long long)d.Lp * d.Mp, sB, d.Mp,
+                            d.Lp, 3 * d.N, tw[1], nr, p->stream));
+    if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
+    MARIE_CUDA_TRY(ML::zmul(B, sB, fN, d, tw[2], nr, p->stream));
+    if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
+    MARIE_CUDA_TRY(ML::cols(true, d.Mp, B, (long long)d.Lp * d.Mp, sB, d.Mp, A, (long long)d.Lp * d.M, sA, d.M,
+                            d.Lp, 3 * d.N, tw[1], nr, p->stream));
+    if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[4], p->stream));
+    MARIE_CUDA_TRY(ML::xinv(A, sA, Jc, n, inv, ep, oc, n, d, tw[0], nr, p->stream));
+    count_launch(5);
+    if (prof) {
+      MARIE_CUDA_TRY(cudaEventRecord(p->ev[5], p->stream));
+      MARIE_CUDA_TRY(cudaEventSynchronize(p->ev[5]));
+      for (int k = 0; k < 5; ++k) {
+        float ms = 0;
+        MARIE_CUDA_TRY(cudaEventElapsedTime(&ms, p->ev[k], p->ev[k + 1]));
+        p->pass_ms[k] += ms;
+      }
+      p->profiled += 1;
+    }
+  }
+  return MARIE_OK;
+}
+
+int run_matvec(marie_plan* p, int prec, const double2* J, double2* out, long long n, int nrhs, const int* inv,
+               const Prologue& pro, const Epilogue& ep) {
+  if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator: call marie_set_operator or marie_plan_assemble");
+  if (prec == MARIE_FP32) {
+    if (!p->fN32) return set_error(MARIE_EINVAL, "plan was not created with FP32 arithmetic");
+    return run_matvec_t<float>(p, J, out, n, nrhs, inv, pro, ep, p->fN32, p->tw32);
+  }
+  if (!p->fN64) return set_error(MARIE_EINVAL, "plan was not created with FP64 arithmetic");
+  return run_matvec_t<double>(p, J, out, n, nrhs, inv, pro, ep, p->fN64, p->tw64);
+}
+
+// twiddles exp(-2*pi*i*k/n), built in double on the host
+template <typename V> static int make_twiddles(int n, V** out, cudaStream_t st) {
+  std::vector<V> h(n);
+  for (int k = 0; k < n; ++k) {
+    const double a = 2.0 * M_PI * (double)k / (double)n;
+    h[k].x = (decltype(V::x))std::cos(a);
+    h[k].y = (decltype(V::x))(-std::sin(a));
+  }
+  MARIE_CUDA_TRY(cudaMalloc(out, n * sizeof(V)));
+  MARIE_CUDA_TRY(cudaMemcpy(*out, h.data(), n * sizeof(V), cudaMemcpyHostToDevice));
+  return MARIE_OK;
+}
+
+__global__ void k_scale_convert(const double2* in, long long n, double s, double2* o64, float2* o32) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double2 v = in[i];
+    if (o64) o64[i] = mk<double2>(v.x * s, v.y * s);
+    if (o32) o32[i] = mk<float2>((float)(v.x * s), (float)(v.y * s));
+  }
+}
+
+int install_operator(marie_plan* p, const double2* fN_dev) {
+  const long long P = (long long)p->d.Lp * p->d.Mp * p->d.Np;
+  const long long n = 6 * P;
+  const bool need64 = p->precision != MARIE_FP32;
+  const bool need32 = p->precision != MARIE_FP64;
+  if (need64 && !p->fN64) MARIE_CUDA_TRY(cudaMalloc(&p->fN64, n * sizeof(double2)));
+  if (need32 && !p->fN32) MARIE_CUDA_TRY(cudaMalloc(&p->fN32, n * sizeof(float2)));
+  k_scale_convert<<<grid_for(n), 256, 0, p->stream>>>(fN_dev, n, 1.0 / (double)P, need64 ? p->fN64 : nullptr,
+                                                       need32 ? p->fN32 : nullptr);
+  count_launch();
+  MARIE_CUDA_TRY(cudaGetLastError());
+  MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  p->has_op = true;
+  return MARIE_OK;
+}
+
+}  // namespace marie
+
+using namespace marie;
+
+extern "C" {
+
+const char* marie_last_error(void) { return g_err; }
+int marie_version(void) { return 1; }
+
+int marie_plan_create(int64_t L, int64_t M, int64_t N, int precision, int64_t nrhs_max, void* stream,
+                      marie_plan** out) {
+  if (!out) return set_error(MARIE_EINVAL, "plan output pointer is NULL");
+  *out = nullptr;
+  if (L < 1 || M < 1 || N < 1) return set_error(MARIE_EINVAL, "grid dimensions must be positive");
+  if (!fft_length_supported((int)(2 * L)) || !fft_length_supported((int)(2 * M)) ||
+      !fft_length_supported((int)(2 * N)))
+    return set_error(MARIE_EUNSUPPORTED,
+                     "padded FFT lengths %lld x %lld x %lld: each must be one of 8 16 24 32 40 48 64 80 96 128 160 "
+                     "192 256 320 384 512",
+                     (long long)(2 * L), (long long)(2 * M), (long long)(2 * N));
+  if (precision != MARIE_FP64 && precision != MARIE_FP32 && precision != MARIE_MIXED)
+    return set_error(MARIE_EINVAL, "precision must be MARIE_FP64, MARIE_FP32 or MARIE_MIXED");
+  marie_plan* p = new marie_plan();
+  p->d.L = (int)L; p->d.M = (int)M; p->d.N = (int)N;
+  p->d.Lp = (int)(2 * L); p->d.Mp = (int)(2 * M); p->d.Np = (int)(2 * N);
+  p->d.V = L * M * N;
+  p->precision = precision;
+  p->nrhs_max = nrhs_max > 0 ? nrhs_max : 1;
+  cudaGetDevice(&p->device);
+  if (stream) {
+    p->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete p;
+      return set_error(MARIE_ECUDA, "stream creation failed");
+    }
+    p->own_stream = true;
+  }
+  const int lens[3] = {p->d.Lp, p->d.Mp, p->d.Np};
+  for (int a = 0; a < 3; ++a) {
+    int s = MARIE_OK;
+    if (precision != MARIE_FP32 && s == MARIE_OK) s = make_twiddles(lens[a], &p->tw64[a], p->stream);
+    if (precision != MARIE_FP64 && s == MARIE_OK) s = make_twiddles(lens[a], &p->tw32[a], p->stream);
+    if (s != MARIE_OK) {
+      marie_plan_destroy(p);
+      return s;
+    }
+  }
+  *out = p;
+  return MARIE_OK;
+}
+
+int marie_plan_destroy(marie_plan* p) {
+  if (!p) return MARIE_OK;
+  if (p->stream) cudaStreamSynchronize(p->stream);
+  if (p->wsA) cudaFreeAsync(p->wsA, p->stream);
+  if (p->wsB) cudaFreeAsync(p->wsB, p->stream);
+  if (p->stream) cudaStreamSynchronize(p->stream);
+  cudaFree(p->fN64);
+  cudaFree(p->fN32);
+  for (int a = 0; a < 3; ++a) {
+    cudaFree(p->tw64[a]);
+    cudaFree(p->tw32[a]);
+  }
+  if (p->pinned) cudaFreeHost(p->pinned);
+  for (int k = 0; k < 6; ++k)
+    if (p->ev[k]) cudaEventDestroy(p->ev[k]);
+  if (p->own_stream) cudaStreamDestroy(p->stream);
+  delete p;
+  return MARIE_OK;
+}
+
+void* marie_plan_stream(marie_plan* p) { return p ? (void*)p->stream : nullptr; }
+
+int64_t marie_launch_count(void) { return g_launches.load(); }
+
+int marie_plan_profile(marie_plan* p, int enable, double* pass_ms, int64_t* count) {
+  if (!p) return set_error(MARIE_EINVAL, "NULL plan");
+  if (pass_ms) {
+    for (int k = 0; k < 5; ++k) pass_ms[k] = p->profiled ? p->pass_ms[k] / (double)p->profiled : 0.0;
+  }
+  if (count) *count = p->profiled;
+  for (int k = 0; k < 5; ++k) p->pass_ms[k] = 0;
+  p->profiled = 0;
+  if (enable && !p->ev[0])
+    for (int k = 0; k < 6; ++k) MARIE_CUDA_TRY(cudaEventCreate(&p->ev[k]));
+  p->profile = enable != 0;
+  return MARIE_OK;
+}
+
+int marie_set_operator(marie_plan* p, const double* fN, int64_t Lf, int64_t Mf, int64_t Nf) {
+  if (!p || !fN) return set_error(MARIE_EINVAL, "NULL plan or operator");
+  if (Lf != p->d.Lp || Mf != p->d.Mp || Nf != p->d.Np)
+    return set_error(MARIE_EINVAL, "operator is %lldx%lldx%lld, plan expects %dx%dx%d", (long long)Lf,
+                     (long long)Mf, (long long)Nf, p->d.Lp, p->d.Mp, p->d.Np);
+  const size_t bytes = (size_t)6 * Lf * Mf * Nf * sizeof(double2);
+  DBuf tmp;
+  const void* dev = nullptr;
+  MARIE_TRY(stage_in(fN, bytes, p->stream, tmp, &dev));
+  return install_operator(p, (const double2*)dev);
+}
+
+int marie_get_plan_operator(marie_plan* p, double* fN_out) {
+  if (!p || !fN_out) return set_error(MARIE_EINVAL, "NULL plan or output");
+  if (!p->has_op || !p->fN64) return set_error(MARIE_ENOOP, "plan holds no FP64 operator");
+  const long long P = (long long)p->d.Lp * p->d.Mp * p->d.Np;
+  const size_t bytes = (size_t)6 * P * sizeof(double2);
+  DBuf tmp;
+  void* dev = nullptr;
+  MARIE_TRY(stage_out(fN_out, bytes, p->stream, tmp, &dev));
+  k_scale_convert<<<grid_for(6 * P), 256, 0, p->stream>>>(p->fN64, 6 * P, (double)P, (double2*)dev, nullptr);
+  count_launch();
+  MARIE_CUDA_TRY(cudaGetLastError());
+  MARIE_TRY(finish_out(fN_out, dev, bytes, p->stream));
+  return MARIE_OK;
+}
+
+static int check_prec(marie_plan* p, int precision) {
+  if (precision != MARIE_FP64 && precision != MARIE_FP32)
+    return set_error(MARIE_EINVAL, "matvec precision must be MARIE_FP64 or MARIE_FP32");
+  if (precision == MARIE_FP32 && !p->fN32) return set_error(MARIE_EINVAL, "plan has no FP32 operator");
+  if (precision == MARIE_FP64 && !p->fN64) return set_error(MARIE_EINVAL, "plan has no FP64 operator");
+  return MARIE_OK;
+}
+
+int marie_mv_AN(marie_plan* p, const double* JIn0, const double* Mr, const double* Mc, double Gram, int transp,
+                const int64_t* idx, int64_t n_idx, double* JOut, int64_t nrhs, int precision) {
+  if (!p || !JIn0 || !Mr || !Mc || !JOut || (!idx && n_idx > 0)) return set_error(MARIE_EINVAL, "NULL argument");
+  if (nrhs < 1) return set_error(MARIE_EINVAL, "nrhs must be >= 1");
+  if (transp != 0 && transp != 1) return set_error(MARIE_EINVAL, "transp must be 0 ('notransp') or 1 ('transp')");
+  MARIE_TRY(check_prec(p, precision));
+  if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator");
+  const long long V = p->d.V, n = n_idx;
+  DBuf tJ, tMr, tMc, tidx, tout, inv, ca, cb;
+  const void *J_d, *Mr_d, *Mc_d, *idx_d;
+  void* out_d;
+  MARIE_TRY(stage_in(JIn0, n * nrhs * sizeof(double2), p->stream, tJ, &J_d));
+  MARIE_TRY(stage_in(Mr, V * sizeof(double2), p->stream, tMr, &Mr_d));
+  MARIE_TRY(stage_in(Mc, V * sizeof(double2), p->stream, tMc, &Mc_d));
+  MARIE_TRY(stage_in(idx, n * sizeof(int64_t), p->stream, tidx, &idx_d));
+  MARIE_TRY(stage_out(JOut, n * nrhs * sizeof(double2), p->stream, tout, &out_d));
+  MARIE_TRY(inv.alloc(3 * V * sizeof(int), p->stream));
+  MARIE_TRY(ca.alloc(n * sizeof(double2), p->stream));
+  MARIE_TRY(cb.alloc(n * sizeof(double2), p->stream));
+  MARIE_TRY(build_inverse_index(p, (const int64_t*)idx_d, n, inv.as<int>()));
+  MARIE_TRY(build_coefficients(p, (const int64_t*)idx_d, n, (const double2*)Mr_d, (const double2*)Mc_d, Gram, transp,
+                               ca.as<double2>(), cb.as<double2>()));
+  Prologue pro{nullptr, 0};
+  Epilogue ep{};
+  if (transp == 0) {
+    ep.a = ca.as<double2>();
+    ep.b = cb.as<double2>();
+    ep.conjout = 0;
+  } else {
+    pro.pre = cb.as<double2>();
+    pro.conjin = 1;
+    ep.a = ca.as<double2>();
+    ep.conjout = 1;
+  }
+  if (n > 0)
+    MARIE_TRY(run_matvec(p, precision, (const double2*)J_d, (double2*)out_d, n, (int)nrhs, inv.as<int>(), pro, ep));
+  MARIE_TRY(finish_out(JOut, out_d, n * nrhs * sizeof(double2), p->stream));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return MARIE_OK;
+}
+
+int marie_mv_L(marie_plan* p, const double* JIn0, double Gram, const int64_t* idx, int64_t n_idx, double* JOut,
+               int64_t nrhs, int precision) {
+  if (!p || !JIn0 || !JOut || (!idx && n_idx > 0)) return set_error(MARIE_EINVAL, "NULL argument");
+  if (nrhs < 1) return set_error(MARIE_EINVAL, "nrhs must be >= 1");
+  MARIE_TRY(check_prec(p, precision));
+  if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator");
+  const long long V = p->d.V, n = n_idx;
+  DBuf tJ, tidx, tout, inv;
+  const void *J_d, *idx_d;
+  void* out_d;
+  MARIE_TRY(stage_in(JIn0, n * nrhs * sizeof(double2), p->stream, tJ, &J_d));
+  MARIE_TRY(stage_in(idx, n * sizeof(int64_t), p->stream, tidx, &idx_d));
+  MARIE_TRY(stage_out(JOut, n * nrhs * sizeof(double2), p->stream, tout, &out_d));
+  MARIE_TRY(inv.alloc(3 * V * sizeof(int), p->stream));
+  MARIE_TRY(build_inverse_index(p, (const int64_t*)idx_d, n, inv.as<int>()));
+  Prologue pro{nullptr, 0};
+  Epilogue ep{};
+  ep.a_s = mk<double2>(-Gram, 0.0);
+  ep.b_s = mk<double2>(-1.0, 0.0);
+  if (n > 0)
+    MARIE_TRY(run_matvec(p, precision, (const double2*)J_d, (double2*)out_d, n, (int)nrhs, inv.as<int>(), pro, ep));
+  MARIE_TRY(finish_out(JOut, out_d, n * nrhs * sizeof(double2), p->stream));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return MARIE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,242 @@
+// Register-resident mixed-radix Stockham FFT for sequences staged in shared memory.
+//
+// A sequence of compile-time length N is processed by T = N/E threads; each
+// thread keeps E complex values in registers.  A pass of radix R performs E/R
+// butterflies per thread entirely in registers; between passes the values are
+// exchanged through shared memory (one store + one load per element).  The
+// Stockham autosort indexing (input j + r*N/R, output (j/Ns)*Ns*R + j%Ns + r*Ns)
+// leaves the result in natural order, so no bit-reversal pass is needed.
+//
+// Shared-memory layout is described by an element pointer `base` (this thread's
+// sequence) and an element stride `es`, so the same engine serves contiguous
+// rows and strided columns (columns use es = S+1 with S sequences interleaved,
+// which keeps every warp access to full 128-byte rows).
+//
+// Twiddles come from a per-length table exp(-2*pi*i*k/N), k < N, built on the
+// host in double precision and staged into shared memory by the caller.
+#pragma once
+#include "common.cuh"
+
+namespace marie {
+
+template <int... Rs> struct RList {};
+
+// Radix schedule per FFT length.  E = lcm of the radices (values per thread).
+// The first radix is even so that a zero-padded input (only the first N/2
+// values non-zero) skips the loads of the known-zero half in the first pass.
+template <int N> struct FFTCfg;
+template <> struct FFTCfg<8>   { using R = RList<8>;        static constexpr int E = 8; };
+template <> struct FFTCfg<16>  { using R = RList<4, 4>;     static constexpr int E = 4; };
+template <> struct FFTCfg<24>  { using R = RList<8, 3>;     static constexpr int E = 24; };
+template <> struct FFTCfg<32>  { using R = RList<8, 4>;     static constexpr int E = 8; };
+template <> struct FFTCfg<40>  { using R = RList<2, 4, 5>;  static constexpr int E = 20; };
+template <> struct FFTCfg<48>  { using R = RList<4, 4, 3>;  static constexpr int E = 12; };
+template <> struct FFTCfg<64>  { using R = RList<8, 8>;     static constexpr int E = 8; };
+template <> struct FFTCfg<80>  { using R = RList<4, 4, 5>;  static constexpr int E = 20; };
+template <> struct FFTCfg<96>  { using R = RList<8, 4, 3>;  static constexpr int E = 24; };
+template <> struct FFTCfg<128> { using R = RList<8, 4, 4>;  static constexpr int E = 8; };
+template <> struct FFTCfg<160> { using R = RList<4, 4, 2, 5>; static constexpr int E = 20; };
+template <> struct FFTCfg<192> { using R = RList<8, 8, 3>;  static constexpr int E = 24; };
+template <> struct FFTCfg<256> { using R = RList<8, 8, 4>;  static constexpr int E = 8; };
+template <> struct FFTCfg<320> { using R = RList<4, 4, 4, 5>; static constexpr int E = 20; };
+template <> struct FFTCfg<384> { using R = RList<8, 8, 2, 3>; static constexpr int E = 24; };
+template <> struct FFTCfg<512> { using R = RList<8, 8, 8>;  static constexpr int E = 8; };
+
+template <typename L> struct RFirst;
+template <int R0, int... Rs> struct RFirst<RList<R0, Rs...>> { static constexpr int value = R0; };
+
+// ---------------------------------------------------------------------------
+// Small DFTs in registers.  Forward uses exp(-2*pi*i/R); INV uses exp(+2*pi*i/R).
+// ---------------------------------------------------------------------------
+template <int R, bool INV> struct DFT;
+
+template <bool INV> struct DFT<2, INV> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    V a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+
+template <bool INV> struct DFT<4, INV> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    V t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+    V t2 = cadd(v[1], v[3]), t3 = rot90<INV>(csub(v[1], v[3]));
+    v[0] = cadd(t0, t2);
+    v[2] = csub(t0, t2);
+    v[1] = cadd(t1, t3);
+    v[3] = csub(t1, t3);
+  }
+};
+
+template <bool INV> struct DFT<8, INV> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    using T = decltype(V::x);
+    const T h = (T)0.70710678118654752440;  // cos(pi/4)
+    V a[4], b[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      a[k] = cadd(v[k], v[k + 4]);
+      b[k] = csub(v[k], v[k + 4]);
+    }
+    // b[k] *= exp(-+ i*pi*k/4)
+    b[1] = INV ? mk<V>(h * (b[1].x - b[1].y), h * (b[1].x + b[1].y))
+               : mk<V>(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x));
+    b[2] = rot90<INV>(b[2]);
+    b[3] = INV ? mk<V>(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y))
+               : mk<V>(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y));
+    DFT<4, INV>::run(a);
+    DFT<4, INV>::run(b);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      v[2 * q] = a[q];
+      v[2 * q + 1] = b[q];
+    }
+  }
+};
+
+template <bool INV> struct DFT<3, INV> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    using T = decltype(V::x);
+    const T s = (T)0.86602540378443864676;  // sin(2*pi/3)
+    V t1 = cadd(v[1], v[2]);
+    V t2 = mk<V>(v[0].x - (T)0.5 * t1.x, v[0].y - (T)0.5 * t1.y);
+    V d = csub(v[1], v[2]);
+    V t3 = rot90<INV>(mk<V>(s * d.x, s * d.y));
+    v[0] = cadd(v[0], t1);
+    v[1] = cadd(t2, t3);
+    v[2] = csub(t2, t3);
+  }
+};
+
+template <bool INV> struct DFT<5, INV> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    using T = decltype(V::x);
+    const T c1 = (T)0.30901699437494742410;   // cos(2*pi/5)
+    const T c2 = (T)-0.80901699437494742410;  // cos(4*pi/5)
+    const T s1 = (T)0.95105651629515357212;   // sin(2*pi/5)
+    const T s2 = (T)0.58778525229247312917;   // sin(4*pi/5)
+    V t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+    V t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+    V a1 = mk<V>(v[0].x + c1 * t1.x + c2 * t2.x, v[0].y + c1 * t1.y + c2 * t2.y);
+    V a2 = mk<V>(v[0].x + c2 * t1.x + c1 * t2.x, v[0].y + c2 * t1.y + c1 * t2.y);
+    V b1 = mk<V>(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+    V b2 = mk<V>(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+    V rb1 = rot90<INV>(b1), rb2 = rot90<INV>(b2);
+    v[0] = cadd(v[0], cadd(t1, t2));
+    v[1] = cadd(a1, rb1);
+    v[4] = csub(a1, rb1);
+    v[2] = cadd(a2, rb2);
+    v[3] = csub(a2, rb2);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Pass recursion.  reg[b*R + r] holds input r of butterfly j = t + b*T.
+// ---------------------------------------------------------------------------
+template <typename V, int N, int E, bool INV, int NS, typename L> struct Passes;
+
+template <typename V, int N, int E, bool INV, int NS, int R, int... Rest>
+struct Passes<V, N, E, INV, NS, RList<R, Rest...>> {
+  static constexpr int T = N / E;
+  static constexpr int NB = E / R;
+  static_assert(E % R == 0, "E must be a multiple of every radix");
+
+  // Runs this pass and all following ones.  After return, reg[b*R_last + r]
+  // holds output position out_pos(t, b, r) of the last pass.
+  __device__ __forceinline__ static void run(V* reg, V* base, int es, int t, const V* tw) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int j = t + b * T;
+      V* v = reg + b * R;
+      if (NS > 1) {
+        const int k = j % NS;
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          V w = tw[(r * k * (N / (NS * R))) % N];
+          v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
+        }
+      }
+      DFT<R, INV>::run(v);
+    }
+    if constexpr (sizeof...(Rest) > 0) {
+      constexpr int R2 = RFirst<RList<Rest...>>::value;
+      __syncthreads();
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        const int j = t + b * T;
+        const int d = (j / NS) * NS * R + (j % NS);
+#pragma unroll
+        for (int r = 0; r < R; ++r) base[(d + r * NS) * es] = reg[b * R + r];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int b = 0; b < E / R2; ++b) {
+#pragma unroll
+        for (int r = 0; r < R2; ++r) reg[b * R2 + r] = base[(t + b * T + r * (N / R2)) * es];
+      }
+      Passes<V, N, E, INV, NS * R, RList<Rest...>>::run(reg, base, es, t, tw);
+    }
+  }
+};
+
+// Output position bookkeeping for the last pass.
+template <int N, int E, int NS, typename L> struct LastPass;
+template <int N, int E, int NS, int R> struct LastPass<N, E, NS, RList<R>> {
+  static constexpr int R_last = R;
+  static constexpr int NS_last = NS;
+};
+template <int N, int E, int NS, int R, int R2, int... Rest>
+struct LastPass<N, E, NS, RList<R, R2, Rest...>> : LastPass<N, E, NS * R, RList<R2, Rest...>> {};
+
+template <typename V, int N, bool INV> struct FFT {
+  using Cfg = FFTCfg<N>;
+  static constexpr int E = Cfg::E;
+  static constexpr int T = N / E;
+  static constexpr int R0 = RFirst<typename Cfg::R>::value;
+  using LP = LastPass<N, E, 1, typename Cfg::R>;
+  static constexpr int RL = LP::R_last;
+  static constexpr int NSL = LP::NS_last;
+
+  // Load the first pass's inputs from shared memory.  Positions >= n_valid are
+  // treated as zero without being read (zero padding).
+  __device__ __forceinline__ static void load(V* reg, const V* base, int es, int t, int n_valid) {
+#pragma unroll
+    for (int b = 0; b < E / R0; ++b) {
+#pragma unroll
+      for (int r = 0; r < R0; ++r) {
+        const int p = t + b * T + r * (N / R0);
+        reg[b * R0 + r] = (p < n_valid) ? base[p * es] : mk<V>(0, 0);
+      }
+    }
+  }
+  // Same, but the caller guarantees n_valid <= N/2 at compile time shape: the
+  // upper half of every first-pass butterfly is zero.
+  __device__ __forceinline__ static void load_half(V* reg, const V* base, int es, int t, int n_valid) {
+#pragma unroll
+    for (int b = 0; b < E / R0; ++b) {
+#pragma unroll
+      for (int r = 0; r < R0; ++r) {
+        const int p = t + b * T + r * (N / R0);
+        reg[b * R0 + r] = (r < R0 / 2 && p < n_valid) ? base[p * es] : mk<V>(0, 0);
+      }
+    }
+  }
+  __device__ __forceinline__ static void run(V* reg, V* base, int es, int t, const V* tw) {
+    Passes<V, N, E, INV, 1, typename Cfg::R>::run(reg, base, es, t, tw);
+  }
+  // Output position of reg[b*RL + r] after run().
+  __device__ __forceinline__ static int out_pos(int t, int b, int r) {
+    const int j = t + b * T;
+    return (j / NSL) * NSL * RL + (j % NSL) + r * NSL;
+  }
+  // Store all outputs (natural order) back to shared memory.  Caller syncs.
+  __device__ __forceinline__ static void store(const V* reg, V* base, int es, int t) {
+#pragma unroll
+    for (int b = 0; b < E / RL; ++b)
+#pragma unroll
+      for (int r = 0; r < RL; ++r) base[out_pos(t, b, r) * es] = reg[b * RL + r];
+  }
+};
+
+}  // namespace marie

@@ -1,0 +1,3 @@
+// FP64 instantiation of the matvec passes.
+#include "matvec_launch.cuh"
+template struct marie::MatvecLaunch<double>;

@@ -1,0 +1,105 @@
+// Internal plan state shared by the C-ABI translation units.
+#pragma once
+#include <functional>
+#include <vector>
+
+#include "common.cuh"
+#include "matvec_kernels.cuh"
+
+struct marie_plan {
+  marie::Dims d{};
+  int precision = MARIE_FP64;
+  long long nrhs_max = 1;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+
+  // Operator, full 2L x 2M x 2N x 6 layout, pre-scaled by 1/(8LMN).
+  double2* fN64 = nullptr;
+  float2* fN32 = nullptr;
+  bool has_op = false;
+
+  // Twiddle tables exp(-2*pi*i*k/n) for the three padded axis lengths.
+  double2* tw64[3] = {nullptr, nullptr, nullptr};
+  float2* tw32[3] = {nullptr, nullptr, nullptr};
+
+  // Spectra workspaces (A: 3 x N x M x 2L, B: 3 x N x 2M x 2L per rhs).
+  void* wsA = nullptr;
+  void* wsB = nullptr;
+  size_t ws_bytes_A = 0, ws_bytes_B = 0;
+
+  // Optional per-pass timing of the matvec (events recorded between passes).
+  bool profile = false;
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  float pass_ms[5] = {0, 0, 0, 0, 0};
+  long long profiled = 0;
+
+  // Pinned host staging for small scalars (reductions, Hessenberg columns).
+  double* pinned = nullptr;
+  size_t pinned_len = 0;
+
+  long long elems_A() const { return 3LL * d.Lp * d.M * d.N; }
+  long long elems_B() const { return 3LL * d.Lp * d.Mp * d.N; }
+};
+
+namespace marie {
+
+// Device buffer that is released on scope exit (stream-ordered).
+struct DBuf {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { if (p) cudaFreeAsync(p, s); }
+  int alloc(size_t bytes, cudaStream_t st);
+  template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// True when ptr is device (or managed) memory of the current device.
+bool is_device_ptr(const void* ptr);
+
+// Input view: device pointer to `bytes` of data, copying from host if needed.
+int stage_in(const void* user, size_t bytes, cudaStream_t st, DBuf& tmp, const void** dev);
+// Output view: device pointer to write to; finish_out copies back to host.
+int stage_out(void* user, size_t bytes, cudaStream_t st, DBuf& tmp, void** dev);
+int finish_out(void* user, const void* dev, size_t bytes, cudaStream_t st);
+
+int ensure_workspace(marie_plan* p, int prec, long long nrhs);
+int ensure_pinned(marie_plan* p, size_t n_doubles);
+
+// Build the inverse map inv[g] = k for 1-based idx[k]; -1 elsewhere.  Fails on
+// out-of-range or repeated indices.
+int build_inverse_index(marie_plan* p, const int64_t* idx_dev, long long n, int* inv);
+
+// One circulant matvec (nrhs columns of length n, device pointers).
+int run_matvec(marie_plan* p, int prec, const double2* J, double2* out, long long n, int nrhs, const int* inv,
+               const Prologue& pro, const Epilogue& ep);
+
+// Scale fN by 1/(8LMN) into the plan's FP64/FP32 copies (fN_dev: full layout).
+int install_operator(marie_plan* p, const double2* fN_dev);
+
+// Per-DOF coefficient arrays for mv_AN: (a, b) or (pre, a) for the adjoint.
+// mode 0: a = Gram*Mr, b = Mc      mode 1: pre = Mc, a = Gram*conj(Mr)
+int build_coefficients(marie_plan* p, const int64_t* idx_dev, long long n, const double2* Mr,
+                       const double2* Mc, double Gram, int mode, double2* a, double2* b);
+
+// Deterministic reductions and vector kernels (krylov.cu).
+int dev_norm2(marie_plan* p, const double2* x, long long n, double* out_host);
+
+// A linear operator on device vectors of length n.
+using DevOp = std::function<int(const double2* x, double2* y)>;
+
+struct GmresResult {
+  int flag = 1;
+  double relres = 0;
+  int iter[2] = {0, 0};
+  std::vector<double> resvec;
+};
+
+// pgmres semantics (pgmres.m:70-181) on device vectors.
+int gmres(marie_plan* p, const DevOp& A, const DevOp* L1, const DevOp* L2, const DevOp* R1, const DevOp* R2,
+          const double2* b, long long n, int restart, double tol, int maxit, const double2* x0, double2* x,
+          GmresResult& res);
+
+}  // namespace marie

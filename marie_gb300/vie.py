@@ -1,0 +1,440 @@
+"""Reference-facing host API of the J-VIE solve path.
+
+Mirrors the MATLAB functions of MARIE that this path replaces, with the same
+argument order, defaults and return tuples:
+
+    getOPERATORS(r, f, op, type, singular)       src_vie/src_operators/getOPERATORS.m:1
+    mv_AN(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, GPU_flag)
+                                                 src_vie/src_mvp/mv_AN.m:1
+    mv_L(JIn0, fN, r, Gram, idx, GPU_flag)       src_vie/src_mvp/mv_L.m:1
+    pgmres(A, b, restart, tol, maxit, L1, L2, R1, R2, x0)
+                                                 src_numeric/src_iterative/pgmres.m:70
+    JVIE_Solver(Einc, e_r, r, freq, fN, tol, form, solver, precond, max_it,
+                inner_it, outer_it, ritz, gpu_flag, logfile)
+                                                 src_vie/src_solver/JVIE_Solver.m:1
+    E_field_Nop(J, fN, Gram, freq, Einc, GPU_flag)
+                                                 src_vie/src_fields/src_op/E_field_Nop.m:1
+    PlaneWave_Excitation(r, k, omega_mu, Eo)     src_vie/src_fields/src_excitations/PlaneWave_Excitation.m:1
+    Dipole_Excitation(r, k, DipJ, DipCoord)      src_vie/src_fields/src_excitations/Dipole_Excitation.m:1
+
+Grid arrays are (L, M, N[, 3 or 6]) in column-major order, exactly the
+reference's MATLAB arrays: numpy arrays (host; copied to the device per call,
+like gpuArray/gather) or torch CUDA tensors with column-major strides (used in
+place).  idx vectors are 1-based.  All compute runs in libmarie_vie.so on the
+GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import MARIE_FP32, MARIE_FP64, MARIE_MIXED, check
+
+try:  # torch is only needed for device-resident arrays
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+MU0 = 4 * math.pi * 1e-7
+C0 = 299792458.0
+EPS0 = 1.0 / C0**2 / MU0
+
+_PREC = {"fp64": MARIE_FP64, "fp32": MARIE_FP32, "mixed": MARIE_MIXED,
+         64: MARIE_FP64, 32: MARIE_FP32, 96: MARIE_MIXED}
+
+
+def EMconstants(freq):
+    """EMconstants.m:13-20."""
+    omega = 2 * math.pi * freq
+    return dict(mu=MU0, co=C0, eo=EPS0, omega=omega, lambda_=C0 / freq, ko=2 * math.pi * freq / C0,
+                omega_mu=omega * MU0, eta=3.767303134617706e+002)
+
+
+# ---------------------------------------------------------------------------
+# array plumbing
+# ---------------------------------------------------------------------------
+def _is_cuda(a) -> bool:
+    return torch is not None and isinstance(a, torch.Tensor) and a.is_cuda
+
+
+def _colmajor_cuda(t, dtype):
+    """Column-major contiguous CUDA tensor of the same shape (no copy if already)."""
+    t = t.to(dtype)
+    if t.dim() <= 1:
+        return t.contiguous()
+    rev = list(range(t.dim() - 1, -1, -1))
+    return t.permute(*rev).contiguous().permute(*rev)
+
+
+def _in(a, dtype=np.complex128):
+    """Pointer + keep-alive for an input array (host numpy or CUDA torch)."""
+    if _is_cuda(a):
+        tdt = {np.complex128: torch.complex128, np.float64: torch.float64, np.int64: torch.int64}[dtype]
+        t = _colmajor_cuda(a, tdt)
+        return C.c_void_p(t.data_ptr()), t
+    arr = np.asfortranarray(np.asarray(a, dtype=dtype))
+    return C.c_void_p(arr.ctypes.data), arr
+
+
+def _out(shape, like_cuda: bool, dtype=np.complex128):
+    if like_cuda:
+        tdt = {np.complex128: torch.complex128, np.float64: torch.float64}[dtype]
+        rev = tuple(reversed(shape))
+        t = torch.empty(rev, dtype=tdt, device="cuda").permute(*range(len(shape) - 1, -1, -1))
+        return C.c_void_p(t.data_ptr()), t
+    arr = np.empty(shape, dtype=dtype, order="F")
+    return C.c_void_p(arr.ctypes.data), arr
+
+
+def _sync():
+    if torch is not None and torch.cuda.is_available():
+        torch.cuda.current_stream().synchronize()
+
+
+# ---------------------------------------------------------------------------
+# the operator held on the device (gpuArray(fN) in JVIE_Solver.m:271)
+# ---------------------------------------------------------------------------
+class Operator:
+    """A plan for an L x M x N grid holding the FFT-of-circulant operator fN on the
+    device, in FP64 and/or FP32 (precision 'fp64', 'fp32' or 'mixed')."""
+
+    def __init__(self, L, M, N, precision="fp64", nrhs_max=1):
+        self.lib = _lib.load()
+        self.L, self.M, self.N = int(L), int(M), int(N)
+        self.precision = _PREC[precision]
+        ph = C.c_void_p()
+        check(self.lib.marie_plan_create(self.L, self.M, self.N, self.precision, int(nrhs_max), None, C.byref(ph)))
+        self._plan = ph
+        self.dx = None
+        self.freq = None
+
+    @property
+    def plan(self):
+        if self._plan is None:
+            raise RuntimeError("operator closed")
+        return self._plan
+
+    @classmethod
+    def from_array(cls, fN, precision="fp64", nrhs_max=1):
+        Lf, Mf, Nf, q = fN.shape
+        if q != 6 or Lf % 2 or Mf % 2 or Nf % 2:
+            raise ValueError("fN must be 2L x 2M x 2N x 6")
+        op = cls(Lf // 2, Mf // 2, Nf // 2, precision, nrhs_max)
+        ptr, keep = _in(fN)
+        check(op.lib.marie_set_operator(op.plan, ptr, Lf, Mf, Nf))
+        del keep
+        return op
+
+    @classmethod
+    def assemble(cls, L, M, N, dx, freq, precision="fp64", singular="DIRECTFN", singular_values=None, nrhs_max=1):
+        """getOPERATORS(r, f, 'N') computed straight into the plan (no host copy)."""
+        op = cls(L, M, N, precision, nrhs_max)
+        sv, keep = _singular_arg(singular, singular_values)
+        check(op.lib.marie_plan_assemble(op.plan, float(dx), float(freq), sv[0], sv[1]))
+        op.dx, op.freq = dx, freq
+        return op
+
+    def to_array(self):
+        """The FP64 operator as a 2L x 2M x 2N x 6 numpy array."""
+        ptr, arr = _out((2 * self.L, 2 * self.M, 2 * self.N, 6), False)
+        check(self.lib.marie_get_plan_operator(self.plan, ptr))
+        return arr
+
+    def close(self):
+        if self._plan is not None:
+            self.lib.marie_plan_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _singular_arg(singular, values):
+    if values is not None:
+        v = np.asarray(values, dtype=np.complex128).reshape(5)
+        arr = np.ascontiguousarray(v)
+        return (b"U", C.c_void_p(arr.ctypes.data)), arr
+    if singular not in ("DIRECTFN", "D", "DEMCEM"):
+        raise ValueError("singular must be 'DIRECTFN' (or pass singular_values)")
+    return (b"D", None), None
+
+
+def _operator_for(fN, precision):
+    if isinstance(fN, Operator):
+        return fN, False
+    return Operator.from_array(fN, precision=precision), True
+
+
+# ---------------------------------------------------------------------------
+# getOPERATORS
+# ---------------------------------------------------------------------------
+def getOPERATORS(r, f, op="N", type="FFTofC", singular="DIRECTFN", singular_values=None):
+    """getOPERATORS.m:1-127 for op 'N'.  type 'FFTofC' (default), 'C' or 'T'.
+
+    singular='DIRECTFN' evaluates the weakly singular self/edge/vertex integrals
+    with a converged device quadrature; singular_values = [ST, EAc, EAo, VAc,
+    VAo] overrides them (e.g. with the reference's own DIRECTFN values)."""
+    lib = _lib.load()
+    if op != "N":
+        raise NotImplementedError("only the N operator is on this path")
+    L, M, N = r.shape[:3]
+    t = {"FFTofC": b"F", "C": b"C", "T": b"T"}[type]
+    shape = (L, M, N, 6) if t == b"T" else (2 * L, 2 * M, 2 * N, 6)
+    rp, rk = _in(r, np.float64)
+    op_ptr, out = _out(shape, _is_cuda(r))
+    sv, keep = _singular_arg(singular, singular_values)
+    check(lib.marie_get_operators(rp, L, M, N, float(f), b"N", t, sv[0], sv[1], op_ptr))
+    return out
+
+
+def singular_integrals(ko, dx):
+    """[ST, EAc, EAo, VAc, VAo] (complex) for wavenumber ko and voxel edge dx."""
+    lib = _lib.load()
+    out = np.zeros(10)
+    check(lib.marie_singular_integrals(float(ko), float(dx), C.c_void_p(out.ctypes.data)))
+    return out[0::2] + 1j * out[1::2]
+
+
+# ---------------------------------------------------------------------------
+# matvecs
+# ---------------------------------------------------------------------------
+def mv_AN(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, GPU_flag=1, precision="fp64"):
+    """mv_AN.m: 'notransp' -> Gram*Mr*J - Mc*N J ; 'transp' -> its Hermitian adjoint.
+
+    JIn0 may be a vector (n,) or a batch (n, nrhs) of columns."""
+    if transp_flag not in ("notransp", "transp"):
+        raise ValueError("transp_flag must be 'notransp' or 'transp'")
+    prec = _PREC[precision]
+    opr, tmp = _operator_for(fN, "mixed" if prec == MARIE_FP32 else "fp64")
+    try:
+        cuda = _is_cuda(JIn0)
+        n = JIn0.shape[0]
+        nrhs = 1 if JIn0.ndim == 1 else JIn0.shape[1]
+        jp, jk = _in(JIn0)
+        mrp, mrk = _in(Mr)
+        mcp, mck = _in(Mc)
+        ip, ik = _in(idx, np.int64)
+        op_, out = _out(JIn0.shape, cuda)
+        check(opr.lib.marie_mv_AN(opr.plan, jp, mrp, mcp, float(Gram), 1 if transp_flag == "transp" else 0,
+                                  ip, n, op_, nrhs, prec))
+        return out
+    finally:
+        if tmp:
+            opr.close()
+
+
+def mv_L(JIn0, fN, r, Gram, idx, GPU_flag=1, precision="fp64"):
+    """mv_L.m: crop(N J) - Gram*J on the entries idx."""
+    prec = _PREC[precision]
+    opr, tmp = _operator_for(fN, "mixed" if prec == MARIE_FP32 else "fp64")
+    try:
+        cuda = _is_cuda(JIn0)
+        n = JIn0.shape[0]
+        nrhs = 1 if JIn0.ndim == 1 else JIn0.shape[1]
+        jp, jk = _in(JIn0)
+        ip, ik = _in(idx, np.int64)
+        op_, out = _out(JIn0.shape, cuda)
+        check(opr.lib.marie_mv_L(opr.plan, jp, float(Gram), ip, n, op_, nrhs, prec))
+        return out
+    finally:
+        if tmp:
+            opr.close()
+
+
+def E_field_Nop(J, fN, Gram, freq, Einc=None, GPU_flag=1, precision="fp64"):
+    """E_field_Nop.m:59-84: Etot = Einc + (N J - Gram J)/(Gram j omega eps0)."""
+    opr, tmp = _operator_for(fN, "fp64")
+    try:
+        if Einc is not None and not np.any(np.asarray(J.cpu() if _is_cuda(J) else J)):
+            return Einc
+        jp, jk = _in(J)
+        if Einc is not None:
+            ep, ek = _in(Einc)
+        else:
+            ep, ek = None, None
+        op_, out = _out(tuple(J.shape), _is_cuda(J))
+        check(opr.lib.marie_e_field_nop(opr.plan, jp, float(Gram), float(freq), ep, op_, _PREC[precision]))
+        return out
+    finally:
+        if tmp:
+            opr.close()
+
+
+# ---------------------------------------------------------------------------
+# pgmres with function-handle operators
+# ---------------------------------------------------------------------------
+class _CudaVec:
+    """__cuda_array_interface__ view of a raw device vector of complex128."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<c16", "data": (ptr, False), "version": 3,
+                                         "strides": None}
+
+
+def _wrap_handle(fn, host_mode):
+    def cb(ctx, x, y, n):
+        try:
+            xt = torch.as_tensor(_CudaVec(x, n), device="cuda")
+            yt = torch.as_tensor(_CudaVec(y, n), device="cuda")
+            if host_mode:
+                res = np.asarray(fn(xt.cpu().numpy()), dtype=np.complex128).reshape(-1)
+                yt.copy_(torch.from_numpy(res))
+            else:
+                res = fn(xt)
+                yt.copy_(res.reshape(-1).to(torch.complex128))
+            torch.cuda.current_stream().synchronize()
+            return 0
+        except Exception as e:  # surfaced as a status; the message is kept
+            _wrap_handle.last_exc = e
+            return -1
+
+    return _lib.OP_FN(cb)
+
+
+_wrap_handle.last_exc = None
+_vec_plan = None
+
+
+def _vector_plan():
+    global _vec_plan
+    if _vec_plan is None:
+        _vec_plan = Operator(4, 4, 4, "fp64")
+    return _vec_plan
+
+
+def pgmres(A, b, restart=50, tol=1e-3, maxit=10, L1=None, L2=None, R1=None, R2=None, x0=None):
+    """pgmres.m:70-181 on the device.  A, L1, L2, R1, R2 are function handles
+    (preconditioners are applied as products, like the reference).  With a
+    numpy b the handles receive and return numpy vectors; with a CUDA tensor b
+    they receive and return CUDA tensors.  Returns (x, flag, relres, iter, resvec)."""
+    if restart is None:
+        restart = 50
+    if tol is None:
+        tol = 1e-3
+    if maxit is None:
+        maxit = 10
+    host = not _is_cuda(b)
+    opr = _vector_plan()
+    lib = opr.lib
+    n = b.shape[0]
+    cbs = [_wrap_handle(A, host)]
+    nulls = []
+    for h in (L1, L2, R1, R2):
+        if h is None:
+            nulls.append(_lib.OP_FN())
+        else:
+            f = _wrap_handle(h, host)
+            cbs.append(f)
+            nulls.append(f)
+    bp, bk = _in(b)
+    x0p, x0k = _in(x0) if x0 is not None else (None, None)
+    xp, x = _out((n,), not host)
+    flag = C.c_int()
+    relres = C.c_double()
+    it = (C.c_int * 2)()
+    cap = restart * maxit + 1
+    resvec = np.zeros(cap)
+    rlen = C.c_int64()
+    _wrap_handle.last_exc = None
+    st = lib.marie_pgmres(opr.plan, cbs[0], None, bp, n, int(restart), float(tol), int(maxit),
+                          nulls[0], None, nulls[1], None, nulls[2], None, nulls[3], None,
+                          x0p, xp, C.byref(flag), C.byref(relres), it, resvec.ctypes.data_as(_lib._dp), cap,
+                          C.byref(rlen))
+    if st != 0 and _wrap_handle.last_exc is not None:
+        raise _wrap_handle.last_exc
+    check(st)
+    return x, flag.value, relres.value, [it[0], it[1]], resvec[:rlen.value]
+
+
+# ---------------------------------------------------------------------------
+# JVIE_Solver
+# ---------------------------------------------------------------------------
+def JVIE_Solver(Einc, e_r, r, freq, fN, tol=None, form=None, solver="G", precond=None, max_it=None, inner_it=None,
+                outer_it=None, ritz=None, gpu_flag=1, logfile=None, precision=None):
+    """JVIE_Solver.m with solver 'G' (restarted GMRES) on the device.
+
+    fN is an Operator (or a 2L x 2M x 2N x 6 array).  precision: 'fp64' (the
+    reference arithmetic), 'fp32', or 'mixed' (FP32 circulant matvec inside FP64
+    GMRES with FP64 iterative refinement); defaults to the Operator's.
+    Returns (Je, flag, relres, iter, resvec, solvert)."""
+    if solver not in ("G", None):
+        raise NotImplementedError("only solver 'G' (pgmres) is on this path")
+    tol = 1e-3 if tol is None else tol
+    form = 2 if form is None else form
+    pc = {None: b"\0", 0: b"\0", "L": b"L", "R": b"R"}.get(precond, b"\0")
+    inner_it = 50 if inner_it is None or inner_it < 1 else inner_it
+    outer_it = 200 if outer_it is None or outer_it < 1 else outer_it
+    if isinstance(fN, Operator):
+        opr, tmp = fN, False
+        if precision is not None and _PREC[precision] != opr.precision:
+            raise ValueError("precision differs from the Operator's; build the Operator with it")
+    else:
+        opr, tmp = Operator.from_array(fN, precision=precision or "fp64"), True
+    try:
+        L, M, N = e_r.shape
+        dx = float(r[1, 0, 0, 0] - r[0, 0, 0, 0]) if not _is_cuda(r) else float((r[1, 0, 0, 0] - r[0, 0, 0, 0]).item())
+        cuda = _is_cuda(Einc)
+        ep, ek = _in(Einc)
+        erp, erk = _in(e_r)
+        jp, Je = _out((L, M, N, 3), cuda)
+        flag = C.c_int()
+        relres = C.c_double()
+        it = (C.c_int * 2)()
+        cap = 1 + inner_it * outer_it * 4
+        resvec = np.zeros(cap)
+        rlen = C.c_int64()
+        solvert = C.c_double()
+        check(opr.lib.marie_jvie_solve(opr.plan, ep, erp, dx, float(freq), int(form), pc, float(tol), int(inner_it),
+                                       int(outer_it), jp, C.byref(flag), C.byref(relres), it,
+                                       resvec.ctypes.data_as(_lib._dp), cap, C.byref(rlen), C.byref(solvert)))
+        return Je, flag.value, relres.value, [it[0], it[1]], resvec[:min(rlen.value, cap)], solvert.value
+    finally:
+        if tmp:
+            opr.close()
+
+
+# ---------------------------------------------------------------------------
+# excitations
+# ---------------------------------------------------------------------------
+def PlaneWave_Excitation(r, k, omega_mu, Eo):
+    """PlaneWave_Excitation.m:39-95 -> (E, H), voxel-averaged plane wave."""
+    lib = _lib.load()
+    L, M, N = r.shape[:3]
+    rp, rk = _in(r, np.float64)
+    kk = np.ascontiguousarray(np.asarray(k, dtype=np.float64).reshape(3))
+    eo = np.asarray(Eo, dtype=np.complex128).reshape(3)
+    eov = np.ascontiguousarray(np.stack([eo.real, eo.imag], axis=1).reshape(-1))
+    ptr, E = _out((L, M, N, 3), _is_cuda(r))
+    check(lib.marie_plane_wave(rp, L, M, N, C.c_void_p(kk.ctypes.data), C.c_void_p(eov.ctypes.data), ptr))
+    Ho = np.cross(kk, eo) / omega_mu
+    c = int(np.argmax(np.abs(eo)))
+    base = E[..., c] / eo[c]
+    if _is_cuda(r):
+        H = torch.stack([base * complex(Ho[i]) for i in range(3)], dim=3)
+    else:
+        H = np.stack([base * Ho[i] for i in range(3)], axis=3)
+    return E, H
+
+
+def Dipole_Excitation(r, k, DipJ, DipCoord):
+    """Dipole_Excitation.m:39-54 (E field of electric dipoles via E_field_DGF.m).
+    DipJ: (ndip, 3) complex moments, DipCoord: (ndip, 3) positions.  Returns E
+    (the magnetic field is not on this path)."""
+    lib = _lib.load()
+    L, M, N = r.shape[:3]
+    Jd = np.asarray(DipJ, dtype=np.complex128).reshape(-1, 3)
+    pos = np.ascontiguousarray(np.asarray(DipCoord, dtype=np.float64).reshape(-1, 3))
+    jv = np.ascontiguousarray(np.stack([Jd.real, Jd.imag], axis=2).reshape(-1))
+    rp, rk = _in(r, np.float64)
+    ptr, E = _out((L, M, N, 3), _is_cuda(r))
+    check(lib.marie_dipole_field(rp, L, M, N, float(k), C.c_void_p(jv.ctypes.data), C.c_void_p(pos.ctypes.data),
+                                 Jd.shape[0], ptr))
+    return E

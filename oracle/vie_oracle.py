@@ -1,0 +1,512 @@
+"""numpy/scipy restatement of the reference J-VIE path (TEST INFRASTRUCTURE ONLY).
+
+Arrays follow the reference's MATLAB layout: numpy arrays of shape
+(L, M, N[, 3 or 6]) addressed in Fortran (column-major) order; idx vectors are
+1-based.  Every function cites the reference file:line it restates.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.fft
+import scipy.special as sp
+
+# ---------------------------------------------------------------------------
+# constants: src_vie/src_solver/EMconstants.m:13-20
+# ---------------------------------------------------------------------------
+MU0 = 4 * np.pi * 1e-7
+C0 = 299792458.0
+EPS0 = 1.0 / C0**2 / MU0
+
+
+def EMconstants(freq):
+    omega = 2 * np.pi * freq
+    lam = C0 / freq
+    ko = 2 * np.pi / lam
+    return dict(mu=MU0, co=C0, eo=EPS0, omega=omega, ko=ko, omega_mu=omega * MU0)
+
+
+def _fftn(x, s, workers):
+    return scipy.fft.fftn(x, s=s, axes=(0, 1, 2), workers=workers)
+
+
+def _ifftn(x, workers):
+    return scipy.fft.ifftn(x, axes=(0, 1, 2), workers=workers)
+
+
+# ---------------------------------------------------------------------------
+# matvecs
+# ---------------------------------------------------------------------------
+def mv_AN(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, workers=None):
+    """src_vie/src_mvp/mv_AN.m:40-146 ('notransp' :101-131, 'transp' :65-99)."""
+    LfN, MfN, NfN, _ = fN.shape
+    L, M, N = Mr.shape
+    s = (LfN, MfN, NfN)
+    flat = np.zeros(L * M * N * 3, dtype=complex)
+    flat[np.asarray(idx) - 1] = JIn0
+    JIn = flat.reshape((L, M, N, 3), order="F")
+    JOut = np.zeros((L, M, N, 3), dtype=complex)
+    sym = ((0, 1, 2), (1, 3, 4), (2, 4, 5))  # x->(1,2,3), y->(2,4,5), z->(3,5,6)
+    acc = [0, 0, 0]
+    if transp_flag == "transp":
+        Mcc = np.conj(Mc)
+        for c in range(3):
+            fJ = _fftn(np.conj(Mcc * JIn[:, :, :, c]), s, workers)
+            for o in range(3):
+                acc[o] = acc[o] + fN[:, :, :, sym[c][o]] * fJ
+        for o in range(3):
+            Jo = _ifftn(acc[o], workers)
+            JOut[:, :, :, o] = Gram * np.conj(Mr) * JIn[:, :, :, o] - np.conj(Jo[:L, :M, :N])
+    elif transp_flag == "notransp":
+        for c in range(3):
+            fJ = _fftn(JIn[:, :, :, c], s, workers)
+            for o in range(3):
+                acc[o] = acc[o] + fN[:, :, :, sym[c][o]] * fJ
+        for o in range(3):
+            Jo = _ifftn(acc[o], workers)
+            JOut[:, :, :, o] = Gram * Mr * JIn[:, :, :, o] - Mc * Jo[:L, :M, :N]
+    else:
+        raise ValueError("transp_flag must be 'transp' or 'notransp'")
+    return JOut.reshape(-1, order="F")[np.asarray(idx) - 1]
+
+
+def mv_L(JIn0, fN, r_shape, Gram, idx, workers=None):
+    """src_vie/src_mvp/mv_L.m:30-97: crop(N J) - Gram J on the entries idx."""
+    LfN, MfN, NfN, _ = fN.shape
+    L, M, N = r_shape[:3]
+    flat = np.zeros(L * M * N * 3, dtype=complex)
+    flat[np.asarray(idx) - 1] = JIn0
+    JIn = flat.reshape((L, M, N, 3), order="F")
+    JOut = np.zeros((L, M, N, 3), dtype=complex)
+    sym = ((0, 1, 2), (1, 3, 4), (2, 4, 5))
+    acc = [0, 0, 0]
+    for c in range(3):
+        fJ = _fftn(JIn[:, :, :, c], (LfN, MfN, NfN), workers)
+        for o in range(3):
+            acc[o] = acc[o] + fN[:, :, :, sym[c][o]] * fJ
+    for o in range(3):
+        Jo = _ifftn(acc[o], workers)
+        JOut[:, :, :, o] = Jo[:L, :M, :N] - Gram * JIn[:, :, :, o]
+    return JOut.reshape(-1, order="F")[np.asarray(idx) - 1]
+
+
+def E_field_Nop(J, fN, Gram, freq, Einc=None, workers=None):
+    """src_vie/src_fields/src_op/E_field_Nop.m:59-84."""
+    if Einc is None:
+        Einc = np.zeros_like(J)
+    if not np.any(J):
+        return Einc
+    omega = 2 * np.pi * freq
+    L, M, N, _ = J.shape
+    idx = np.arange(1, 3 * L * M * N + 1)
+    E = mv_L(J.reshape(-1, order="F"), fN, J.shape, Gram, idx, workers)
+    E = E.reshape((L, M, N, 3), order="F")
+    return Einc + E / (Gram * 1j * omega * EPS0)
+
+
+# ---------------------------------------------------------------------------
+# GMRES: src_numeric/src_iterative/pgmres.m:70-181, pgmres_iter.m:22-150
+# ---------------------------------------------------------------------------
+def pgmres_iter(A, x, r, m, L1, L2, R1, R2, tol):
+    n = r.shape[0]
+    V = np.zeros((n, m + 1), dtype=complex)
+    V[:, 0] = r / np.linalg.norm(r)
+    H = np.zeros((m + 1, m), dtype=complex)
+    resvec = np.zeros(m)
+    y = res = None
+    k = 0
+    for k in range(1, m + 1):
+        w = V[:, k - 1]
+        if R1 is not None:
+            w = R1(w)
+        if R2 is not None:
+            w = R2(w)
+        w = A(w)
+        if L1 is not None:
+            w = L1(w)
+        if L2 is not None:
+            w = L2(w)
+        H[:k, k - 1] = V[:, :k].conj().T @ w          # pgmres_iter.m:106 (CGS)
+        w = w - V[:, :k] @ H[:k, k - 1]              # :107
+        H[k, k - 1] = np.linalg.norm(w)              # :109
+        with np.errstate(divide="ignore", invalid="ignore"):
+            V[:, k] = w / H[k, k - 1]                # :110
+        rhs = np.zeros(k + 1, dtype=complex)
+        rhs[0] = np.linalg.norm(r)
+        Hc = H[:k + 1, :k]
+        y = np.linalg.lstsq(Hc, rhs, rcond=None)[0]  # :118  y = Hc \ rhs
+        res = rhs - Hc @ y
+        resvec[k - 1] = np.linalg.norm(res)
+        if resvec[k - 1] < tol:
+            break
+    resvec = resvec[:k]
+    xupd = V[:, :k] @ y
+    if R1 is not None:
+        xupd = R1(xupd)
+    if R2 is not None:
+        xupd = R2(xupd)
+    x = x + xupd
+    with np.errstate(invalid="ignore"):
+        r = V[:, :k + 1] @ res
+    return x, r, k, resvec
+
+
+def pgmres(A, b, restart=50, tol=1e-3, maxit=10, L1=None, L2=None, R1=None, R2=None, x0=None):
+    """Returns (x, flag, relres, iter, resvec) like pgmres.m."""
+    if x0 is None:
+        x0 = np.zeros_like(b)
+    r = b - A(x0) if np.count_nonzero(x0) else b.copy()
+    bp = b.copy()
+    if L1 is not None:
+        r = L1(r)
+        bp = L1(bp)
+    if L2 is not None:
+        r = L2(r)
+        bp = L2(bp)
+    bnorm = np.linalg.norm(bp)
+    resvec = [np.linalg.norm(r) / bnorm]
+    outit = 0
+    x = x0.copy()
+    p = 0
+    while resvec[-1] > tol and outit < maxit:
+        outit += 1
+        x, r, p, rin = pgmres_iter(A, x, r, restart, L1, L2, R1, R2, tol * bnorm)
+        resvec.extend(list(rin / bnorm))
+    relres = np.linalg.norm(b - A(x)) / np.linalg.norm(b)
+    flag = 0 if relres <= tol else 1
+    return x, flag, relres, [p, outit], np.array(resvec)
+
+
+# ---------------------------------------------------------------------------
+# JVIE_Solver (solver 'G'): src_vie/src_solver/JVIE_Solver.m:71-156,176-299,513-514
+# ---------------------------------------------------------------------------
+def jvie_setup(Einc, e_r, r, freq, form=2):
+    em = EMconstants(freq)
+    Mr = e_r.astype(complex).copy()
+    Mc = e_r - 1.0
+    dx = r[1, 0, 0, 0] - r[0, 0, 0, 0]
+    Gram = dx**3
+    L, M, N = e_r.shape
+    nD = L * M * N
+    idxS = np.nonzero(np.abs(Mc.reshape(-1, order="F")) > 1e-12)[0] + 1
+    idxS3 = np.concatenate([idxS, nD + idxS, 2 * nD + idxS])
+    tau = 1j * em["omega"] * em["eo"] * Mc
+    tau3 = np.concatenate([tau.reshape(-1, order="F")] * 3)
+    Vrhs = Gram * tau3[idxS3 - 1] * Einc.reshape(-1, order="F")[idxS3 - 1]
+    if form != 1:
+        Mc = Mc / Mr
+        mr = Mr.reshape(-1, order="F")[idxS - 1]
+        Vrhs = Vrhs / np.concatenate([mr, mr, mr])
+        Mr = Mr / Mr
+    return dict(Mr=Mr, Mc=Mc, Gram=Gram, idxS3=idxS3, Vrhs=Vrhs, shape=(L, M, N))
+
+
+def JVIE_Solver(Einc, e_r, r, freq, fN, tol=1e-3, form=2, precond=0, inner_it=50, outer_it=200, workers=None):
+    if tol < 1e-15 or tol >= 1:
+        tol = 1e-3
+    S = jvie_setup(Einc, e_r, r, freq, form)
+    Mr, Mc, Gram, idx = S["Mr"], S["Mc"], S["Gram"], S["idxS3"]
+
+    def fA(J):
+        return mv_AN(J, fN, Mr, Mc, Gram, "notransp", idx, workers)
+
+    def fP(J):
+        return mv_AN(J, fN, 1.0 / Mr, 1.0 / Mr - 1.0, Gram, "notransp", idx, workers)
+
+    if precond == "R":
+        vsol, flag, relres, it, resvec = pgmres(fA, S["Vrhs"], inner_it, tol, outer_it, None, None, fP)
+    elif precond == "L":
+        vsol, flag, relres, it, resvec = pgmres(fA, S["Vrhs"], inner_it, tol, outer_it, fP)
+    else:
+        vsol, flag, relres, it, resvec = pgmres(fA, S["Vrhs"], inner_it, tol, outer_it)
+    L, M, N = S["shape"]
+    Je = np.zeros(L * M * N * 3, dtype=complex)
+    Je[idx - 1] = vsol
+    return Je.reshape((L, M, N, 3), order="F"), flag, relres, it, resvec
+
+
+# ---------------------------------------------------------------------------
+# excitations
+# ---------------------------------------------------------------------------
+def PlaneWave_Excitation(r, k, omega_mu, Eo):
+    """src_vie/src_fields/src_excitations/PlaneWave_Excitation.m:39-95 (E and H)."""
+    L, M, N, _ = r.shape
+    dx = r[1, 0, 0, 0] - r[0, 0, 0, 0]
+    dy = r[0, 1, 0, 1] - r[0, 0, 0, 1]
+    dz = r[0, 0, 1, 2] - r[0, 0, 0, 2]
+    k = np.asarray(k, dtype=float)
+    Eo = np.asarray(Eo, dtype=complex)
+    Ho = (1 / omega_mu) * np.cross(k, Eo)
+    fac = []
+    for a, d in zip(range(3), (dx, dy, dz)):
+        if k[a] != 0:
+            fac.append(np.exp(-1j * k[a] * r[:, :, :, a]) * (np.exp(-1j * k[a] * d / 2) - np.exp(1j * k[a] * d / 2))
+                       / (-1j * k[a]))
+        else:
+            fac.append(d * np.ones((L, M, N)))
+    Eexc = fac[0] * fac[1] * fac[2]
+    E = np.stack([Eo[i] * Eexc for i in range(3)], axis=3) / (dx * dy * dz)
+    H = np.stack([Ho[i] * Eexc for i in range(3)], axis=3) / (dx * dy * dz)
+    return E, H
+
+
+def E_field_DGF(J, Icoord, Ocoord, ko):
+    """src_vie/src_fields/src_dgf/E_field_DGF.m:36-99; J is Ni x 3, coords are N x 3."""
+    omega = ko * C0
+    J = np.asarray(J, dtype=complex).reshape(-1, 3)
+    X = Ocoord[:, 0:1] - Icoord[None, :, 0]
+    Y = Ocoord[:, 1:2] - Icoord[None, :, 1]
+    Z = Ocoord[:, 2:3] - Icoord[None, :, 2]
+    R2 = X * X + Y * Y + Z * Z
+    R = np.sqrt(R2)
+    R3 = R * R2
+    chi = 1j * omega * MU0 * np.exp(-1j * ko * R) / (4 * np.pi * ko * ko * R3)
+    P = 1j * ko * R + 1
+    Q = ko * ko * R2 - P
+    P = (Q - 2 * P) / R2
+    Q = chi * Q
+    P = chi * P
+    E = np.zeros((Ocoord.shape[0], 3), dtype=complex)
+    E[:, 0] = (P * X * X - Q) @ J[:, 0] + (P * (X * Y)) @ J[:, 1] + (P * (X * Z)) @ J[:, 2]
+    E[:, 1] = (P * (X * Y)) @ J[:, 0] + (P * (Y * Y) - Q) @ J[:, 1] + (P * (Y * Z)) @ J[:, 2]
+    E[:, 2] = (P * (X * Z)) @ J[:, 0] + (P * (Y * Z)) @ J[:, 1] + (P * (Z * Z) - Q) @ J[:, 2]
+    return E
+
+
+def Dipole_Excitation(r, ko, DipJ, DipCoord):
+    """src_vie/src_fields/src_excitations/Dipole_Excitation.m:39-54 (E only)."""
+    L, M, N, _ = r.shape
+    O = r.reshape((L * M * N, 3), order="F")
+    E = E_field_DGF(DipJ, np.asarray(DipCoord, dtype=float).reshape(-1, 3), O, ko)
+    return E.reshape((L, M, N, 3), order="F")
+
+
+# ---------------------------------------------------------------------------
+# operator assembly: src_vie/src_operators/*
+# ---------------------------------------------------------------------------
+def gauss_1d(n):
+    """cubatures/gauss_1d.m: Gauss-Legendre on [-1,1], ascending (pinned to the table)."""
+    x, w = np.polynomial.legendre.leggauss(n)
+    return w, x
+
+
+def gauss_2d(n):
+    """cubatures/gauss_2d.m:1-19."""
+    w1, x1 = gauss_1d(n)
+    W = np.outer(w1, w1).reshape(-1) / 4
+    U = np.repeat((x1 + 1) / 2, n)
+    V = np.tile((x1 + 1) / 2, n)
+    return n * n, W, U, V
+
+
+def cube_faces(dx, dy, dz):
+    """cube_faces.m:4-38 -> R_faces[3, 4, 6] (coordinate, corner, face)."""
+    R = np.zeros((3, 4, 6))
+    R[:, :, 0] = np.array([[0, 0, 0], [0, dy, 0], [0, dy, dz], [0, 0, dz]]).T
+    R[:, :, 1] = np.array([[dx, 0, 0], [dx, dy, 0], [dx, dy, dz], [dx, 0, dz]]).T
+    R[:, :, 2] = np.array([[0, 0, 0], [dx, 0, 0], [dx, 0, dz], [0, 0, dz]]).T
+    R[:, :, 3] = np.array([[0, dy, 0], [dx, dy, 0], [dx, dy, dz], [0, dy, dz]]).T
+    R[:, :, 4] = np.array([[0, 0, 0], [dx, 0, 0], [dx, dy, 0], [0, dy, 0]]).T
+    R[:, :, 5] = np.array([[0, 0, dz], [dx, 0, dz], [dx, dy, dz], [0, dy, dz]]).T
+    return R
+
+
+INDEX_OBS = [0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 4, 4, 5]  # cubature_nop.cpp:24
+INDEX_SRC = [0, 1, 2, 3, 4, 5, 0, 2, 3, 4, 5, 2, 3, 4, 5, 2, 4, 5, 4, 5, 4]  # cubature_nop.cpp:26
+MIRROR = [((1, 1), (0, 0)), ((2, 0), (1, 3)), ((2, 1), (0, 3)), ((3, 0), (1, 2)), ((3, 1), (0, 2)),
+          ((3, 3), (2, 2)), ((4, 0), (1, 5)), ((4, 1), (0, 5)), ((4, 2), (3, 5)), ((4, 3), (2, 5)),
+          ((5, 0), (1, 4)), ((5, 1), (0, 4)), ((5, 2), (3, 4)), ((5, 3), (2, 4)), ((5, 5), (4, 4))]  # :100-115
+
+
+def cubature_nop_batch(Np, w, u, v, r_m, R_faces, ko, dx):
+    """cubature_nop.cpp:8-125 for a batch of observation offsets r_m (B x 3), r_n = 0.
+
+    Returns I_mn of shape (B, 6, 6), already multiplied by dx^4."""
+    r_m = np.atleast_2d(r_m)
+    B = r_m.shape[0]
+    I = np.zeros((B, 6, 6), dtype=complex)
+    W = np.outer(w, w)
+    for io, isrc in zip(INDEX_OBS, INDEX_SRC):
+        p1, p2, p4 = R_faces[:, 0, io], R_faces[:, 1, io], R_faces[:, 3, io]
+        q1, q2, q4 = R_faces[:, 0, isrc], R_faces[:, 1, isrc], R_faces[:, 3, isrc]
+        rp = p1[None, :] + np.outer(u, p2 - p1) + np.outer(v, p4 - p1)  # Np x 3
+        rq = q1[None, :] + np.outer(u, q2 - q1) + np.outer(v, q4 - q1)
+        d = rq[None, None, :, :] - (rp[None, :, None, :] + r_m[:, None, None, :])  # B x Np x Np x 3
+        R = np.sqrt(np.sum(d * d, axis=-1))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            G = np.exp(-1j * ko * R) / R
+        I[:, io, isrc] = np.sum(W[None] * G, axis=(1, 2))
+    for (a, b), (c, d_) in MIRROR:
+        I[:, a, b] = I[:, c, d_]
+    return dx**4 * I
+
+
+def vector_projection():
+    """vector_projection.m:10-25 -> P[6, 6, 6]."""
+    e = np.eye(3)
+    KL = np.array([-e[0], e[0], -e[1], e[1], -e[2], e[2]])
+    comps = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+    P = np.zeros((6, 6, 6))
+    for kk in range(6):
+        for ll in range(6):
+            for c, (a, b) in enumerate(comps):
+                P[kk, ll, c] = np.dot(np.cross(KL[kk], e[a]), np.cross(KL[ll], e[b]))
+    return P
+
+
+def near_class(m, i, j):
+    """Geometric class of face pair (obs face i of the voxel at offset m in {0,1}^3,
+    src face j at the origin): 0 regular, 1 ST, 2 EAc, 3 EAo, 4 VAc, 5 VAo.  This
+    restates the C/P tables of nearby_correct.m:5-143 (pinned by a fixture)."""
+    ai, si, aj, sj = i // 2, i % 2, j // 2, j % 2
+    if ai == aj:
+        if m[ai] + si != sj:
+            return 0
+        shifted = sum(m[b] for b in range(3) if b != ai)
+        return 1 if shifted == 0 else (2 if shifted == 1 else 4)
+    ci, cj = m[ai] + si, sj
+    if not (m[aj] <= cj <= m[aj] + 1) or not (0 <= ci <= 1):
+        return 0
+    b = 3 - ai - aj
+    return 3 if m[b] == 0 else 5
+
+
+def nearby_correct(m, I_non, sing):
+    """nearby_correct.m: replace the weakly singular pairs with sing[cls-1]."""
+    J = I_non.copy()
+    for i in range(6):
+        for j in range(6):
+            c = near_class(m, i, j)
+            if c:
+                J[i, j] = sing[c - 1]
+    return J
+
+
+def singular_integrals(ko, a, n=32):
+    """Weakly singular square-square integrals {ST, EAc, EAo, VAc, VAo} of
+    exp(-j ko R)/R for voxel edge a, replacing singular_st/ea/va.m.  Relative
+    coordinates turn each into an integral of f(|u|) times hat-function weights;
+    a Duffy substitution removes the 1/R point singularity at the origin."""
+    x, w = np.polynomial.legendre.leggauss(n)
+    x = (x + 1) / 2
+    w = w / 2
+    S, T = np.meshgrid(x, x, indexing="ij")
+    W2 = np.outer(w, w)
+    S3, T1, T2 = np.meshgrid(x, x, x, indexing="ij")
+    W3 = np.einsum("i,j,k->ijk", w, w, w)
+    k = ko
+
+    def e2(s, t):
+        rho = np.sqrt(1 + t * t)
+        return np.exp(-1j * k * a * s * rho) / rho
+
+    def e3(s, t1, t2):
+        rho = np.sqrt(1 + t1 * t1 + t2 * t2)
+        return np.exp(-1j * k * a * s * rho) / rho
+
+    def f(R):
+        return np.exp(-1j * k * R) / R
+
+    a3 = a**3
+    ST = 8 * a3 * np.sum(W2 * e2(S, T) * (1 - S) * (1 - S * T))
+    p1 = a3 * np.sum(W2 * e2(S, T) * (S * (1 - S * T) + S * T * (1 - S)))
+    U1, U2 = a + a * S, a * T
+    p2 = a * a * np.sum(W2 * f(np.hypot(U1, U2)) * (2 * a - U1) * (a - U2))
+    EAc = 2 * (p1 + p2)
+    EAo = 2 * a3 * np.sum(W3 * e3(S3, T1, T2) * (S3 * (1 - S3 * T1) + S3 * (1 - S3) + S3 * (1 - S3 * T2)))
+    q0 = 2 * a3 * np.sum(W2 * e2(S, T) * S * S * T)
+    q1 = a * a * np.sum(W2 * f(np.hypot(a + a * S, a * T)) * (2 * a - (a + a * S)) * (a * T))
+    q2 = a * a * np.sum(W2 * f(np.hypot(a + a * S, a + a * T)) * (2 * a - (a + a * S)) * (2 * a - (a + a * T)))
+    VAc = q0 + 2 * q1 + q2
+    s0 = a3 * np.sum(W3 * e3(S3, T1, T2) * (S3 * S3 * T1 + S3 * S3 + S3 * S3 * T2))
+    U1, U2, U3 = a * S3, a + a * T1, a * T2
+    s1 = a3 * np.sum(W3 * f(np.sqrt(U1**2 + U2**2 + U3**2)) * (2 * a - U2))
+    VAo = s0 + s1
+    return np.array([ST, EAc, EAo, VAc, VAo])
+
+
+def assembly_nop(L, M, N, ko, dx, sing):
+    """assembly_nop.m:7-136 -> G_mn (L, M, N, 6)."""
+    R_faces = cube_faces(dx, dx, dx)
+    J = np.zeros((L, M, N, 6, 6), dtype=complex)
+    d = np.array([dx, dx, dx])
+    # far: all offsets, 4-point rule (assembly_nop.m:37-59); batched over x
+    Np, w, u, v = gauss_2d(4)
+    for mz in range(N):
+        for my in range(M):
+            mx = np.arange(L)
+            r_m = np.stack([mx * dx, np.full(L, my * dx), np.full(L, mz * dx)], axis=1)
+            J[:, my, mz] = cubature_nop_batch(Np, w, u, v, r_m, R_faces, ko, dx)
+    # medium: offsets 1..5 per axis with the 10-point rule (:67-83)
+    Np, w, u, v = gauss_2d(10)
+    for mx in range(min(5, L)):
+        for my in range(min(5, M)):
+            for mz in range(min(5, N)):
+                J[mx, my, mz] = cubature_nop_batch(Np, w, u, v, np.array([mx, my, mz]) * d, R_faces, ko, dx)[0]
+    # near: 20-point rule + singular corrections (:96-114)
+    Np, w, u, v = gauss_2d(20)
+    for mx in range(min(2, L)):
+        for my in range(min(2, M)):
+            for mz in range(min(2, N)):
+                I_non = cubature_nop_batch(Np, w, u, v, np.array([mx, my, mz]) * d, R_faces, ko, dx)[0]
+                J[mx, my, mz] = nearby_correct((mx, my, mz), I_non, sing)
+    P = vector_projection()
+    G = np.einsum("xyzij,ijk->xyzk", J, P)
+    return G / (4 * np.pi)
+
+
+# gperiodic_coeff_nop.m:4-30
+_GP = {
+    "L": [+1, -1, -1, +1, +1, +1], "M": [+1, -1, +1, +1, -1, +1], "N": [+1, +1, -1, +1, -1, +1],
+    "LM": [+1, +1, -1, +1, -1, +1], "LN": [+1, -1, +1, +1, -1, +1], "MN": [+1, -1, -1, +1, +1, +1],
+}
+
+
+def circulant_nop(G):
+    """circulant_nop.m:23-40 (block copies with the gperiodic coefficients)."""
+    L, M, N, _ = G.shape
+    C = np.zeros((2 * L, 2 * M, 2 * N, 6), dtype=complex)
+    C[:L, :M, :N] = G
+    for ii in range(6):
+        C[L + 1:, :M, :N, ii] = G[L - 1:0:-1, :, :, ii] * _GP["L"][ii]
+        C[:L, M + 1:, :N, ii] = G[:, M - 1:0:-1, :, ii] * _GP["M"][ii]
+        C[:L, :M, N + 1:, ii] = G[:, :, N - 1:0:-1, ii] * _GP["N"][ii]
+        C[L + 1:, M + 1:, :N, ii] = G[L - 1:0:-1, M - 1:0:-1, :, ii] * _GP["LM"][ii]
+        C[L + 1:, :M, N + 1:, ii] = G[L - 1:0:-1, :, N - 1:0:-1, ii] * _GP["LN"][ii]
+        C[:L, M + 1:, N + 1:, ii] = G[:, M - 1:0:-1, N - 1:0:-1, ii] * _GP["MN"][ii]
+    C[L + 1:, M + 1:, N + 1:] = G[L - 1:0:-1, M - 1:0:-1, N - 1:0:-1]
+    return C
+
+
+def fft_operator(A, workers=None):
+    """fft_operator.m:6-8."""
+    return scipy.fft.fftn(A, axes=(0, 1, 2), workers=workers)
+
+
+def getOPERATORS(r, f, op="N", typ="FFTofC", sing=None):
+    """getOPERATORS.m:36-90 for op 'N'.  sing = the five singular integrals
+    (defaults to the converged quadrature of singular_integrals)."""
+    if op != "N":
+        raise NotImplementedError("only the N operator")
+    dx = r[1, 0, 0, 0] - r[0, 0, 0, 0]
+    ko = 2 * np.pi / 299792458 * f
+    L, M, N, _ = r.shape
+    if sing is None:
+        sing = singular_integrals(ko, dx)
+    T = assembly_nop(L, M, N, ko, dx, sing)
+    if typ == "T":
+        return T
+    C = circulant_nop(T)
+    if typ == "C":
+        return C
+    return fft_operator(C)
+
+
+# ---------------------------------------------------------------------------
+# grid helpers (grid3d.m:35-61 layout: L x M x N x 3 voxel centres)
+# ---------------------------------------------------------------------------
+def grid(L, M, N, dx, center=(0.0, 0.0, 0.0)):
+    xs = (np.arange(L) - (L - 1) / 2) * dx + center[0]
+    ys = (np.arange(M) - (M - 1) / 2) * dx + center[1]
+    zs = (np.arange(N) - (N - 1) / 2) * dx + center[2]
+    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
+    return np.stack([X, Y, Z], axis=3)

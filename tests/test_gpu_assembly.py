@@ -1,0 +1,94 @@
+"""GPU parity of getOPERATORS (Toeplitz, circulant, FFT of circulant), the
+singular integrals and the excitations against the oracle and the reference's
+golden DIRECTFN / cubature values."""
+import numpy as np
+import pytest
+
+from oracle import vie_oracle as vo
+
+pytestmark = pytest.mark.gpu
+FREQ = 298e6
+
+
+def relerr(a, b):
+    return np.max(np.abs(np.asarray(a) - np.asarray(b))) / np.max(np.abs(b))
+
+
+def test_singular_integrals_match_oracle_and_directfn(golden):
+    import marie_gb300 as mg
+
+    for d in golden["directfn"]:
+        dev = mg.singular_integrals(d["ko"], d["dx"])
+        ora = vo.singular_integrals(d["ko"], d["dx"])
+        np.testing.assert_allclose(dev, ora, rtol=1e-13)
+        ref = np.array(d["re"]) + 1j * np.array(d["im"])
+        assert np.max(np.abs(dev - ref) / np.abs(ref)) < (4e-5 if d["Np"] == 20 else 1e-6)
+
+
+@pytest.mark.parametrize("shape,dx", [((8, 8, 8), 5e-3), ((12, 4, 8), 2e-3), ((6, 7, 5), 3e-3)])
+def test_toeplitz_matches_oracle(shape, dx):
+    import marie_gb300 as mg
+
+    r = vo.grid(*shape, dx)
+    ref = vo.getOPERATORS(r, FREQ, typ="T")
+    out = mg.getOPERATORS(r, FREQ, "N", "T")
+    assert relerr(out, ref) < 1e-12
+
+
+def test_reference_singular_values_give_exact_parity(golden):
+    """singular='U' with the reference's own DIRECTFN values (Np_1D = 20)."""
+    import marie_gb300 as mg
+
+    d = [g for g in golden["directfn"] if g["dx"] == 5e-3 and g["Np"] == 20][0]
+    sv = np.array(d["re"]) + 1j * np.array(d["im"])
+    r = vo.grid(8, 8, 8, 5e-3)
+    ref = vo.getOPERATORS(r, FREQ, sing=sv)
+    out = mg.getOPERATORS(r, FREQ, singular_values=sv)
+    assert relerr(out, ref) < 1e-12
+    # the converged singular integrals move fN by far less than the FP32 bar
+    conv = mg.getOPERATORS(r, FREQ)
+    assert relerr(conv, ref) < 1e-5
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (12, 16, 4), (24, 8, 20)])
+def test_circulant_and_fft_match_oracle(shape):
+    import marie_gb300 as mg
+
+    r = vo.grid(*shape, 5e-3)
+    C = vo.getOPERATORS(r, FREQ, typ="C")
+    F = vo.fft_operator(C)
+    assert relerr(mg.getOPERATORS(r, FREQ, "N", "C"), C) < 1e-12
+    assert relerr(mg.getOPERATORS(r, FREQ), F) < 1e-12
+    op = mg.Operator.assemble(*shape, 5e-3, FREQ)
+    assert relerr(op.to_array(), F) < 1e-12
+
+
+def test_plane_wave_and_dipoles_match_oracle():
+    import marie_gb300 as mg
+
+    r = vo.grid(12, 8, 16, 4e-3)
+    em = vo.EMconstants(FREQ)
+    for k, Eo in (([0, 0, em["ko"]], [1, 0, 0]), ([em["ko"] / 2, 0, em["ko"] * 0.8], [0, 1j, 0.5])):
+        Eref, Href = vo.PlaneWave_Excitation(r, k, em["omega_mu"], Eo)
+        E, H = mg.PlaneWave_Excitation(r, k, em["omega_mu"], Eo)
+        assert relerr(E, Eref) < 1e-13
+        assert relerr(H, Href) < 1e-13
+    pos = np.array([[0.15, 0, 0.01], [0, -0.15, -0.05], [-0.1, 0.1, 0.0]])
+    Jd = np.array([[0, 0, 1], [0, 0, 1], [0.3, 0, 1j]], complex)
+    Eref = vo.Dipole_Excitation(r, em["ko"], Jd, pos)
+    E = mg.Dipole_Excitation(r, em["ko"], Jd, pos)
+    assert relerr(E, Eref) < 1e-12
+
+
+def test_e_field_nop_matches_oracle():
+    import marie_gb300 as mg
+
+    L, M, N = 8, 12, 8
+    rng = np.random.default_rng(0)
+    r = vo.grid(L, M, N, 5e-3)
+    fN = vo.getOPERATORS(r, FREQ)
+    J = np.asfortranarray(rng.standard_normal((L, M, N, 3)) + 1j * rng.standard_normal((L, M, N, 3)))
+    Ei = np.asfortranarray(rng.standard_normal((L, M, N, 3)) + 0j)
+    ref = vo.E_field_Nop(J, fN, 1.25e-7, FREQ, Ei)
+    out = mg.E_field_Nop(J, mg.Operator.from_array(fN), 1.25e-7, FREQ, Ei)
+    assert relerr(out, ref) < 1e-12

@@ -1,0 +1,115 @@
+"""GPU parity of pgmres and JVIE_Solver against the oracle restatements of
+pgmres.m / pgmres_iter.m / JVIE_Solver.m, the mixed-precision solve against
+the FP64 solve, and the Mie-series sphere check (RUN_Sphere_VIE_MIE.m)."""
+import numpy as np
+import pytest
+
+from oracle import mie
+from oracle import vie_oracle as vo
+
+pytestmark = pytest.mark.gpu
+FREQ = 298e6
+
+
+def dense(n, seed):
+    rng = np.random.default_rng(seed)
+    A = np.eye(n) * 3 + 0.4 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    return A, b
+
+
+@pytest.mark.parametrize("restart,tol,maxit", [(10, 1e-10, 20), (5, 1e-6, 3), (50, 1e-12, 2)])
+def test_pgmres_host_handles_match_oracle(restart, tol, maxit):
+    import marie_gb300 as mg
+
+    A, b = dense(60, restart)
+    ref = vo.pgmres(lambda v: A @ v, b, restart, tol, maxit)
+    out = mg.pgmres(lambda v: A @ v, b, restart, tol, maxit)
+    assert out[1] == ref[1]
+    assert out[3] == ref[3]
+    np.testing.assert_allclose(out[4], ref[4], rtol=1e-8, atol=1e-14)
+    np.testing.assert_allclose(out[0], ref[0], rtol=1e-9, atol=1e-12)
+    assert abs(out[2] - ref[2]) <= 1e-9 * max(ref[2], 1e-12) + 1e-15
+
+
+def test_pgmres_preconditioners_and_x0(cuda):
+    import torch
+
+    import marie_gb300 as mg
+
+    A, b = dense(50, 4)
+    P = np.diag(1.0 / np.diag(A))
+    Pt = torch.from_numpy(P).to(cuda)
+    At = torch.from_numpy(A).to(cuda)
+    x0 = np.full(50, 0.1 + 0.2j)
+    for kw in (dict(R1=lambda v: P @ v), dict(L1=lambda v: P @ v), dict(L1=lambda v: P @ v, R2=lambda v: P @ v)):
+        ref = vo.pgmres(lambda v: A @ v, b, 8, 1e-9, 10, x0=x0, **kw)
+        out = mg.pgmres(lambda v: A @ v, b, 8, 1e-9, 10, x0=x0, **kw)
+        assert out[3] == ref[3] and out[1] == ref[1]
+        np.testing.assert_allclose(out[4], ref[4], rtol=1e-8, atol=1e-14)
+        np.testing.assert_allclose(out[0], ref[0], rtol=1e-8)
+    # device handles on a device right-hand side
+    bt = torch.from_numpy(b).to(cuda)
+    out = mg.pgmres(lambda v: At @ v, bt, 8, 1e-9, 10, R1=lambda v: Pt @ v)
+    ref = vo.pgmres(lambda v: A @ v, b, 8, 1e-9, 10, R1=lambda v: P @ v)
+    assert out[0].is_cuda
+    np.testing.assert_allclose(out[0].cpu().numpy(), ref[0], rtol=1e-8)
+
+
+def sphere_problem(L, dx, radius, eps_r=50.0, sigma=0.5):
+    r = vo.grid(L, L, L, dx)
+    er = np.ones((L, L, L), complex)
+    er[np.sum(r * r, axis=3) < radius**2] = eps_r - 1j * sigma / (vo.EPS0 * 2 * np.pi * FREQ)
+    em = vo.EMconstants(FREQ)
+    E, _ = vo.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
+    return r, np.asfortranarray(er), np.asfortranarray(E)
+
+
+@pytest.mark.parametrize("form,precond", [(2, 0), (1, 0), (1, "R"), (2, "L")])
+def test_jvie_solver_matches_oracle(form, precond):
+    import marie_gb300 as mg
+
+    L, dx = 8, 5e-3
+    r, er, E = sphere_problem(L, dx, 0.018)
+    fN = vo.getOPERATORS(r, FREQ)
+    ref = vo.JVIE_Solver(E, er, r, FREQ, fN, tol=1e-10, form=form, precond=precond, inner_it=20)
+    op = mg.Operator.from_array(fN)
+    out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-10, form=form, precond=precond, inner_it=20)
+    assert out[1] == ref[1] == 0
+    assert out[3] == ref[3]
+    np.testing.assert_allclose(out[4], ref[4], rtol=1e-6, atol=1e-13)
+    assert np.max(np.abs(out[0] - ref[0])) < 1e-8 * np.max(np.abs(ref[0]))
+
+
+def test_mixed_precision_solve_matches_fp64():
+    import marie_gb300 as mg
+
+    L, dx = 16, 5e-3
+    r, er, E = sphere_problem(L, dx, 0.035)
+    op64 = mg.Operator.assemble(L, L, L, dx, FREQ, precision="fp64")
+    opm = mg.Operator.assemble(L, L, L, dx, FREQ, precision="mixed")
+    J64, f64, rr64, it64, _, _ = mg.JVIE_Solver(E, er, r, FREQ, op64, tol=1e-6)
+    Jm, fm, rrm, itm, resm, _ = mg.JVIE_Solver(E, er, r, FREQ, opm, tol=1e-6)
+    assert f64 == 0 and fm == 0 and rrm <= 1e-6
+    # both solutions satisfy the FP64 system to 1e-6: fields agree to ~cond * tol
+    assert np.linalg.norm(Jm - J64) / np.linalg.norm(J64) < 2e-5
+
+
+def test_mie_sphere_c1():
+    """32^3 at 5 mm, r = 7.5 cm, eps_r = 50, sigma = 0.5 S/m, 298 MHz, x-polarised
+    +z plane wave.  The reference compares visually; here the relative L2 error of
+    the total field inside the sphere, excluding the outermost voxel shell, must
+    be below 10% (staircase discretisation error at 5 mm)."""
+    import marie_gb300 as mg
+
+    L, dx, R = 32, 5e-3, 0.075
+    r, er, E = sphere_problem(L, dx, R)
+    op = mg.Operator.assemble(L, L, L, dx, FREQ, precision="fp64")
+    Je, flag, relres, it, resvec, _ = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-6)
+    assert flag == 0
+    Et = mg.E_field_Nop(Je, op, dx**3, FREQ, E)
+    rad = np.sqrt(np.sum(r * r, axis=3))
+    core = rad < R - 1.5 * dx
+    Em = mie.MIE_SERIES(r[core][:, None, None, :], R, 50.0, 0.5, FREQ)[:, 0, 0, :]
+    err = np.linalg.norm(Et[core] - Em) / np.linalg.norm(Em)
+    assert err < 0.10, err

@@ -1,0 +1,172 @@
+"""CPU tests of the oracle (the checker) against the reference's golden vectors
+and known-answer identities.  No GPU."""
+import numpy as np
+import pytest
+
+from oracle import vie_oracle as vo
+
+FREQ = 298e6
+
+
+def test_gauss_rules_match_reference_table(golden):
+    for n in (4, 10, 20):
+        w, x = vo.gauss_1d(n)
+        g = golden["gauss_1d"][str(n)]
+        np.testing.assert_allclose(x, g["x"], rtol=0, atol=2e-15)
+        np.testing.assert_allclose(w, g["w"], rtol=0, atol=2e-15)
+
+
+def test_near_classes_match_nearby_correct_tables(golden):
+    for key, codes in golden["nearby"].items():
+        m = tuple(int(c) for c in key.split(","))
+        mine = [[vo.near_class(m, i, j) for j in range(6)] for i in range(6)]
+        assert mine == codes, key
+
+
+def test_cubature_matches_reference_cpp(golden):
+    for case in golden["cubature_nop"]:
+        dx, ko = case["dx"], case["ko"]
+        Np, w, u, v = vo.gauss_2d(case["order"])
+        Rf = vo.cube_faces(dx, dx, dx)
+        I = vo.cubature_nop_batch(Np, w, u, v, np.array(case["m"], float)[None] * dx, Rf, ko, dx)[0]
+        ref = np.array(case["re"]) + 1j * np.array(case["im"])
+        # touching faces evaluate 1/0 at coincident Gauss points in both codes
+        fin = np.isfinite(ref)
+        assert np.array_equal(fin, np.isfinite(I))
+        np.testing.assert_allclose(I[fin], ref[fin], rtol=1e-13, atol=1e-13 * np.abs(ref[fin]).max())
+
+
+def test_singular_integrals_static_closed_form():
+    # int_{[0,1]^2} int_{[0,1]^2} 1/|x-y| = 4 ln(1+sqrt 2) + (4/3)(1 - sqrt 2)
+    s = vo.singular_integrals(1e-12, 1.0)
+    exact = 4 * np.log(1 + np.sqrt(2)) + 4 / 3 * (1 - np.sqrt(2))
+    assert abs(s[0].real - exact) < 1e-14 * exact
+
+
+def test_singular_integrals_vs_reference_directfn(golden):
+    """DIRECTFN at the reference's Np_1D = 20 carries a truncation error of up to
+    ~3.4e-5 (edge-adjacent terms); at Np_1D = 64 it agrees to ~5e-7, i.e. DIRECTFN
+    converges towards the restatement's values.  The
+    restatement converges to machine precision (self-convergence below)."""
+    for d in golden["directfn"]:
+        ref = np.array(d["re"]) + 1j * np.array(d["im"])
+        mine = vo.singular_integrals(d["ko"], d["dx"])
+        rel = np.abs(mine - ref) / np.abs(ref)
+        assert rel.max() < (4e-5 if d["Np"] == 20 else 1e-6), (d["Np"], rel)
+        # the imaginary (smooth) parts agree to round-off at every Np
+        np.testing.assert_allclose(mine.imag, ref.imag, rtol=1e-12)
+    a = vo.singular_integrals(6.2, 5e-3, n=24)
+    b = vo.singular_integrals(6.2, 5e-3, n=48)
+    assert np.max(np.abs(a - b) / np.abs(b)) < 1e-14
+
+
+def test_circulant_parity_structure():
+    rng = np.random.default_rng(0)
+    L, M, N = 4, 3, 5
+    G = rng.standard_normal((L, M, N, 6)) + 1j * rng.standard_normal((L, M, N, 6))
+    C = vo.circulant_nop(G)
+    par = [(1, 1, 1), (-1, -1, 1), (-1, 1, -1), (1, 1, 1), (1, -1, -1), (1, 1, 1)]
+    for q in range(6):
+        for ix in range(2 * L):
+            for iy in range(2 * M):
+                for iz in range(2 * N):
+                    if ix == L or iy == M or iz == N:
+                        assert C[ix, iy, iz, q] == 0
+                        continue
+                    s = 1
+                    sx, sy, sz = ix, iy, iz
+                    if ix > L:
+                        sx, s = 2 * L - ix, s * par[q][0]
+                    if iy > M:
+                        sy, s = 2 * M - iy, s * par[q][1]
+                    if iz > N:
+                        sz, s = 2 * N - iz, s * par[q][2]
+                    assert C[ix, iy, iz, q] == s * G[sx, sy, sz, q]
+
+
+def _random_problem(L, M, N, seed=0, frac=0.6):
+    rng = np.random.default_rng(seed)
+    fN = rng.standard_normal((2 * L, 2 * M, 2 * N, 6)) + 1j * rng.standard_normal((2 * L, 2 * M, 2 * N, 6))
+    Mr = 1 + rng.random((L, M, N)) + 1j * rng.random((L, M, N))
+    Mc = Mr - 1
+    mask = rng.random(L * M * N) < frac
+    idxS = np.nonzero(mask)[0] + 1
+    V = L * M * N
+    idx = np.concatenate([idxS, V + idxS, 2 * V + idxS])
+    J = rng.standard_normal(idx.size) + 1j * rng.standard_normal(idx.size)
+    return fN, Mr, Mc, idx, J
+
+
+def test_mv_AN_delta_operator_is_diagonal():
+    """fN = FFT of a delta at the origin (xx=yy=zz=1): N J = J, so
+    mv_AN = (Gram*Mr - Mc) J."""
+    L, M, N = 4, 5, 3
+    _, Mr, Mc, idx, J = _random_problem(L, M, N)
+    fN = np.zeros((2 * L, 2 * M, 2 * N, 6), complex)
+    fN[..., 0] = fN[..., 3] = fN[..., 5] = 1.0
+    out = vo.mv_AN(J, fN, Mr, Mc, 0.3, "notransp", idx)
+    v = (idx - 1) % (L * M * N)
+    exp = (0.3 * Mr.reshape(-1, order="F")[v] - Mc.reshape(-1, order="F")[v]) * J
+    np.testing.assert_allclose(out, exp, rtol=1e-13, atol=1e-13)
+
+
+def test_mv_AN_transp_is_hermitian_adjoint():
+    L, M, N = 4, 3, 4
+    fN0, Mr, Mc, idx, x = _random_problem(L, M, N, seed=1)
+    # a physical fN is the FFT of a parity-symmetric circulant (N symmetric)
+    rng = np.random.default_rng(5)
+    G = rng.standard_normal((L, M, N, 6)) + 1j * rng.standard_normal((L, M, N, 6))
+    # components odd along an axis vanish on the zero-offset plane of that axis
+    G[0, :, :, [1, 2]] = 0
+    G[:, 0, :, [1, 4]] = 0
+    G[:, :, 0, [2, 4]] = 0
+    fN = vo.fft_operator(vo.circulant_nop(G))
+    y = rng.standard_normal(idx.size) + 1j * rng.standard_normal(idx.size)
+    Ax = vo.mv_AN(x, fN, Mr, Mc, 0.7, "notransp", idx)
+    AHy = vo.mv_AN(y, fN, Mr, Mc, 0.7, "transp", idx)
+    lhs = np.vdot(y, Ax)
+    rhs = np.vdot(AHy, x)
+    assert abs(lhs - rhs) < 1e-12 * abs(lhs)
+
+
+def test_pgmres_dense_system_matches_solve():
+    rng = np.random.default_rng(3)
+    n = 40
+    A = np.eye(n) * 4 + 0.3 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    x, flag, relres, it, resvec = vo.pgmres(lambda v: A @ v, b, 10, 1e-12, 20)
+    assert flag == 0 and relres <= 1e-12
+    np.testing.assert_allclose(x, np.linalg.solve(A, b), rtol=1e-10)
+    assert resvec[0] == pytest.approx(1.0)
+
+
+def test_jvie_field_current_identity():
+    """Inside the body E = J/(j omega eps0 (eps_c - 1)) for the converged J
+    (E_field_Nop.m:84 with JVIE_Solver.m:151-156)."""
+    L = M = N = 6
+    dx = 5e-3
+    r = vo.grid(L, M, N, dx)
+    er = np.ones((L, M, N), complex)
+    inside = np.sum(r * r, axis=3) < (2.2 * dx) ** 2
+    er[inside] = 40 - 20j
+    fN = vo.getOPERATORS(r, FREQ)
+    em = vo.EMconstants(FREQ)
+    E, _ = vo.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
+    Je, flag, relres, it, resvec = vo.JVIE_Solver(E, er, r, FREQ, fN, tol=1e-10, form=1)
+    assert flag == 0
+    Et = vo.E_field_Nop(Je, fN, dx**3, FREQ, E)
+    Ej = Je[inside] / (1j * em["omega"] * vo.EPS0 * (er[inside, None] - 1))
+    np.testing.assert_allclose(Et[inside], Ej, rtol=1e-6, atol=1e-6 * np.abs(Ej).max())
+
+
+def test_getoperators_small_grid_self_consistency():
+    """Toeplitz / circulant / FFT outputs of the restatement agree with each other."""
+    L, M, N = 3, 4, 2
+    r = vo.grid(L, M, N, 5e-3)
+    T = vo.getOPERATORS(r, FREQ, typ="T")
+    Cc = vo.getOPERATORS(r, FREQ, typ="C")
+    F = vo.getOPERATORS(r, FREQ)
+    np.testing.assert_allclose(Cc[:L, :M, :N], T)
+    np.testing.assert_allclose(np.fft.fftn(Cc, axes=(0, 1, 2)), F, rtol=1e-12, atol=1e-12 * np.abs(F).max())
+    # the diagonal components dominate and are even
+    assert np.abs(T[0, 0, 0, 0]) > np.abs(T[0, 0, 0, 1])
