@@ -208,7 +208,7 @@ static int run_matvec_t(marie_plan* p, const double2* J, double2* out, long long
     MARIE_CUDA_TRY(ML::cols(false, d.Mp, A, (long long)d.Lp * d.M, sA, d.M, B, (long long)d.Lp * d.Mp, sB, d.Mp,
                             d.Lp, 3 * d.N, tw[1], nr, p->stream));
     if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
-    MARIE_CUDA_TRY(ML::zmul(B, sB, fN, d, tw[2], nr, p->stream));
+    MARIE_CUDA_TRY(ML::zmul(B, sB, fN, p->oct, d, tw[2], nr, p->stream));
     if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
     MARIE_CUDA_TRY(ML::cols(true, d.Mp, B, (long long)d.Lp * d.Mp, sB, d.Mp, A, (long long)d.Lp * d.M, sA, d.M,
                             d.Lp, 3 * d.N, tw[1], nr, p->stream));
@@ -261,18 +261,115 @@ __global__ void k_scale_convert(const double2* in, long long n, double s, double
   }
 }
 
+// parity of component q along axis a (0 x, 1 y, 2 z): true = odd
+__host__ __device__ inline bool comp_odd(int q, int a) {
+  return a == 0 ? (q == 1 || q == 2) : (a == 1 ? (q == 1 || q == 4) : (q == 2 || q == 4));
+}
+
+// max |fN(k) - s fN(mirror k)| and max |fN(k)| over the full operator (as the
+// bit patterns of non-negative doubles, which order like the values).
+__global__ void k_symmetry_check(const double2* __restrict__ f, int L, int M, int N,
+                                 unsigned long long* __restrict__ out) {
+  const long long Lp = 2LL * L, Mp = 2LL * M, Np = 2LL * N, P = Lp * Mp * Np;
+  double dev = 0, mx = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 6 * P; t += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(t / P);
+    long long r = t - q * P;
+    const long long ix = r % Lp;
+    r /= Lp;
+    const long long iy = r % Mp, iz = r / Mp;
+    const long long jx = ix > L ? Lp - ix : ix, jy = iy > M ? Mp - iy : iy, jz = iz > N ? Np - iz : iz;
+    const bool neg = ((ix > L) && comp_odd(q, 0)) ^ ((iy > M) && comp_odd(q, 1)) ^ ((iz > N) && comp_odd(q, 2));
+    const double2 a = f[t];
+    double2 b = f[q * P + jx + Lp * (jy + Mp * jz)];
+    if (neg) b = mk<double2>(-b.x, -b.y);
+    dev = fmax(dev, hypot(a.x - b.x, a.y - b.y));
+    mx = fmax(mx, hypot(a.x, a.y));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    dev = fmax(dev, __shfl_xor_sync(0xffffffffu, dev, o));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&out[0], (unsigned long long)__double_as_longlong(dev));
+    atomicMax(&out[1], (unsigned long long)__double_as_longlong(mx));
+  }
+}
+
+// octant (L+1) x (M+1) x (N+1) x 6 of the full operator, scaled, in FP64 and/or FP32
+__global__ void k_extract_octant(const double2* __restrict__ f, int L, int M, int N, double s, double2* o64,
+                                 float2* o32) {
+  const long long Lp = 2LL * L, Mp = 2LL * M, Np = 2LL * N, P = Lp * Mp * Np;
+  const long long Lo = L + 1, Mo = M + 1, No = N + 1, O = Lo * Mo * No;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 6 * O; t += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(t / O);
+    long long r = t - q * O;
+    const long long ox = r % Lo;
+    r /= Lo;
+    const long long oy = r % Mo, oz = r / Mo;
+    const double2 v = f[q * P + ox + Lp * (oy + Mp * oz)];
+    if (o64) o64[t] = mk<double2>(v.x * s, v.y * s);
+    if (o32) o32[t] = mk<float2>((float)(v.x * s), (float)(v.y * s));
+  }
+}
+
+// full operator from the octant (inverse of k_extract_octant), scaled by s
+__global__ void k_expand_octant(const double2* __restrict__ o, int L, int M, int N, double s, double2* __restrict__ f) {
+  const long long Lp = 2LL * L, Mp = 2LL * M, Np = 2LL * N, P = Lp * Mp * Np;
+  const long long Lo = L + 1, Mo = M + 1, No = N + 1, O = Lo * Mo * No;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 6 * P; t += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(t / P);
+    long long r = t - q * P;
+    const long long ix = r % Lp;
+    r /= Lp;
+    const long long iy = r % Mp, iz = r / Mp;
+    const long long jx = ix > L ? Lp - ix : ix, jy = iy > M ? Mp - iy : iy, jz = iz > N ? Np - iz : iz;
+    const bool neg = ((ix > L) && comp_odd(q, 0)) ^ ((iy > M) && comp_odd(q, 1)) ^ ((iz > N) && comp_odd(q, 2));
+    double2 v = o[q * O + jx + Lo * (jy + Mo * jz)];
+    const double sg = neg ? -s : s;
+    f[t] = mk<double2>(v.x * sg, v.y * sg);
+  }
+}
+
+// Installs fN (full layout, device) into the plan: the octant when fN has the
+// circulant's parity symmetry to 1e-12 of its maximum (every operator built
+// by getOPERATORS does), the full array otherwise.  Scaled by 1/(8LMN).
 int install_operator(marie_plan* p, const double2* fN_dev) {
-  const long long P = (long long)p->d.Lp * p->d.Mp * p->d.Np;
-  const long long n = 6 * P;
+  const Dims& d = p->d;
+  const long long P = (long long)d.Lp * d.Mp * d.Np;
+  const long long O = (long long)(d.L + 1) * (d.M + 1) * (d.N + 1);
   const bool need64 = p->precision != MARIE_FP32;
   const bool need32 = p->precision != MARIE_FP64;
-  if (need64 && !p->fN64) MARIE_CUDA_TRY(cudaMalloc(&p->fN64, n * sizeof(double2)));
-  if (need32 && !p->fN32) MARIE_CUDA_TRY(cudaMalloc(&p->fN32, n * sizeof(float2)));
-  k_scale_convert<<<grid_for(n), 256, 0, p->stream>>>(fN_dev, n, 1.0 / (double)P, need64 ? p->fN64 : nullptr,
-                                                       need32 ? p->fN32 : nullptr);
+  DBuf flags;
+  MARIE_TRY(flags.alloc(2 * sizeof(unsigned long long), p->stream));
+  MARIE_CUDA_TRY(cudaMemsetAsync(flags.p, 0, 2 * sizeof(unsigned long long), p->stream));
+  k_symmetry_check<<<grid_for(6 * P), 256, 0, p->stream>>>(fN_dev, d.L, d.M, d.N, flags.as<unsigned long long>());
+  count_launch();
+  unsigned long long h[2];
+  MARIE_CUDA_TRY(cudaMemcpyAsync(h, flags.p, sizeof(h), cudaMemcpyDeviceToHost, p->stream));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  double dev, mx;
+  memcpy(&dev, &h[0], sizeof(double));
+  memcpy(&mx, &h[1], sizeof(double));
+  const int oct = (dev <= 1e-12 * mx) ? 1 : 0;
+  const long long n = oct ? 6 * O : 6 * P;
+  cudaFree(p->fN64);
+  cudaFree(p->fN32);
+  p->fN64 = nullptr;
+  p->fN32 = nullptr;
+  if (need64) MARIE_CUDA_TRY(cudaMalloc(&p->fN64, n * sizeof(double2)));
+  if (need32) MARIE_CUDA_TRY(cudaMalloc(&p->fN32, n * sizeof(float2)));
+  if (oct) {
+    k_extract_octant<<<grid_for(n), 256, 0, p->stream>>>(fN_dev, d.L, d.M, d.N, 1.0 / (double)P,
+                                                         need64 ? p->fN64 : nullptr, need32 ? p->fN32 : nullptr);
+  } else {
+    k_scale_convert<<<grid_for(n), 256, 0, p->stream>>>(fN_dev, n, 1.0 / (double)P, need64 ? p->fN64 : nullptr,
+                                                         need32 ? p->fN32 : nullptr);
+  }
   count_launch();
   MARIE_CUDA_TRY(cudaGetLastError());
   MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  p->oct = oct;
   p->has_op = true;
   return MARIE_OK;
 }
@@ -387,7 +484,11 @@ int marie_get_plan_operator(marie_plan* p, double* fN_out) {
   DBuf tmp;
   void* dev = nullptr;
   MARIE_TRY(stage_out(fN_out, bytes, p->stream, tmp, &dev));
-  k_scale_convert<<<grid_for(6 * P), 256, 0, p->stream>>>(p->fN64, 6 * P, (double)P, (double2*)dev, nullptr);
+  if (p->oct)
+    k_expand_octant<<<grid_for(6 * P), 256, 0, p->stream>>>(p->fN64, p->d.L, p->d.M, p->d.N, (double)P,
+                                                            (double2*)dev);
+  else
+    k_scale_convert<<<grid_for(6 * P), 256, 0, p->stream>>>(p->fN64, 6 * P, (double)P, (double2*)dev, nullptr);
   count_launch();
   MARIE_CUDA_TRY(cudaGetLastError());
   MARIE_TRY(finish_out(fN_out, dev, bytes, p->stream));

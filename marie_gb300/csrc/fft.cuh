@@ -15,13 +15,35 @@
 // Twiddles come from a per-length table exp(-2*pi*i*k/N), k < N, built on the
 // host in double precision and staged into shared memory by the caller.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace marie {
 
 template <int... Rs> struct RList {};
 
-// Radix schedule per FFT length.  E = lcm of the radices (values per thread).
+// Reversed radix list: the inverse transform runs the forward schedule
+// backwards, so its first pass consumes the registers exactly as the forward
+// transform's last pass left them (no exchange between a forward transform, a
+// pointwise product and the inverse transform).
+template <typename A, typename B> struct RCat;
+template <int... A, int... B> struct RCat<RList<A...>, RList<B...>> { using type = RList<A..., B...>; };
+template <typename L> struct RRev;
+template <> struct RRev<RList<>> { using type = RList<>; };
+template <int R0, int... Rs> struct RRev<RList<R0, Rs...>> {
+  using type = typename RCat<typename RRev<RList<Rs...>>::type, RList<R0>>::type;
+};
+
+// Radix schedule per FFT length for 4-byte reals (FP32): radix-16 passes keep
+// 16 complex values per thread and halve the exchanges of the 256-point
+// transform.  E = lcm of the radices (values per thread).
+template <int N> struct FFTCfgWide;
+template <> struct FFTCfgWide<16>  { using R = RList<16>;     static constexpr int E = 16; };
+template <> struct FFTCfgWide<128> { using R = RList<16, 8>;  static constexpr int E = 16; };
+template <> struct FFTCfgWide<256> { using R = RList<16, 16>; static constexpr int E = 16; };
+
+// Radix schedule per FFT length (FP64, and FP32 lengths without a wide entry).
 // The first radix is even so that a zero-padded input (only the first N/2
 // values non-zero) skips the loads of the known-zero half in the first pass.
 template <int N> struct FFTCfg;
@@ -131,13 +153,96 @@ template <bool INV> struct DFT<5, INV> {
   }
 };
 
+template <bool INV> struct DFT<16, INV> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    V a[8], b[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      a[k] = cadd(v[k], v[k + 8]);
+      b[k] = csub(v[k], v[k + 8]);
+    }
+    twiddle16(b);
+    DFT<8, INV>::run(a);
+    DFT<8, INV>::run(b);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      v[2 * q] = a[q];
+      v[2 * q + 1] = b[q];
+    }
+  }
+  // upper half of the inputs is zero (zero-padded transform)
+  template <typename V> __device__ __forceinline__ static void run_half(V* v) {
+    V a[8], b[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = b[k] = v[k];
+    twiddle16(b);
+    DFT<8, INV>::run(a);
+    DFT<8, INV>::run(b);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      v[2 * q] = a[q];
+      v[2 * q + 1] = b[q];
+    }
+  }
+  // b[k] *= exp(-+ 2 pi i k / 16), k = 1..7
+  template <typename V> __device__ __forceinline__ static void twiddle16(V* b) {
+    using T = decltype(V::x);
+    const T c1 = (T)0.92387953251128675613;  // cos(pi/8)
+    const T s1 = (T)0.38268343236508977173;  // sin(pi/8)
+    const T h = (T)0.70710678118654752440;   // cos(pi/4)
+    const T sg = INV ? (T)1 : (T)-1;         // sign of the imaginary part of the root
+    const T wr[8] = {1, c1, h, s1, 0, -s1, -h, -c1};
+    const T wi[8] = {0, s1, h, c1, 1, c1, h, s1};
+#pragma unroll
+    for (int k = 1; k < 8; ++k) {
+      if (k == 4) {
+        b[4] = rot90<INV>(b[4]);
+      } else {
+        const T ci = sg * wi[k];
+        b[k] = mk<V>(b[k].x * wr[k] - b[k].y * ci, b[k].x * ci + b[k].y * wr[k]);
+      }
+    }
+  }
+};
+
+// DFT of R values whose upper half is zero.  Radix 16 and 8 skip the first
+// butterfly stage; other radices run the full transform on the zeros.
+template <int R, bool INV> struct DFTHalf {
+  template <typename V> __device__ __forceinline__ static void run(V* v) { DFT<R, INV>::run(v); }
+};
+template <bool INV> struct DFTHalf<16, INV> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) { DFT<16, INV>::run_half(v); }
+};
+template <bool INV> struct DFTHalf<8, INV> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    using T = decltype(V::x);
+    const T h = (T)0.70710678118654752440;
+    V a[4], b[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a[k] = b[k] = v[k];
+    b[1] = INV ? mk<V>(h * (b[1].x - b[1].y), h * (b[1].x + b[1].y))
+               : mk<V>(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x));
+    b[2] = rot90<INV>(b[2]);
+    b[3] = INV ? mk<V>(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y))
+               : mk<V>(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y));
+    DFT<4, INV>::run(a);
+    DFT<4, INV>::run(b);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      v[2 * q] = a[q];
+      v[2 * q + 1] = b[q];
+    }
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Pass recursion.  reg[b*R + r] holds input r of butterfly j = t + b*T.
+// HALF: the inputs of this (first) pass have a zero upper half.
 // ---------------------------------------------------------------------------
-template <typename V, int N, int E, bool INV, int NS, typename L> struct Passes;
+template <typename V, int N, int E, bool INV, int NS, bool HALF, typename L> struct Passes;
 
-template <typename V, int N, int E, bool INV, int NS, int R, int... Rest>
-struct Passes<V, N, E, INV, NS, RList<R, Rest...>> {
+template <typename V, int N, int E, bool INV, int NS, bool HALF, int R, int... Rest>
+struct Passes<V, N, E, INV, NS, HALF, RList<R, Rest...>> {
   static constexpr int T = N / E;
   static constexpr int NB = E / R;
   static_assert(E % R == 0, "E must be a multiple of every radix");
@@ -157,7 +262,10 @@ struct Passes<V, N, E, INV, NS, RList<R, Rest...>> {
           v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
         }
       }
-      DFT<R, INV>::run(v);
+      if (HALF)
+        DFTHalf<R, INV>::run(v);
+      else
+        DFT<R, INV>::run(v);
     }
     if constexpr (sizeof...(Rest) > 0) {
       constexpr int R2 = RFirst<RList<Rest...>>::value;
@@ -175,7 +283,7 @@ struct Passes<V, N, E, INV, NS, RList<R, Rest...>> {
 #pragma unroll
         for (int r = 0; r < R2; ++r) reg[b * R2 + r] = base[(t + b * T + r * (N / R2)) * es];
       }
-      Passes<V, N, E, INV, NS * R, RList<Rest...>>::run(reg, base, es, t, tw);
+      Passes<V, N, E, INV, NS * R, false, RList<Rest...>>::run(reg, base, es, t, tw);
     }
   }
 };
@@ -189,14 +297,35 @@ template <int N, int E, int NS, int R> struct LastPass<N, E, NS, RList<R>> {
 template <int N, int E, int NS, int R, int R2, int... Rest>
 struct LastPass<N, E, NS, RList<R, R2, Rest...>> : LastPass<N, E, NS * R, RList<R2, Rest...>> {};
 
+template <int N> struct HasWide { static constexpr bool value = false; };
+template <> struct HasWide<16> { static constexpr bool value = true; };
+template <> struct HasWide<128> { static constexpr bool value = true; };
+template <> struct HasWide<256> { static constexpr bool value = true; };
+
+template <typename V, int N, bool W = (sizeof(V) == 8) && HasWide<N>::value> struct Sched {
+  using R = typename FFTCfg<N>::R;
+  static constexpr int E = FFTCfg<N>::E;
+};
+template <typename V, int N> struct Sched<V, N, true> {
+  using R = typename FFTCfgWide<N>::R;
+  static constexpr int E = FFTCfgWide<N>::E;
+};
+
+// Transform of length N on values of type V (float2 / double2).  The forward
+// transform uses the schedule's radix list; the inverse uses it reversed, so
+// reg after FFT<V,N,false>::run is directly the input of FFT<V,N,true>::run.
 template <typename V, int N, bool INV> struct FFT {
-  using Cfg = FFTCfg<N>;
-  static constexpr int E = Cfg::E;
+  using RF = typename Sched<V, N>::R;
+  using RL_ = typename std::conditional<INV, typename RRev<RF>::type, RF>::type;
+  static constexpr int E = Sched<V, N>::E;
   static constexpr int T = N / E;
-  static constexpr int R0 = RFirst<typename Cfg::R>::value;
-  using LP = LastPass<N, E, 1, typename Cfg::R>;
+  static constexpr int R0 = RFirst<RL_>::value;
+  using LP = LastPass<N, E, 1, RL_>;
   static constexpr int RL = LP::R_last;
   static constexpr int NSL = LP::NS_last;
+
+  // Input position of reg[b*R0 + r] for the first pass.
+  __device__ __forceinline__ static int in_pos(int t, int b, int r) { return t + b * T + r * (N / R0); }
 
   // Load the first pass's inputs from shared memory.  Positions >= n_valid are
   // treated as zero without being read (zero padding).
@@ -205,25 +334,30 @@ template <typename V, int N, bool INV> struct FFT {
     for (int b = 0; b < E / R0; ++b) {
 #pragma unroll
       for (int r = 0; r < R0; ++r) {
-        const int p = t + b * T + r * (N / R0);
+        const int p = in_pos(t, b, r);
         reg[b * R0 + r] = (p < n_valid) ? base[p * es] : mk<V>(0, 0);
       }
     }
   }
-  // Same, but the caller guarantees n_valid <= N/2 at compile time shape: the
-  // upper half of every first-pass butterfly is zero.
+  // Same, but the caller guarantees n_valid <= N/2: the upper half of every
+  // first-pass butterfly is zero.  Pair with run_half().
   __device__ __forceinline__ static void load_half(V* reg, const V* base, int es, int t, int n_valid) {
 #pragma unroll
     for (int b = 0; b < E / R0; ++b) {
 #pragma unroll
       for (int r = 0; r < R0; ++r) {
-        const int p = t + b * T + r * (N / R0);
+        const int p = in_pos(t, b, r);
         reg[b * R0 + r] = (r < R0 / 2 && p < n_valid) ? base[p * es] : mk<V>(0, 0);
       }
     }
   }
   __device__ __forceinline__ static void run(V* reg, V* base, int es, int t, const V* tw) {
-    Passes<V, N, E, INV, 1, typename Cfg::R>::run(reg, base, es, t, tw);
+    Passes<V, N, E, INV, 1, false, RL_>::run(reg, base, es, t, tw);
+  }
+  // First pass on inputs with a zero upper half (R0 even).
+  __device__ __forceinline__ static void run_half(V* reg, V* base, int es, int t, const V* tw) {
+    static_assert(R0 % 2 == 0, "zero-half skipping needs an even first radix");
+    Passes<V, N, E, INV, 1, true, RL_>::run(reg, base, es, t, tw);
   }
   // Output position of reg[b*RL + r] after run().
   __device__ __forceinline__ static int out_pos(int t, int b, int r) {

@@ -1,3 +1,3 @@
 // FP64 instantiation of the matvec passes.
-#include "matvec_launch.cuh"
+#include "matvec_impl.cuh"
 template struct marie::MatvecLaunch<double>;

@@ -92,7 +92,7 @@ k_xfwd(const double2* __restrict__ J, long long j_stride, const int* __restrict_
   const int s = threadIdx.x % S, t = threadIdx.x / S;
   V reg[F::E];
   F::load_half(reg, buf + s, ES, t, d.L);
-  F::run(reg, buf + s, ES, t, tw_s);
+  F::run_half(reg, buf + s, ES, t, tw_s);
   __syncthreads();
   F::store(reg, buf + s, ES, t);
   __syncthreads();
@@ -167,6 +167,10 @@ k_xinv(const cplx<T>* __restrict__ A, long long a_stride, const double2* __restr
 // ---------------------------------------------------------------------------
 template <typename T> struct ColS { static constexpr int S = 128 / (int)sizeof(cplx<T>); };
 
+// Columns are loaded straight into the first pass's registers and the last
+// pass's registers are stored straight to global memory: lanes run over S
+// consecutive kx (one 128-byte row segment per warp access), the FFT's
+// exchanges go through shared memory only.
 template <typename T, int NC, bool INV>
 __global__ void __launch_bounds__(ColS<T>::S * FFT<cplx<T>, NC, INV>::T)
 k_cols(const cplx<T>* __restrict__ in, long long in_w, long long in_rhs, int n_in,
@@ -176,6 +180,7 @@ k_cols(const cplx<T>* __restrict__ in, long long in_w, long long in_rhs, int n_i
   using F = FFT<V, NC, INV>;
   constexpr int S = ColS<T>::S;
   constexpr int ES = S + 1;
+  constexpr int E = F::E, R0 = F::R0, RL = F::RL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw_s = reinterpret_cast<V*>(smem_raw);
   V* buf = tw_s + NC;
@@ -184,31 +189,46 @@ k_cols(const cplx<T>* __restrict__ in, long long in_w, long long in_rhs, int n_i
   const V* inp = in + blockIdx.z * in_rhs + w * in_w + kx0;
   V* outp = out + blockIdx.z * out_rhs + w * out_w + kx0;
   stage_twiddles(tw_s, tw, NC);
-  for (int i = threadIdx.x; i < S * n_in; i += blockDim.x) {
-    const int y = i / S, s = i - y * S;
-    buf[y * ES + s] = (kx0 + s < Lp) ? inp[(long long)y * Lp + s] : mk<V>(0, 0);
-  }
-  __syncthreads();
   const int s = threadIdx.x % S, t = threadIdx.x / S;
-  V reg[F::E];
-  if (!INV && 2 * n_in <= NC)
-    F::load_half(reg, buf + s, ES, t, n_in);
-  else
-    F::load(reg, buf + s, ES, t, n_in);
-  F::run(reg, buf + s, ES, t, tw_s);
-  __syncthreads();
-  F::store(reg, buf + s, ES, t);
-  __syncthreads();
-  for (int i = threadIdx.x; i < S * n_out; i += blockDim.x) {
-    const int y = i / S, ss = i - y * S;
-    if (kx0 + ss < Lp) outp[(long long)y * Lp + ss] = buf[y * ES + ss];
+  const bool active = kx0 + s < Lp;
+  const bool half = !INV && 2 * n_in <= NC;
+  V reg[E];
+#pragma unroll
+  for (int b = 0; b < E / R0; ++b)
+#pragma unroll
+    for (int r = 0; r < R0; ++r) {
+      const int p = F::in_pos(t, b, r);
+      const bool ok = active && p < n_in && (!half || r < R0 / 2);
+      reg[b * R0 + r] = ok ? inp[(long long)p * Lp + s] : mk<V>(0, 0);
+    }
+  __syncthreads();  // twiddles staged
+  if constexpr (!INV && R0 % 2 == 0) {
+    if (half)
+      F::run_half(reg, buf + s, ES, t, tw_s);
+    else
+      F::run(reg, buf + s, ES, t, tw_s);
+  } else {
+    F::run(reg, buf + s, ES, t, tw_s);
   }
+#pragma unroll
+  for (int b = 0; b < E / RL; ++b)
+#pragma unroll
+    for (int r = 0; r < RL; ++r) {
+      const int y = F::out_pos(t, b, r);
+      if (active && y < n_out) outp[(long long)y * Lp + s] = reg[b * RL + r];
+    }
 }
 
 // ---------------------------------------------------------------------------
 // zmul: per (kx, ky) column: forward z transform of the three components,
 // symmetric 3x3 multiply by fN, inverse z transform, keep z < N.  In place.
-// B[c][z][ky][kx], fN[q][kz][ky][kx].  grid.x = Lp / S, grid.y = Mp, grid.z = rhs
+// B[c][z][ky][kx].  grid.x = Lp / S, grid.y = Mp, grid.z = rhs
+//
+// Operator storage (oct = 1): the circulant's per-axis parities make
+// fN(2L-kx, ky, kz) = +-fN(kx, ky, kz) (sign = parity of the component along the
+// reflected axis), so only the octant k <= (L, M, N) is kept:
+// fNo[q][oz][oy][ox], (L+1) x (M+1) x (N+1) per component.  oct = 0: full
+// fN[q][kz][ky][kx].
 // ---------------------------------------------------------------------------
 template <typename T, int NZ> struct ZS {
   static constexpr int S0 = ColS<T>::S;
@@ -217,73 +237,96 @@ template <typename T, int NZ> struct ZS {
   static constexpr int THREADS = S * FFT<cplx<T>, NZ, false>::T;
 };
 
+// odd components along x, y, z: xy (1), xz (2) | xy (1), yz (4) | xz (2), yz (4)
+__device__ __forceinline__ bool odd_x(int q) { return q == 1 || q == 2; }
+__device__ __forceinline__ bool odd_y(int q) { return q == 1 || q == 4; }
+__device__ __forceinline__ bool odd_z(int q) { return q == 2 || q == 4; }
+
 template <typename T, int NZ>
 __global__ void __launch_bounds__(ZS<T, NZ>::THREADS)
-k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN, Dims d,
+k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN, int oct, Dims d,
        const cplx<T>* __restrict__ tw) {
   using V = cplx<T>;
   using FF = FFT<V, NZ, false>;
   using FI = FFT<V, NZ, true>;
   constexpr int S = ZS<T, NZ>::S;
   constexpr int ES = S + 1;
+  constexpr int E = FF::E, R0 = FF::R0, RL = FF::RL, RLI = FI::RL;
+  static_assert(FI::R0 == RL, "inverse must start where the forward transform ended");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw_s = reinterpret_cast<V*>(smem_raw);
-  V* buf = tw_s + NZ;  // 3 components x NZ x ES
+  V* buf = tw_s + NZ;  // 3 exchange buffers of NZ x ES
   const int kx0 = blockIdx.x * S;
   const int ky = blockIdx.y;
-  const long long plane = (long long)d.Lp * d.Mp;            // one z-plane of B
-  const long long comp = plane * d.N;                        // one component of B
+  const long long plane = (long long)d.Lp * d.Mp;  // one z-plane of B
+  const long long comp = plane * d.N;               // one component of B
   V* Bp = B + blockIdx.z * b_rhs + (long long)ky * d.Lp + kx0;
   stage_twiddles(tw_s, tw, NZ);
-  for (int i = threadIdx.x; i < 3 * S * d.N; i += blockDim.x) {
-    const int c = i / (S * d.N);
-    const int rem = i - c * S * d.N;
-    const int z = rem / S, s = rem - z * S;
-    buf[(c * NZ + z) * ES + s] = (kx0 + s < d.Lp) ? Bp[c * comp + z * plane + s] : mk<V>(0, 0);
-  }
-  __syncthreads();
   const int s = threadIdx.x % S, t = threadIdx.x / S;
-  V reg[FF::E];
-#pragma unroll 1
-  for (int c = 0; c < 3; ++c) {
-    V* base = buf + c * NZ * ES + s;
-    FF::load_half(reg, base, ES, t, d.N);
-    FF::run(reg, base, ES, t, tw_s);
-    __syncthreads();
-    FF::store(reg, base, ES, t);
-    __syncthreads();
+  const int kx = kx0 + s;
+  const bool active = kx < d.Lp;
+  V reg[3][E];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int b = 0; b < E / R0; ++b)
+#pragma unroll
+      for (int r = 0; r < R0; ++r) {
+        const int p = FF::in_pos(t, b, r);
+        reg[c][b * R0 + r] = (active && r < R0 / 2 && p < d.N) ? Bp[c * comp + p * plane + s] : mk<V>(0, 0);
+      }
+  __syncthreads();  // twiddles staged
+#pragma unroll
+  for (int c = 0; c < 3; ++c) FF::run_half(reg[c], buf + c * NZ * ES + s, ES, t, tw_s);
+
+  // symmetric tensor multiply on the registers
+  int ox = kx, oy = ky;
+  bool fx = false, fy = false;
+  if (oct) {
+    if (kx > d.L) { ox = d.Lp - kx; fx = true; }
+    if (ky > d.M) { oy = d.Mp - ky; fy = true; }
   }
-  // symmetric tensor multiply
-  const long long fq = (long long)d.Lp * d.Mp * d.Np;
-  const V* fp = fN + (long long)ky * d.Lp + kx0;
-  for (int i = threadIdx.x; i < S * NZ; i += blockDim.x) {
-    const int kz = i / S, ss = i - kz * S;
-    const long long o = (long long)kz * plane + ss;
-    if (kx0 + ss >= d.Lp) continue;
-    const V nxx = fp[o], nxy = fp[fq + o], nxz = fp[2 * fq + o];
-    const V nyy = fp[3 * fq + o], nyz = fp[4 * fq + o], nzz = fp[5 * fq + o];
-    V* e = buf + kz * ES + ss;
-    const V jx = e[0], jy = e[NZ * ES], jz = e[2 * NZ * ES];
-    e[0] = cadd(cadd(cmul(nxx, jx), cmul(nxy, jy)), cmul(nxz, jz));
-    e[NZ * ES] = cadd(cadd(cmul(nxy, jx), cmul(nyy, jy)), cmul(nyz, jz));
-    e[2 * NZ * ES] = cadd(cadd(cmul(nxz, jx), cmul(nyz, jy)), cmul(nzz, jz));
-  }
-  __syncthreads();
-#pragma unroll 1
-  for (int c = 0; c < 3; ++c) {
-    V* base = buf + c * NZ * ES + s;
-    FI::load(reg, base, ES, t, NZ);
-    FI::run(reg, base, ES, t, tw_s);
-    __syncthreads();
-    FI::store(reg, base, ES, t);
-    __syncthreads();
-  }
-  for (int i = threadIdx.x; i < 3 * S * d.N; i += blockDim.x) {
-    const int c = i / (S * d.N);
-    const int rem = i - c * S * d.N;
-    const int z = rem / S, ss = rem - z * S;
-    if (kx0 + ss < d.Lp) Bp[c * comp + z * plane + ss] = buf[(c * NZ + z) * ES + ss];
-  }
+  const long long fq = oct ? (long long)(d.L + 1) * (d.M + 1) * (d.N + 1) : (long long)d.Lp * d.Mp * d.Np;
+  const long long fplane = oct ? (long long)(d.L + 1) * (d.M + 1) : plane;
+  const long long frow = oct ? (long long)(d.L + 1) : d.Lp;
+  const V* fp = fN + (long long)oy * frow + ox;
+#pragma unroll
+  for (int b = 0; b < E / RL; ++b)
+#pragma unroll
+    for (int r = 0; r < RL; ++r) {
+      const int kz = FF::out_pos(t, b, r);
+      int oz = kz;
+      bool fz = false;
+      if (oct && kz > d.N) { oz = d.Np - kz; fz = true; }
+      V n6[6];
+      if (active) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          V v = fp[q * fq + oz * fplane];
+          const bool neg = (fx && odd_x(q)) ^ (fy && odd_y(q)) ^ (fz && odd_z(q));
+          n6[q] = neg ? mk<V>(-v.x, -v.y) : v;
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) n6[q] = mk<V>(0, 0);
+      }
+      const int i = b * RL + r;
+      const V jx = reg[0][i], jy = reg[1][i], jz = reg[2][i];
+      reg[0][i] = cadd(cadd(cmul(n6[0], jx), cmul(n6[1], jy)), cmul(n6[2], jz));
+      reg[1][i] = cadd(cadd(cmul(n6[1], jx), cmul(n6[3], jy)), cmul(n6[4], jz));
+      reg[2][i] = cadd(cadd(cmul(n6[2], jx), cmul(n6[4], jy)), cmul(n6[5], jz));
+    }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) FI::run(reg[c], buf + c * NZ * ES + s, ES, t, tw_s);
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int b = 0; b < E / RLI; ++b)
+#pragma unroll
+      for (int r = 0; r < RLI; ++r) {
+        const int z = FI::out_pos(t, b, r);
+        if (active && z < d.N) Bp[c * comp + z * plane + s] = reg[c][b * RLI + r];
+      }
 }
 
 }  // namespace marie

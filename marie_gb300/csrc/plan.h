@@ -14,10 +14,11 @@ struct marie_plan {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
 
-  // Operator, full 2L x 2M x 2N x 6 layout, pre-scaled by 1/(8LMN).
+  // Operator, pre-scaled by 1/(8LMN): octant or full 2L x 2M x 2N x 6 layout.
   double2* fN64 = nullptr;
   float2* fN32 = nullptr;
   bool has_op = false;
+  int oct = 0;  // 1: fN64/fN32 hold the (L+1)(M+1)(N+1) octant, 0: the full array
 
   // Twiddle tables exp(-2*pi*i*k/n) for the three padded axis lengths.
   double2* tw64[3] = {nullptr, nullptr, nullptr};
