@@ -128,6 +128,16 @@ int marie_jvie_solve(marie_plan* plan, const double* Einc, const double* e_r, do
                      int outer_it, double* Je, int* flag, double* relres, int* iter,
                      double* resvec, int64_t resvec_cap, int64_t* resvec_len, double* solvert);
 
+/* JVIE_Solver for nexc excitations of one body solved together: Einc and Je
+ * are nexc consecutive L x M x N x 3 arrays; the solves advance in lockstep
+ * (one batched matvec per GMRES step, one graph launch per restart cycle).
+ * Per excitation: flag[e], relres[e], iter[2e..2e+1].  The reference solves
+ * excitations one at a time (JVIE_Solver.m is called per port/excitation). */
+int marie_jvie_solve_batch(marie_plan* plan, const double* Einc, int64_t nexc, const double* e_r,
+                           double dx, double freq, int form, char precond, double tol, int inner_it,
+                           int outer_it, double* Je, int* flag, double* relres, int* iter,
+                           double* solvert);
+
 /* Replaces E_field_Nop(J, fN, Gram, freq, Einc) (src_vie/src_fields/src_op/
  * E_field_Nop.m:59-84): Etot = Einc + (N J - Gram J)/(Gram*j*omega*eps0).
  * J, Einc (may be NULL), Etot: L x M x N x 3 complex. */

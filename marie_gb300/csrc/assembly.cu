@@ -323,11 +323,11 @@ __global__ void k_circulant(const double2* __restrict__ G, int L, int M, int N, 
 
 // plain in-place forward FFT of contiguous rows of length NL (full input)
 template <int NL>
-__global__ void __launch_bounds__(RowCfg<NL>::THREADS)
+__global__ void __launch_bounds__(RowCfg<double2, NL>::THREADS)
 k_rows_full(double2* __restrict__ data, long long rows, const double2* __restrict__ tw) {
   using V = double2;
   using F = FFT<V, NL, false>;
-  constexpr int S = RowCfg<NL>::S;
+  constexpr int S = RowCfg<double2, NL>::S;
   constexpr int ES = S + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw_s = reinterpret_cast<V*>(smem_raw);
@@ -356,11 +356,11 @@ static cudaError_t rows_full(int NL, double2* data, long long rows, const double
   switch (NL) {
 #define MARIE_CASE(n_)                                                                                   \
   case n_: {                                                                                             \
-    constexpr int S = RowCfg<n_>::S;                                                                     \
+    constexpr int S = RowCfg<double2, n_>::S;                                                                     \
     const size_t smem = (size_t)(n_ + n_ * (S + 1)) * sizeof(double2);                                   \
     cudaError_t e = opt_in_smem(k_rows_full<n_>, smem);                                                  \
     if (e != cudaSuccess) return e;                                                                      \
-    k_rows_full<n_><<<(unsigned)((rows + S - 1) / S), RowCfg<n_>::THREADS, smem, st>>>(data, rows, tw); \
+    k_rows_full<n_><<<(unsigned)((rows + S - 1) / S), RowCfg<double2, n_>::THREADS, smem, st>>>(data, rows, tw); \
     count_launch();                                                                                      \
     return cudaGetLastError();                                                                           \
   }

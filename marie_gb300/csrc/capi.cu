@@ -3,6 +3,9 @@
 #include <cmath>
 #include <cstdarg>
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -15,6 +18,24 @@ static thread_local char g_err[512] = "";
 static std::atomic<long long> g_launches{0};
 
 void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+static std::mutex g_smem_mu;
+static std::map<std::pair<const void*, int>, size_t> g_smem_set;  // (kernel, device) -> bytes
+
+bool smem_opted_in(const void* kernel, size_t bytes) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> g(g_smem_mu);
+  auto it = g_smem_set.find({kernel, dev});
+  return it != g_smem_set.end() && it->second >= bytes;
+}
+void smem_mark_opted_in(const void* kernel, size_t bytes) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> g(g_smem_mu);
+  size_t& v = g_smem_set[{kernel, dev}];
+  if (bytes > v) v = bytes;
+}
 
 int set_error(int code, const char* fmt, ...) {
   va_list ap;
@@ -75,9 +96,9 @@ int finish_out(void* user, const void* dev, size_t bytes, cudaStream_t st) {
   return MARIE_OK;
 }
 
-int ensure_workspace(marie_plan* p, int prec, long long nrhs) {
+int ensure_workspace(marie_plan* p, int prec, long long nrhs, bool with_A) {
   const size_t es = (prec == MARIE_FP32) ? sizeof(float2) : sizeof(double2);
-  const size_t need_A = (size_t)p->elems_A() * es * nrhs;
+  const size_t need_A = with_A ? (size_t)p->elems_A() * es * nrhs : 0;
   const size_t need_B = (size_t)p->elems_B() * es * nrhs;
   if (need_A > p->ws_bytes_A) {
     if (p->wsA) cudaFreeAsync(p->wsA, p->stream);
@@ -187,34 +208,53 @@ int build_coefficients(marie_plan* p, const int64_t* idx_dev, long long n, const
 }
 
 template <typename T>
-static int run_matvec_t(marie_plan* p, const double2* J, double2* out, long long n, int nrhs, const int* inv,
-                        const Prologue& pro, const Epilogue& ep, const cplx<T>* fN, cplx<T>* const* tw) {
+static int run_matvec_t(marie_plan* p, const double2* J, long long js, double2* out, long long os, long long n,
+                        int nrhs, const int* inv, const Prologue& pro, const Epilogue& ep, const cplx<T>* fN,
+                        cplx<T>* const* tw, const int* stop, int step) {
   using ML = MatvecLaunch<T>;
-  const Dims& d = p->d;
   const int prec = sizeof(T) == 4 ? MARIE_FP32 : MARIE_FP64;
   const long long chunk_max = p->nrhs_max > 0 ? p->nrhs_max : 1;
+  const bool fused = p->fuse && ML::fused(p->d);
   for (long long r0 = 0; r0 < nrhs; r0 += chunk_max) {
     const int nr = (int)((nrhs - r0) < chunk_max ? (nrhs - r0) : chunk_max);
-    MARIE_TRY(ensure_workspace(p, prec, nr));
+    MARIE_TRY(ensure_workspace(p, prec, nr, !fused));
+    Dims d = p->d;
+    d.stop = stop ? stop + r0 : nullptr;
+    d.step = step;
     cplx<T>* A = reinterpret_cast<cplx<T>*>(p->wsA);
     cplx<T>* B = reinterpret_cast<cplx<T>*>(p->wsB);
     const long long sA = p->elems_A(), sB = p->elems_B();
-    const double2* Jc = J + r0 * n;
-    double2* oc = out + r0 * n;
+    const double2* Jc = J + r0 * js;
+    double2* oc = out + r0 * os;
     const bool prof = p->profile;
     if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[0], p->stream));
-    MARIE_CUDA_TRY(ML::xfwd(Jc, n, inv, pro, A, sA, d, tw[0], nr, p->stream));
-    if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[1], p->stream));
-    MARIE_CUDA_TRY(ML::cols(false, d.Mp, A, (long long)d.Lp * d.M, sA, d.M, B, (long long)d.Lp * d.Mp, sB, d.Mp,
-                            d.Lp, 3 * d.N, tw[1], nr, p->stream));
-    if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
-    MARIE_CUDA_TRY(ML::zmul(B, sB, fN, p->oct, d, tw[2], nr, p->stream));
-    if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
-    MARIE_CUDA_TRY(ML::cols(true, d.Mp, B, (long long)d.Lp * d.Mp, sB, d.Mp, A, (long long)d.Lp * d.M, sA, d.M,
-                            d.Lp, 3 * d.N, tw[1], nr, p->stream));
-    if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[4], p->stream));
-    MARIE_CUDA_TRY(ML::xinv(A, sA, Jc, n, inv, ep, oc, n, d, tw[0], nr, p->stream));
-    count_launch(5);
+    if (fused) {
+      MARIE_CUDA_TRY(ML::xyfwd(Jc, js, inv, pro, B, sB, d, tw[0], tw[1], nr, p->stream));
+      if (prof) {
+        MARIE_CUDA_TRY(cudaEventRecord(p->ev[1], p->stream));
+        MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
+      }
+      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, p->oct, d, tw[2], nr, p->stream));
+      if (prof) {
+        MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
+        MARIE_CUDA_TRY(cudaEventRecord(p->ev[4], p->stream));
+      }
+      MARIE_CUDA_TRY(ML::yxinv(B, sB, Jc, js, inv, ep, oc, os, d, tw[0], tw[1], nr, p->stream));
+      count_launch(3);
+    } else {
+      MARIE_CUDA_TRY(ML::xfwd(Jc, js, inv, pro, A, sA, d, tw[0], nr, p->stream));
+      if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[1], p->stream));
+      MARIE_CUDA_TRY(ML::cols(false, d.Mp, A, (long long)d.Lp * d.M, sA, d.M, B, (long long)d.Lp * d.Mp, sB, d.Mp,
+                              d.Lp, 3 * d.N, tw[1], nr, p->stream, d.stop, step));
+      if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
+      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, p->oct, d, tw[2], nr, p->stream));
+      if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
+      MARIE_CUDA_TRY(ML::cols(true, d.Mp, B, (long long)d.Lp * d.Mp, sB, d.Mp, A, (long long)d.Lp * d.M, sA, d.M,
+                              d.Lp, 3 * d.N, tw[1], nr, p->stream, d.stop, step));
+      if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[4], p->stream));
+      MARIE_CUDA_TRY(ML::xinv(A, sA, Jc, js, inv, ep, oc, os, d, tw[0], nr, p->stream));
+      count_launch(5);
+    }
     if (prof) {
       MARIE_CUDA_TRY(cudaEventRecord(p->ev[5], p->stream));
       MARIE_CUDA_TRY(cudaEventSynchronize(p->ev[5]));
@@ -229,15 +269,20 @@ static int run_matvec_t(marie_plan* p, const double2* J, double2* out, long long
   return MARIE_OK;
 }
 
-int run_matvec(marie_plan* p, int prec, const double2* J, double2* out, long long n, int nrhs, const int* inv,
-               const Prologue& pro, const Epilogue& ep) {
+int run_matvec(marie_plan* p, int prec, const double2* J, long long js, double2* out, long long os, long long n,
+               int nrhs, const int* inv, const Prologue& pro, const Epilogue& ep, const int* stop, int step) {
   if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator: call marie_set_operator or marie_plan_assemble");
   if (prec == MARIE_FP32) {
     if (!p->fN32) return set_error(MARIE_EINVAL, "plan was not created with FP32 arithmetic");
-    return run_matvec_t<float>(p, J, out, n, nrhs, inv, pro, ep, p->fN32, p->tw32);
+    return run_matvec_t<float>(p, J, js, out, os, n, nrhs, inv, pro, ep, p->fN32, p->tw32, stop, step);
   }
   if (!p->fN64) return set_error(MARIE_EINVAL, "plan was not created with FP64 arithmetic");
-  return run_matvec_t<double>(p, J, out, n, nrhs, inv, pro, ep, p->fN64, p->tw64);
+  return run_matvec_t<double>(p, J, js, out, os, n, nrhs, inv, pro, ep, p->fN64, p->tw64, stop, step);
+}
+
+int run_matvec(marie_plan* p, int prec, const double2* J, double2* out, long long n, int nrhs, const int* inv,
+               const Prologue& pro, const Epilogue& ep) {
+  return run_matvec(p, prec, J, n, out, n, n, nrhs, inv, pro, ep, nullptr, 0);
 }
 
 // twiddles exp(-2*pi*i*k/n), built in double on the host
@@ -402,6 +447,10 @@ int marie_plan_create(int64_t L, int64_t M, int64_t N, int precision, int64_t nr
   p->d.V = L * M * N;
   p->precision = precision;
   p->nrhs_max = nrhs_max > 0 ? nrhs_max : 1;
+  {
+    const char* nf = getenv("MARIE_NO_FUSED");  // forces the five-pass matvec (comparison runs)
+    p->fuse = !(nf && nf[0] == '1');
+  }
   cudaGetDevice(&p->device);
   if (stream) {
     p->stream = (cudaStream_t)stream;

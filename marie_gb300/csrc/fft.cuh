@@ -23,6 +23,16 @@ namespace marie {
 
 template <int... Rs> struct RList {};
 
+// Shared-memory addressing of position p of a sequence: p*es, plus one pad
+// element every 16 positions when swz is set (row layouts, where the first
+// pass writes with stride R and would otherwise hit one bank).
+struct SAddr {
+  int es, m;
+  __host__ __device__ SAddr(int e) : es(e), m(0) {}
+  __host__ __device__ SAddr(int e, bool swz) : es(e), m(swz ? -1 : 0) {}
+  __device__ __forceinline__ int operator()(int p) const { return p * es + ((p >> 4) & m); }
+};
+
 // Reversed radix list: the inverse transform runs the forward schedule
 // backwards, so its first pass consumes the registers exactly as the forward
 // transform's last pass left them (no exchange between a forward transform, a
@@ -249,7 +259,7 @@ struct Passes<V, N, E, INV, NS, HALF, RList<R, Rest...>> {
 
   // Runs this pass and all following ones.  After return, reg[b*R_last + r]
   // holds output position out_pos(t, b, r) of the last pass.
-  __device__ __forceinline__ static void run(V* reg, V* base, int es, int t, const V* tw) {
+  __device__ __forceinline__ static void run(V* reg, V* base, SAddr es, int t, const V* tw) {
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
       const int j = t + b * T;
@@ -275,13 +285,13 @@ struct Passes<V, N, E, INV, NS, HALF, RList<R, Rest...>> {
         const int j = t + b * T;
         const int d = (j / NS) * NS * R + (j % NS);
 #pragma unroll
-        for (int r = 0; r < R; ++r) base[(d + r * NS) * es] = reg[b * R + r];
+        for (int r = 0; r < R; ++r) base[es(d + r * NS)] = reg[b * R + r];
       }
       __syncthreads();
 #pragma unroll
       for (int b = 0; b < E / R2; ++b) {
 #pragma unroll
-        for (int r = 0; r < R2; ++r) reg[b * R2 + r] = base[(t + b * T + r * (N / R2)) * es];
+        for (int r = 0; r < R2; ++r) reg[b * R2 + r] = base[es(t + b * T + r * (N / R2))];
       }
       Passes<V, N, E, INV, NS * R, false, RList<Rest...>>::run(reg, base, es, t, tw);
     }
@@ -329,33 +339,33 @@ template <typename V, int N, bool INV> struct FFT {
 
   // Load the first pass's inputs from shared memory.  Positions >= n_valid are
   // treated as zero without being read (zero padding).
-  __device__ __forceinline__ static void load(V* reg, const V* base, int es, int t, int n_valid) {
+  __device__ __forceinline__ static void load(V* reg, const V* base, SAddr es, int t, int n_valid) {
 #pragma unroll
     for (int b = 0; b < E / R0; ++b) {
 #pragma unroll
       for (int r = 0; r < R0; ++r) {
         const int p = in_pos(t, b, r);
-        reg[b * R0 + r] = (p < n_valid) ? base[p * es] : mk<V>(0, 0);
+        reg[b * R0 + r] = (p < n_valid) ? base[es(p)] : mk<V>(0, 0);
       }
     }
   }
   // Same, but the caller guarantees n_valid <= N/2: the upper half of every
   // first-pass butterfly is zero.  Pair with run_half().
-  __device__ __forceinline__ static void load_half(V* reg, const V* base, int es, int t, int n_valid) {
+  __device__ __forceinline__ static void load_half(V* reg, const V* base, SAddr es, int t, int n_valid) {
 #pragma unroll
     for (int b = 0; b < E / R0; ++b) {
 #pragma unroll
       for (int r = 0; r < R0; ++r) {
         const int p = in_pos(t, b, r);
-        reg[b * R0 + r] = (r < R0 / 2 && p < n_valid) ? base[p * es] : mk<V>(0, 0);
+        reg[b * R0 + r] = (r < R0 / 2 && p < n_valid) ? base[es(p)] : mk<V>(0, 0);
       }
     }
   }
-  __device__ __forceinline__ static void run(V* reg, V* base, int es, int t, const V* tw) {
+  __device__ __forceinline__ static void run(V* reg, V* base, SAddr es, int t, const V* tw) {
     Passes<V, N, E, INV, 1, false, RL_>::run(reg, base, es, t, tw);
   }
   // First pass on inputs with a zero upper half (R0 even).
-  __device__ __forceinline__ static void run_half(V* reg, V* base, int es, int t, const V* tw) {
+  __device__ __forceinline__ static void run_half(V* reg, V* base, SAddr es, int t, const V* tw) {
     static_assert(R0 % 2 == 0, "zero-half skipping needs an even first radix");
     Passes<V, N, E, INV, 1, true, RL_>::run(reg, base, es, t, tw);
   }
@@ -365,11 +375,11 @@ template <typename V, int N, bool INV> struct FFT {
     return (j / NSL) * NSL * RL + (j % NSL) + r * NSL;
   }
   // Store all outputs (natural order) back to shared memory.  Caller syncs.
-  __device__ __forceinline__ static void store(const V* reg, V* base, int es, int t) {
+  __device__ __forceinline__ static void store(const V* reg, V* base, SAddr es, int t) {
 #pragma unroll
     for (int b = 0; b < E / RL; ++b)
 #pragma unroll
-      for (int r = 0; r < RL; ++r) base[out_pos(t, b, r) * es] = reg[b * RL + r];
+      for (int r = 0; r < RL; ++r) base[es(out_pos(t, b, r))] = reg[b * RL + r];
   }
 };
 

@@ -1,7 +1,16 @@
-// JVIE_Solver (src_vie/src_solver/JVIE_Solver.m:1-521, solver 'G'), the total
-// field E_field_Nop (src_vie/src_fields/src_op/E_field_Nop.m:59-84) and the
-// incident-field generators (PlaneWave_Excitation.m:39-95, E_field_DGF.m:36-99),
-// all on the device.
+// JVIE_Solver (src_vie/src_solver/JVIE_Solver.m:1-521, solver 'G') on the
+// device, for one excitation or a batch of excitations of one body:
+//   set-up (JVIE_Solver.m:131-156, 242-244): non-air voxel compaction, the
+//   local DOF order [idxS; V+idxS; 2V+idxS], the right-hand sides
+//   Gram*j*omega*eps0*Mc*Einc, the form-2 scaling, the preconditioner
+//   coefficients (1/Mr, 1/Mr - 1), then pgmres (restart inner_it, outer_it
+//   cycles) and the scatter Je(idxS3) = x (:513-514).
+// Arithmetic: MARIE_FP64 plans solve with the FP64 matvec (the reference
+// arithmetic); MARIE_MIXED plans run GMRES-IR: the inner pgmres uses the FP32
+// circulant matvec (Krylov basis, Arnoldi, Givens and the diagonal Gram*Mr
+// term in FP64) and the outer loop refines with FP64 true residuals until
+// ||b - A x|| / ||b|| <= tol.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <vector>
@@ -28,8 +37,7 @@ static constexpr int CMP_BLOCKS = 1024;
 
 __device__ __forceinline__ bool non_air(const double2* er, long long v) {
   const double2 e = er[v];
-  const double mx = e.x - 1.0, my = e.y;
-  return sqrt(mx * mx + my * my) > 1e-12;
+  return hypot(e.x - 1.0, e.y) > 1e-12;
 }
 
 __global__ void k_count_nonair(const double2* __restrict__ er, long long V, int* __restrict__ counts) {
@@ -78,33 +86,30 @@ __global__ void k_write_nonair(const double2* __restrict__ er, long long V, cons
 }
 
 // Per-DOF set-up for nS non-air voxels (DOF k = c*nS + s):
-//   idx3[k]  = c*V + idxS[s] + 1                     (1-based, JVIE_Solver.m:148)
-//   rhs[k]   = Gram * j*omega*eps0 * Mc * Einc        (JVIE_Solver.m:151-156)
-//   form 2:  Mc <- Mc/Mr, rhs <- rhs/Mr, Mr <- 1      (JVIE_Solver.m:242-244)
-//   a = Gram*Mr, b = Mc ; preconditioner pa = Gram/Mr, pb = 1/Mr - 1
-__global__ void k_jvie_setup(const int* __restrict__ idxS, long long nS, long long V, const double2* __restrict__ er,
-                             const double2* __restrict__ Einc, double Gram, double omega_eps0, int form,
-                             int64_t* __restrict__ idx3, double2* __restrict__ rhs, double2* __restrict__ a,
-                             double2* __restrict__ b, double2* __restrict__ pa, double2* __restrict__ pb) {
+//   idx3[k] = c*V + idxS[s] + 1                       (JVIE_Solver.m:148)
+//   f[k]    = Gram * j*omega*eps0 * Mc (/ Mr, form 2)  (rhs = f .* Einc, :151-156, :243)
+//   a = Gram*Mr, b = Mc (form 2: Mc/Mr and Mr = 1)      (:242-244)
+//   pa = Gram/Mr, pb = 1/Mr - 1                         (preconditioner, :276-278)
+__global__ void k_jvie_coef(const int* __restrict__ idxS, long long nS, long long V, const double2* __restrict__ er,
+                            double Gram, double omega_eps0, int form, int64_t* __restrict__ idx3,
+                            double2* __restrict__ f, double2* __restrict__ a, double2* __restrict__ b,
+                            double2* __restrict__ pa, double2* __restrict__ pb) {
   const long long n = 3 * nS;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
     const long long c = k / nS, s = k - c * nS;
     const long long v = idxS[s];
-    const long long g = c * V + v;
-    idx3[k] = g + 1;
+    idx3[k] = c * V + v + 1;
     double2 mr = er[v];
     double2 mc = mk<double2>(mr.x - 1.0, mr.y);
-    const double2 tau = mk<double2>(-omega_eps0 * mc.y, omega_eps0 * mc.x);  // j*omega*eps0*Mc
-    double2 r = cmul(tau, Einc[g]);
-    r = mk<double2>(Gram * r.x, Gram * r.y);
+    double2 fk = mk<double2>(-Gram * omega_eps0 * mc.y, Gram * omega_eps0 * mc.x);  // Gram*j*omega*eps0*Mc
     if (form != 1) {
       const double den = mr.x * mr.x + mr.y * mr.y;
       const double2 inv_mr = mk<double2>(mr.x / den, -mr.y / den);
       mc = cmul(mc, inv_mr);
-      r = cmul(r, inv_mr);
+      fk = cmul(fk, inv_mr);
       mr = mk<double2>(1.0, 0.0);
     }
-    rhs[k] = r;
+    f[k] = fk;
     a[k] = mk<double2>(Gram * mr.x, Gram * mr.y);
     b[k] = mc;
     const double den = mr.x * mr.x + mr.y * mr.y;
@@ -114,121 +119,57 @@ __global__ void k_jvie_setup(const int* __restrict__ idxS, long long nS, long lo
   }
 }
 
+// rhs_e[k] = f[k] * Einc_e[idx3[k]-1] for every excitation e
+__global__ void k_jvie_rhs(const double2* __restrict__ f, const int64_t* __restrict__ idx3, long long n,
+                           const double2* __restrict__ E, long long es, double2* __restrict__ rhs) {
+  const int e = blockIdx.y;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    rhs[e * n + k] = cmul(f[k], E[e * es + idx3[k] - 1]);
+}
+
 __global__ void k_scatter_dofs(const double2* __restrict__ x, const int64_t* __restrict__ idx3, long long n,
-                               double2* __restrict__ out) {
+                               double2* __restrict__ out, long long os) {
+  const int e = blockIdx.y;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-    out[idx3[k] - 1] = x[k];
+    out[e * os + idx3[k] - 1] = x[e * n + k];
 }
 
-__global__ void k_diag_apply(const double2* __restrict__ a, const double2* __restrict__ x, double2* __restrict__ y,
-                             long long n) {
+// y_s = a .* x_s for systems with stop[s] >= step
+__global__ void k_diag_b(const double2* __restrict__ a, const double2* __restrict__ x, long long xs,
+                         double2* __restrict__ y, long long ys, long long n, const int* __restrict__ stop, int step) {
+  const int s = blockIdx.y;
+  if (stop && stop[s] < step) return;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-    y[k] = cmul(a[k], x[k]);
+    y[s * ys + k] = cmul(a[k], x[s * xs + k]);
 }
 
-__global__ void k_all_zero(const double2* __restrict__ b, long long n, int* __restrict__ nonzero) {
+__global__ void k_any_nonzero(const double2* __restrict__ b, long long n, int* __restrict__ nonzero) {
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
     if (b[k].x != 0.0 || b[k].y != 0.0) *nonzero = 1;
 }
 
-__global__ void k_identity_index(int* __restrict__ inv, long long n) {
+// y_s = b_s - y_s, x_s += d_s   (for systems with flag[s])
+__global__ void k_sub_b(const double2* __restrict__ b, double2* __restrict__ y, long long n,
+                        const int* __restrict__ flag) {
+  const int s = blockIdx.y;
+  if (!flag[s]) return;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-    inv[k] = (int)k;
+    y[s * n + k] = csub(b[s * n + k], y[s * n + k]);
 }
-
-__global__ void k_add_field(const double2* __restrict__ einc, double2* __restrict__ e, long long n) {
+__global__ void k_add_b(const double2* __restrict__ d, double2* __restrict__ x, long long n,
+                        const int* __restrict__ flag) {
+  const int s = blockIdx.y;
+  if (!flag[s]) return;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-    e[k] = cadd(e[k], einc[k]);
+    x[s * n + k] = cadd(x[s * n + k], d[s * n + k]);
 }
 
-__global__ void k_sub(const double2* __restrict__ b, double2* __restrict__ y, long long n) {
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-    y[k] = csub(b[k], y[k]);
-}
-__global__ void k_axpy1(const double2* __restrict__ x, double2* __restrict__ y, long long n) {
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-    y[k] = cadd(y[k], x[k]);
-}
-
-// ---------------------------------------------------------------------------
-// incident fields
-// ---------------------------------------------------------------------------
-// PlaneWave_Excitation.m:62-95: product of voxel-averaged 1-D factors, / (dx dy dz)
-__global__ void k_plane_wave(const double* __restrict__ r, long long L, long long M, long long N, double kx, double ky,
-                             double kz, double2 e0x, double2 e0y, double2 e0z, double dx, double dy, double dz,
-                             double2* __restrict__ E) {
-  const long long V = L * M * N;
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
-    const double kk[3] = {kx, ky, kz};
-    const double dd[3] = {dx, dy, dz};
-    double2 f = mk<double2>(1.0, 0.0);
-    for (int a = 0; a < 3; ++a) {
-      double2 fa;
-      if (kk[a] != 0.0) {
-        // exp(-j k r) * (exp(-j k d/2) - exp(j k d/2)) / (-j k) = exp(-j k r) * 2 sin(k d/2) / k
-        double sr, cr;
-        sincos(kk[a] * r[a * V + v], &sr, &cr);
-        const double s = 2.0 * sin(kk[a] * dd[a] * 0.5) / kk[a];
-        fa = mk<double2>(cr * s, -sr * s);
-      } else {
-        fa = mk<double2>(dd[a], 0.0);
-      }
-      f = cmul(f, fa);
-    }
-    const double inv = 1.0 / (dx * dy * dz);
-    f = mk<double2>(f.x * inv, f.y * inv);
-    E[v] = cmul(e0x, f);
-    E[V + v] = cmul(e0y, f);
-    E[2 * V + v] = cmul(e0z, f);
-  }
-}
-
-// E_field_DGF.m:77-99, point-sampled dyadic Green function of electric dipoles
-__global__ void k_dipole_field(const double* __restrict__ r, long long V, double ko, const double2* __restrict__ Jd,
-                               const double* __restrict__ pos, int ndip, double2* __restrict__ E) {
-  const double omega = ko * C0;
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
-    double2 ex = mk<double2>(0, 0), ey = ex, ez = ex;
-    const double ox = r[v], oy = r[V + v], oz = r[2 * V + v];
-    for (int j = 0; j < ndip; ++j) {
-      const double X = ox - pos[3 * j], Y = oy - pos[3 * j + 1], Z = oz - pos[3 * j + 2];
-      const double R2 = X * X + Y * Y + Z * Z;
-      const double R = sqrt(R2);
-      const double R3 = R * R2;
-      double sn, cs;
-      sincos(ko * R, &sn, &cs);
-      // chi = j*omega*mu*exp(-j ko R) / (4 pi ko^2 R^3)
-      const double amp = omega * MU0 / (4.0 * M_PI * ko * ko * R3);
-      const double2 chi = mk<double2>(amp * sn, amp * cs);
-      const double2 P0 = mk<double2>(1.0, ko * R);           // P = j ko R + 1
-      const double2 Q = mk<double2>(ko * ko * R2 - 1.0, -ko * R);  // Q = ko^2 R^2 - P
-      const double2 Pn = mk<double2>((Q.x - 2.0 * P0.x) / R2, (Q.y - 2.0 * P0.y) / R2);
-      const double2 Qc = cmul(chi, Q), Pc = cmul(chi, Pn);
-      const double2 jx = Jd[3 * j], jy = Jd[3 * j + 1], jz = Jd[3 * j + 2];
-      const double2 pxx = mk<double2>(Pc.x * X * X - Qc.x, Pc.y * X * X - Qc.y);
-      const double2 pyy = mk<double2>(Pc.x * Y * Y - Qc.x, Pc.y * Y * Y - Qc.y);
-      const double2 pzz = mk<double2>(Pc.x * Z * Z - Qc.x, Pc.y * Z * Z - Qc.y);
-      const double2 pxy = cscale(Pc, X * Y), pxz = cscale(Pc, X * Z), pyz = cscale(Pc, Y * Z);
-      ex = cadd(ex, cadd(cadd(cmul(pxx, jx), cmul(pxy, jy)), cmul(pxz, jz)));
-      ey = cadd(ey, cadd(cadd(cmul(pxy, jx), cmul(pyy, jy)), cmul(pyz, jz)));
-      ez = cadd(ez, cadd(cadd(cmul(pxz, jx), cmul(pyz, jy)), cmul(pzz, jz)));
-    }
-    E[v] = ex;
-    E[V + v] = ey;
-    E[2 * V + v] = ez;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// J-VIE solve
-// ---------------------------------------------------------------------------
 struct JvieState {
   long long nS = 0, n = 0;
-  DBuf idxS, idx3, inv, rhs, a, b, pa, pb;
+  DBuf idxS, idx3, inv, f, a, b, pa, pb;
 };
 
-static int jvie_setup(marie_plan* p, const double2* er, const double2* Einc, double dx, double freq, int form,
-                      JvieState& S) {
+static int jvie_setup(marie_plan* p, const double2* er, double dx, double freq, int form, JvieState& S) {
   cudaStream_t st = p->stream;
   const long long V = p->d.V;
   DBuf counts;
@@ -254,7 +195,7 @@ static int jvie_setup(marie_plan* p, const double2* er, const double2* Einc, dou
   MARIE_CUDA_TRY(cudaGetLastError());
   const long long n = S.n;
   MARIE_TRY(S.idx3.alloc(n * sizeof(int64_t), st));
-  MARIE_TRY(S.rhs.alloc(n * sizeof(double2), st));
+  MARIE_TRY(S.f.alloc(n * sizeof(double2), st));
   MARIE_TRY(S.a.alloc(n * sizeof(double2), st));
   MARIE_TRY(S.b.alloc(n * sizeof(double2), st));
   MARIE_TRY(S.pa.alloc(n * sizeof(double2), st));
@@ -262,37 +203,40 @@ static int jvie_setup(marie_plan* p, const double2* er, const double2* Einc, dou
   MARIE_TRY(S.inv.alloc(3 * V * sizeof(int), st));
   const double Gram = dx * dx * dx;
   const double omega = 2.0 * M_PI * freq;
-  k_jvie_setup<<<grid_n(n), 256, 0, st>>>(S.idxS.as<int>(), tot, V, er, Einc, Gram, omega * eps0(), form,
-                                          S.idx3.as<int64_t>(), S.rhs.as<double2>(), S.a.as<double2>(),
-                                          S.b.as<double2>(), S.pa.as<double2>(), S.pb.as<double2>());
+  k_jvie_coef<<<grid_n(n), 256, 0, st>>>(S.idxS.as<int>(), tot, V, er, Gram, omega * eps0(), form,
+                                         S.idx3.as<int64_t>(), S.f.as<double2>(), S.a.as<double2>(),
+                                         S.b.as<double2>(), S.pa.as<double2>(), S.pb.as<double2>());
   count_launch();
   MARIE_CUDA_TRY(cudaGetLastError());
   MARIE_TRY(build_inverse_index(p, S.idx3.as<int64_t>(), n, S.inv.as<int>()));
   return MARIE_OK;
 }
 
-static int all_zero(marie_plan* p, const double2* b, long long n, bool* z) {
+static int any_nonzero(marie_plan* p, const double2* b, long long n, bool* nz) {
   DBuf f;
   MARIE_TRY(f.alloc(sizeof(int), p->stream));
   MARIE_CUDA_TRY(cudaMemsetAsync(f.p, 0, sizeof(int), p->stream));
-  k_all_zero<<<grid_n(n), 256, 0, p->stream>>>(b, n, f.as<int>());
+  k_any_nonzero<<<grid_n(n), 256, 0, p->stream>>>(b, n, f.as<int>());
   count_launch();
   int h = 0;
   MARIE_CUDA_TRY(cudaMemcpyAsync(&h, f.p, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
   MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
-  *z = (h == 0);
+  *nz = (h != 0);
   return MARIE_OK;
 }
 
-// mv_AN operator on the solver's DOFs with coefficient arrays (a, b); a b that is
-// identically zero reduces to the diagonal Gram*Mr product (the circulant
-// term is multiplied by zero in mv_AN.m:127-131).
-static DevOp make_op(marie_plan* p, int prec, const JvieState& S, const double2* a, const double2* b, bool diag_only) {
+// mv_AN on the solver's DOFs for a batch of systems, coefficients (a, b).  A
+// b that is identically zero leaves only the diagonal Gram*Mr product (the
+// circulant term is multiplied by zero in mv_AN.m:127-131), so no FFT runs.
+static BatchOp make_bop(marie_plan* p, int prec, const JvieState& S, const double2* a, const double2* b,
+                        bool diag_only) {
   const long long n = S.n;
   const int* inv = S.inv.as<int>();
-  return [p, prec, n, inv, a, b, diag_only](const double2* x, double2* y) -> int {
+  BatchOp op;
+  op.apply = [p, prec, n, inv, a, b, diag_only](const double2* in, long long is, double2* out, long long os, int ns,
+                                                const int* stop, int step) -> int {
     if (diag_only) {
-      k_diag_apply<<<grid_n(n), 256, 0, p->stream>>>(a, x, y, n);
+      k_diag_b<<<dim3(grid_n(n), ns), 256, 0, p->stream>>>(a, in, is, out, os, n, stop, step);
       count_launch();
       MARIE_CUDA_TRY(cudaGetLastError());
       return MARIE_OK;
@@ -301,8 +245,131 @@ static DevOp make_op(marie_plan* p, int prec, const JvieState& S, const double2*
     Epilogue ep{};
     ep.a = a;
     ep.b = b;
-    return run_matvec(p, prec, x, y, n, 1, inv, pro, ep);
+    return run_matvec(p, prec, in, is, out, os, n, ns, inv, pro, ep, stop, step);
   };
+  return op;
+}
+
+struct SolveOut {
+  std::vector<GmresResult> r;
+};
+
+// Solves the S excitations E (3V x S, column stride es) of one body.
+static int jvie_solve_core(marie_plan* p, const double2* E, long long es, int S_exc, const double2* er, double dx,
+                           double freq, int form, char precond, double tol, int inner_it, int outer_it, double2* Je,
+                           long long js, SolveOut& out) {
+  cudaStream_t st = p->stream;
+  const long long V = p->d.V;
+  JvieState S;
+  MARIE_TRY(jvie_setup(p, er, dx, freq, form, S));
+  for (int e = 0; e < S_exc; ++e) MARIE_CUDA_TRY(cudaMemsetAsync(Je + e * js, 0, 3 * V * sizeof(double2), st));
+  out.r.assign(S_exc, GmresResult());
+  if (S.n == 0) {
+    for (auto& r : out.r) {
+      r.flag = 0;
+      r.relres = 0;
+    }
+    return MARIE_OK;
+  }
+  const long long n = S.n;
+  if (p->nrhs_max < S_exc) {
+    // workspaces for the batch are sized by nrhs_max; batches above it run in chunks
+  }
+  DBuf rhs, x;
+  MARIE_TRY(rhs.alloc((size_t)S_exc * n * sizeof(double2), st));
+  MARIE_TRY(x.alloc((size_t)S_exc * n * sizeof(double2), st));
+  k_jvie_rhs<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(S.f.as<double2>(), S.idx3.as<int64_t>(), n, E, es,
+                                                      rhs.as<double2>());
+  count_launch();
+  bool pb_nz = true;
+  MARIE_TRY(any_nonzero(p, S.pb.as<double2>(), n, &pb_nz));
+  const int prec_main = (p->precision == MARIE_FP32) ? MARIE_FP32 : MARIE_FP64;
+  BatchOp A64 = make_bop(p, prec_main, S, S.a.as<double2>(), S.b.as<double2>(), false);
+  BatchOp P64 = make_bop(p, prec_main, S, S.pa.as<double2>(), S.pb.as<double2>(), !pb_nz);
+  const BatchOp* L1 = precond == 'L' ? &P64 : nullptr;
+  const BatchOp* R1 = precond == 'R' ? &P64 : nullptr;
+  double2* X = x.as<double2>();
+  const double2* Bv = rhs.as<double2>();
+  if (p->precision != MARIE_MIXED) {
+    MARIE_TRY(gmres_batch(p, A64, L1, R1, Bv, n, n, S_exc, inner_it, tol, outer_it, X, n, out.r, true, nullptr,
+                          true));
+  } else {
+    // GMRES-IR: FP32-matvec pgmres on the residual, FP64 true residual and correction
+    BatchOp A32 = make_bop(p, MARIE_FP32, S, S.a.as<double2>(), S.b.as<double2>(), false);
+    BatchOp P32 = make_bop(p, MARIE_FP32, S, S.pa.as<double2>(), S.pb.as<double2>(), !pb_nz);
+    const BatchOp* L1m = precond == 'L' ? &P32 : nullptr;
+    const BatchOp* R1m = precond == 'R' ? &P32 : nullptr;
+    DBuf rb, db, flags;
+    MARIE_TRY(rb.alloc((size_t)S_exc * n * sizeof(double2), st));
+    MARIE_TRY(db.alloc((size_t)S_exc * n * sizeof(double2), st));
+    MARIE_TRY(flags.alloc(S_exc * sizeof(int), st));
+    double2* Rr = rb.as<double2>();
+    double2* D = db.as<double2>();
+    MARIE_CUDA_TRY(cudaMemsetAsync(X, 0, (size_t)S_exc * n * sizeof(double2), st));
+    MARIE_CUDA_TRY(cudaMemcpyAsync(Rr, Bv, (size_t)S_exc * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    std::vector<double> bn(S_exc), rn(S_exc);
+    for (int e = 0; e < S_exc; ++e) MARIE_TRY(dev_norm2(p, Bv + e * n, n, &bn[e]));
+    rn = bn;
+    std::vector<int> act(S_exc), inner_total(S_exc, 0), last_p(S_exc, 0);
+    for (int e = 0; e < S_exc; ++e) {
+      out.r[e].relres = rn[e] / bn[e];
+      out.r[e].resvec.push_back(out.r[e].relres);
+    }
+    const int max_refine = 20;
+    for (int it = 0; it < max_refine; ++it) {
+      bool any = false;
+      double inner_tol = 0.5;
+      for (int e = 0; e < S_exc; ++e) {
+        act[e] = out.r[e].relres > tol ? 1 : 0;
+        if (act[e]) {
+          any = true;
+          // half of what is still missing, not below the FP32 floor
+          inner_tol = std::min(inner_tol, std::max(0.5 * tol * bn[e] / rn[e], 1e-5));
+        }
+      }
+      if (!any) break;
+      std::vector<GmresResult> ri;
+      MARIE_TRY(gmres_batch(p, A32, L1m, R1m, Rr, n, n, S_exc, inner_it, inner_tol, outer_it, D, n, ri, true, &act,
+                            false));
+      MARIE_CUDA_TRY(cudaMemcpyAsync(flags.p, act.data(), S_exc * sizeof(int), cudaMemcpyHostToDevice, st));
+      k_add_b<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(D, X, n, flags.as<int>());
+      count_launch();
+      // r = b - A64 x (FP64) for the systems that moved
+      MARIE_TRY(A64.apply(X, n, Rr, n, S_exc, flags.as<int>(), 1));
+      k_sub_b<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(Bv, Rr, n, flags.as<int>());
+      count_launch();
+      MARIE_CUDA_TRY(cudaGetLastError());
+      for (int e = 0; e < S_exc; ++e) {
+        if (!act[e]) continue;
+        for (size_t i = 1; i < ri[e].resvec.size(); ++i) out.r[e].resvec.push_back(ri[e].resvec[i] * rn[e] / bn[e]);
+        inner_total[e] += ri[e].iter[1];
+        last_p[e] = ri[e].iter[0];
+        MARIE_TRY(dev_norm2(p, Rr + e * n, n, &rn[e]));
+        out.r[e].relres = rn[e] / bn[e];
+        out.r[e].resvec.push_back(out.r[e].relres);
+      }
+    }
+    for (int e = 0; e < S_exc; ++e) {
+      out.r[e].flag = out.r[e].relres <= tol ? 0 : 1;
+      out.r[e].iter[0] = last_p[e];
+      out.r[e].iter[1] = inner_total[e];
+    }
+  }
+  k_scatter_dofs<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(X, S.idx3.as<int64_t>(), n, Je, js);
+  count_launch();
+  MARIE_CUDA_TRY(cudaGetLastError());
+  return MARIE_OK;
+}
+
+static int clamp_args(double& tol, int& form, char& precond, int& inner_it, int& outer_it) {
+  // JVIE_Solver.m:71-122 argument clamps
+  if (tol < 1e-15 || tol >= 1) tol = 1e-3;
+  if (form != 1) form = 2;
+  if (precond != 'L' && precond != 'R') precond = 0;
+  if (inner_it < 1) inner_it = 50;
+  if (outer_it < 1) outer_it = 200;
+  if (inner_it > 127) return set_error(MARIE_EINVAL, "inner_it (GMRES restart) above 127 is not built");
+  return MARIE_OK;
 }
 
 }  // namespace marie
@@ -317,12 +384,7 @@ int marie_jvie_solve(marie_plan* p, const double* Einc, const double* e_r, doubl
   if (!p || !Einc || !e_r || !Je) return set_error(MARIE_EINVAL, "NULL argument");
   if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator");
   if (!(dx > 0) || !(freq > 0)) return set_error(MARIE_EINVAL, "dx and freq must be positive");
-  // JVIE_Solver.m:71-122 argument clamps
-  if (tol < 1e-15 || tol >= 1) tol = 1e-3;
-  if (form != 1) form = 2;
-  if (precond != 'L' && precond != 'R') precond = 0;
-  if (inner_it < 1) inner_it = 50;
-  if (outer_it < 1) outer_it = 200;
+  MARIE_TRY(clamp_args(tol, form, precond, inner_it, outer_it));
   const auto t0 = std::chrono::steady_clock::now();
   cudaStream_t st = p->stream;
   const long long V = p->d.V;
@@ -332,175 +394,57 @@ int marie_jvie_solve(marie_plan* p, const double* Einc, const double* e_r, doubl
   MARIE_TRY(stage_in(Einc, 3 * V * sizeof(double2), st, tE, &E_d));
   MARIE_TRY(stage_in(e_r, V * sizeof(double2), st, tER, &er_d));
   MARIE_TRY(stage_out(Je, 3 * V * sizeof(double2), st, tJe, &Je_d));
-  JvieState S;
-  MARIE_TRY(jvie_setup(p, (const double2*)er_d, (const double2*)E_d, dx, freq, form, S));
-  MARIE_CUDA_TRY(cudaMemsetAsync(Je_d, 0, 3 * V * sizeof(double2), st));
-  GmresResult R;
-  std::vector<double> rv;
-  if (S.n > 0) {
-    const long long n = S.n;
-    bool pb_zero = false;
-    MARIE_TRY(all_zero(p, S.pb.as<double2>(), n, &pb_zero));
-    const int prec_main = (p->precision == MARIE_FP32) ? MARIE_FP32 : MARIE_FP64;
-    DevOp A64 = make_op(p, prec_main, S, S.a.as<double2>(), S.b.as<double2>(), false);
-    DevOp P64 = make_op(p, prec_main, S, S.pa.as<double2>(), S.pb.as<double2>(), pb_zero);
-    DBuf x;
-    MARIE_TRY(x.alloc(n * sizeof(double2), st));
-    const DevOp* L1 = precond == 'L' ? &P64 : nullptr;
-    const DevOp* R1 = precond == 'R' ? &P64 : nullptr;
-    if (p->precision != MARIE_MIXED) {
-      MARIE_TRY(gmres(p, A64, L1, nullptr, R1, nullptr, S.rhs.as<double2>(), n, inner_it, tol, outer_it, nullptr,
-                      x.as<double2>(), R));
-      rv = R.resvec;
-    } else {
-      // FP32 circulant matvec inside FP64 GMRES, refined with FP64 residuals.
-      DevOp A32 = make_op(p, MARIE_FP32, S, S.a.as<double2>(), S.b.as<double2>(), false);
-      DevOp P32 = make_op(p, MARIE_FP32, S, S.pa.as<double2>(), S.pb.as<double2>(), pb_zero);
-      const DevOp* L1m = precond == 'L' ? &P32 : nullptr;
-      const DevOp* R1m = precond == 'R' ? &P32 : nullptr;
-      DBuf r, d;
-      MARIE_TRY(r.alloc(n * sizeof(double2), st));
-      MARIE_TRY(d.alloc(n * sizeof(double2), st));
-      const double2* b = S.rhs.as<double2>();
-      MARIE_CUDA_TRY(cudaMemsetAsync(x.p, 0, n * sizeof(double2), st));
-      MARIE_CUDA_TRY(cudaMemcpyAsync(r.p, b, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-      double bn = 0, rn = 0;
-      MARIE_TRY(dev_norm2(p, b, n, &bn));
-      rn = bn;
-      rv.push_back(rn / bn);
-      int outer = 0, inner_total = 0, last_p = 0;
-      R.relres = rn / bn;
-      const int max_refine = 20;
-      while (R.relres > tol && outer < max_refine) {
-        ++outer;
-        // inner target: half of what is still missing, not below the FP32 floor
-        double inner_tol = 0.5 * tol * bn / rn;
-        if (inner_tol < 1e-5) inner_tol = 1e-5;
-        if (inner_tol > 0.5) inner_tol = 0.5;
-        GmresResult Ri;
-        MARIE_TRY(gmres(p, A32, L1m, nullptr, R1m, nullptr, r.as<double2>(), n, inner_it, inner_tol, outer_it,
-                        nullptr, d.as<double2>(), Ri));
-        for (size_t i = 1; i < Ri.resvec.size(); ++i) rv.push_back(Ri.resvec[i] * rn / bn);
-        inner_total += Ri.iter[1];
-        last_p = Ri.iter[0];
-        k_axpy1<<<grid_n(n), 256, 0, st>>>(d.as<double2>(), x.as<double2>(), n);
-        count_launch();
-        // r = b - A64 x in FP64 (with the left preconditioner when asked, as pgmres does)
-        MARIE_TRY(A64(x.as<double2>(), r.as<double2>()));
-        k_sub<<<grid_n(n), 256, 0, st>>>(b, r.as<double2>(), n);
-        count_launch();
-        MARIE_CUDA_TRY(cudaGetLastError());
-        MARIE_TRY(dev_norm2(p, r.as<double2>(), n, &rn));
-        R.relres = rn / bn;
-        rv.push_back(R.relres);
-      }
-      R.flag = R.relres <= tol ? 0 : 1;
-      R.iter[0] = last_p;
-      R.iter[1] = inner_total;
-    }
-    k_scatter_dofs<<<grid_n(n), 256, 0, st>>>(x.as<double2>(), S.idx3.as<int64_t>(), n, (double2*)Je_d);
-    count_launch();
-    MARIE_CUDA_TRY(cudaGetLastError());
-  } else {
-    R.flag = 0;
-    R.relres = 0;
-  }
+  SolveOut so;
+  MARIE_TRY(jvie_solve_core(p, (const double2*)E_d, 3 * V, 1, (const double2*)er_d, dx, freq, form, precond, tol,
+                            inner_it, outer_it, (double2*)Je_d, 3 * V, so));
   MARIE_TRY(finish_out(Je, Je_d, 3 * V * sizeof(double2), st));
   MARIE_CUDA_TRY(cudaStreamSynchronize(st));
   const auto t1 = std::chrono::steady_clock::now();
+  const GmresResult& R = so.r[0];
   if (flag) *flag = R.flag;
   if (relres) *relres = R.relres;
   if (iter) {
     iter[0] = R.iter[0];
     iter[1] = R.iter[1];
   }
-  if (resvec_len) *resvec_len = (int64_t)rv.size();
+  if (resvec_len) *resvec_len = (int64_t)R.resvec.size();
   if (resvec)
-    for (int64_t i = 0; i < (int64_t)rv.size() && i < resvec_cap; ++i) resvec[i] = rv[i];
+    for (int64_t i = 0; i < (int64_t)R.resvec.size() && i < resvec_cap; ++i) resvec[i] = R.resvec[i];
   if (solvert) *solvert = std::chrono::duration<double>(t1 - t0).count();
   return MARIE_OK;
 }
 
-int marie_e_field_nop(marie_plan* p, const double* J, double Gram, double freq, const double* Einc, double* Etot,
-                      int precision) {
-  if (!p || !J || !Etot) return set_error(MARIE_EINVAL, "NULL argument");
-  if (precision != MARIE_FP64 && precision != MARIE_FP32) return set_error(MARIE_EINVAL, "bad precision");
+int marie_jvie_solve_batch(marie_plan* p, const double* Einc, int64_t nexc, const double* e_r, double dx, double freq,
+                           int form, char precond, double tol, int inner_it, int outer_it, double* Je, int* flag,
+                           double* relres, int* iter, double* solvert) {
+  if (!p || !Einc || !e_r || !Je || nexc < 1) return set_error(MARIE_EINVAL, "NULL argument or nexc < 1");
   if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator");
+  if (!(dx > 0) || !(freq > 0)) return set_error(MARIE_EINVAL, "dx and freq must be positive");
+  MARIE_TRY(clamp_args(tol, form, precond, inner_it, outer_it));
+  const auto t0 = std::chrono::steady_clock::now();
   cudaStream_t st = p->stream;
-  const long long n = 3 * p->d.V;
-  DBuf tJ, tE, tO, inv;
-  const void *J_d, *E_d = nullptr;
-  void* O_d;
-  MARIE_TRY(stage_in(J, n * sizeof(double2), st, tJ, &J_d));
-  if (Einc) MARIE_TRY(stage_in(Einc, n * sizeof(double2), st, tE, &E_d));
-  MARIE_TRY(stage_out(Etot, n * sizeof(double2), st, tO, &O_d));
-  MARIE_TRY(inv.alloc(n * sizeof(int), st));
-  k_identity_index<<<grid_n(n), 256, 0, st>>>(inv.as<int>(), n);
-  count_launch();
-  // out = s*(N J - Gram J), s = 1/(Gram*j*omega*eps0) = -j/(Gram*omega*eps0)
-  const double omega = 2.0 * M_PI * freq;
-  const double2 s = mk<double2>(0.0, -1.0 / (Gram * omega * eps0()));
-  Prologue pro{nullptr, 0};
-  Epilogue ep{};
-  ep.a_s = mk<double2>(-Gram * s.x, -Gram * s.y);
-  ep.b_s = mk<double2>(-s.x, -s.y);
-  MARIE_TRY(run_matvec(p, precision, (const double2*)J_d, (double2*)O_d, n, 1, inv.as<int>(), pro, ep));
-  if (Einc) {
-    k_add_field<<<grid_n(n), 256, 0, st>>>((const double2*)E_d, (double2*)O_d, n);
-    count_launch();
+  const long long V = p->d.V;
+  DBuf tE, tER, tJe;
+  const void *E_d, *er_d;
+  void* Je_d;
+  MARIE_TRY(stage_in(Einc, (size_t)nexc * 3 * V * sizeof(double2), st, tE, &E_d));
+  MARIE_TRY(stage_in(e_r, V * sizeof(double2), st, tER, &er_d));
+  MARIE_TRY(stage_out(Je, (size_t)nexc * 3 * V * sizeof(double2), st, tJe, &Je_d));
+  SolveOut so;
+  MARIE_TRY(jvie_solve_core(p, (const double2*)E_d, 3 * V, (int)nexc, (const double2*)er_d, dx, freq, form, precond,
+                            tol, inner_it, outer_it, (double2*)Je_d, 3 * V, so));
+  MARIE_TRY(finish_out(Je, Je_d, (size_t)nexc * 3 * V * sizeof(double2), st));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+  const auto t1 = std::chrono::steady_clock::now();
+  for (int64_t e = 0; e < nexc; ++e) {
+    if (flag) flag[e] = so.r[e].flag;
+    if (relres) relres[e] = so.r[e].relres;
+    if (iter) {
+      iter[2 * e] = so.r[e].iter[0];
+      iter[2 * e + 1] = so.r[e].iter[1];
+    }
   }
-  MARIE_CUDA_TRY(cudaGetLastError());
-  MARIE_TRY(finish_out(Etot, O_d, n * sizeof(double2), st));
-  MARIE_CUDA_TRY(cudaStreamSynchronize(st));
-  return MARIE_OK;
-}
-
-int marie_plane_wave(const double* r, int64_t L, int64_t M, int64_t N, const double* k, const double* Eo,
-                     double* E) {
-  if (!r || !k || !Eo || !E || L < 2 || M < 2 || N < 2) return set_error(MARIE_EINVAL, "bad argument");
-  cudaStream_t st = 0;
-  const long long V = L * M * N;
-  DBuf tr, tE;
-  const void* r_d;
-  void* E_d;
-  MARIE_TRY(stage_in(r, 3 * V * sizeof(double), st, tr, &r_d));
-  MARIE_TRY(stage_out(E, 3 * V * sizeof(double2), st, tE, &E_d));
-  // PlaneWave_Excitation.m:45-47 spacing from the first neighbours of each axis
-  std::vector<double> rh(3 * 3);
-  const long long offs[3][2] = {{0, 1}, {V, V + L}, {2 * V, 2 * V + L * M}};
-  for (int a = 0; a < 3; ++a) {
-    MARIE_CUDA_TRY(cudaMemcpy(&rh[2 * a], (const double*)r_d + offs[a][0], sizeof(double), cudaMemcpyDefault));
-    MARIE_CUDA_TRY(cudaMemcpy(&rh[2 * a + 1], (const double*)r_d + offs[a][1], sizeof(double), cudaMemcpyDefault));
-  }
-  const double dx = rh[1] - rh[0], dy = rh[3] - rh[2], dz = rh[5] - rh[4];
-  k_plane_wave<<<grid_n(V), 256, 0, st>>>((const double*)r_d, L, M, N, k[0], k[1], k[2], mk<double2>(Eo[0], Eo[1]),
-                                           mk<double2>(Eo[2], Eo[3]), mk<double2>(Eo[4], Eo[5]), dx, dy, dz,
-                                           (double2*)E_d);
-  count_launch();
-  MARIE_CUDA_TRY(cudaGetLastError());
-  MARIE_TRY(finish_out(E, E_d, 3 * V * sizeof(double2), st));
-  MARIE_CUDA_TRY(cudaStreamSynchronize(st));
-  return MARIE_OK;
-}
-
-int marie_dipole_field(const double* r, int64_t L, int64_t M, int64_t N, double ko, const double* Jd,
-                       const double* pos, int64_t ndip, double* E) {
-  if (!r || !Jd || !pos || !E || ndip < 1) return set_error(MARIE_EINVAL, "bad argument");
-  cudaStream_t st = 0;
-  const long long V = L * M * N;
-  DBuf tr, tJ, tP, tE;
-  const void *r_d, *J_d, *P_d;
-  void* E_d;
-  MARIE_TRY(stage_in(r, 3 * V * sizeof(double), st, tr, &r_d));
-  MARIE_TRY(stage_in(Jd, 3 * ndip * sizeof(double2), st, tJ, &J_d));
-  MARIE_TRY(stage_in(pos, 3 * ndip * sizeof(double), st, tP, &P_d));
-  MARIE_TRY(stage_out(E, 3 * V * sizeof(double2), st, tE, &E_d));
-  k_dipole_field<<<grid_n(V), 256, 0, st>>>((const double*)r_d, V, ko, (const double2*)J_d, (const double*)P_d,
-                                             (int)ndip, (double2*)E_d);
-  count_launch();
-  MARIE_CUDA_TRY(cudaGetLastError());
-  MARIE_TRY(finish_out(E, E_d, 3 * V * sizeof(double2), st));
-  MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+  if (solvert) *solvert = std::chrono::duration<double>(t1 - t0).count();
   return MARIE_OK;
 }
 

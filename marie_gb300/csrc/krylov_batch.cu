@@ -1,0 +1,568 @@
+// Batched, device-driven restarted GMRES for S systems that share one
+// operator (many right-hand sides of one body), with the semantics of the
+// reference's pgmres / pgmres_iter (src_numeric/src_iterative/pgmres.m:70-181,
+// pgmres_iter.m:22-150):
+//   * classical Gram-Schmidt, one pass (pgmres_iter.m:106-107);
+//   * the least-squares problem Hc \ rhs solved at every step (here by complex
+//     Givens rotations, then y by back-substitution) and the residual norm
+//     taken as ||rhs - Hc y|| (pgmres_iter.m:116-120);
+//   * a cycle stops at the first step whose residual is below tol*||b||;
+//   * x += R(V y), r = V(:,1:k+1) res at the end of a cycle (:133-150);
+//   * the true residual ||b - A x|| / ||b|| once at the end (pgmres.m:175).
+// All systems advance in lockstep; a system that has stopped inside a cycle
+// is skipped by every kernel (stop[s] < step), including the matvec passes.
+// The Hessenberg update, the rotations and the small solve run on the device
+// in FP64 (one warp per system), so a whole restart cycle has no host
+// synchronisation and is replayed as one CUDA graph launch.
+#include <cmath>
+#include <vector>
+
+#include "plan.h"
+
+namespace marie {
+
+static constexpr int BG = 152 * 2;  // row blocks per system for the reductions
+static constexpr int BT = 256;
+
+__device__ __forceinline__ double2 wsum2(double2 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  return v;
+}
+__device__ __forceinline__ double wsum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+// block sum, valid in thread 0
+__device__ double2 bsum2(double2 v) {
+  __shared__ double2 ws[32];
+  v = wsum2(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) ws[wid] = v;
+  __syncthreads();
+  double2 r = mk<double2>(0, 0);
+  if (wid == 0) {
+    r = lane < (int)(blockDim.x >> 5) ? ws[lane] : mk<double2>(0, 0);
+    r = wsum2(r);
+  }
+  return r;
+}
+__device__ __forceinline__ void rows_of(long long n, long long& i0, long long& i1) {
+  const long long chunk = (n + gridDim.x - 1) / gridDim.x;
+  i0 = blockIdx.x * chunk;
+  i1 = i0 + chunk < n ? i0 + chunk : n;
+}
+__device__ __forceinline__ bool skip(const int* stop, int s, int step) { return stop[s] < step; }
+
+// ||X_s||^2 partials: X_s = X + s*xs
+__global__ void __launch_bounds__(BT) kb_norm_part(const double2* __restrict__ X, long long xs, long long n,
+                                                   const int* __restrict__ stop, int step, double* __restrict__ part) {
+  const int s = blockIdx.y;
+  if (stop && skip(stop, s, step)) return;
+  const double2* x = X + s * xs;
+  long long i0, i1;
+  rows_of(n, i0, i1);
+  double a = 0;
+  for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    const double2 v = x[i];
+    a = fma(v.x, v.x, fma(v.y, v.y, a));
+  }
+  const double2 r = bsum2(mk<double2>(a, 0));
+  if (threadIdx.x == 0) part[(long long)s * gridDim.x + blockIdx.x] = r.x;
+}
+
+// norm[s] = sqrt(sum of partials), fixed order
+__global__ void kb_norm_fin(const double* __restrict__ part, int G, const int* __restrict__ stop, int step,
+                            double* __restrict__ out) {
+  const int s = blockIdx.x;
+  if (stop && skip(stop, s, step)) return;
+  double a = 0;
+  for (int b = threadIdx.x; b < G; b += 32) a += part[(long long)s * G + b];
+  a = wsum(a);
+  if (threadIdx.x == 0) out[s] = sqrt(a);
+}
+
+// cycle start: V_s(:,0) = r_s / beta_s ; g = [beta, 0, ...]
+__global__ void kb_cycle_init(const double2* __restrict__ r, long long rs, double2* __restrict__ Vb, long long vs,
+                              long long n, const double* __restrict__ beta, const int* __restrict__ stop) {
+  const int s = blockIdx.y;
+  if (stop[s] < 1) return;
+  const double inv = 1.0 / beta[s];  // 0 -> Inf/NaN exactly as the reference's r / norm(r)
+  const double2* x = r + s * rs;
+  double2* v = Vb + s * vs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    v[i] = mk<double2>(x[i].x * inv, x[i].y * inv);
+}
+
+// partial[s][j][b] = sum over block rows of conj(V_s(:,j)) w_s, j < k, w_s = V_s(:,k)
+__global__ void __launch_bounds__(BT) kb_dots(const double2* __restrict__ Vb, long long vs, long long n, int k,
+                                              const int* __restrict__ stop, double2* __restrict__ part) {
+  const int s = blockIdx.y;
+  if (skip(stop, s, k)) return;
+  const double2* V = Vb + s * vs;
+  const double2* w = V + (long long)k * n;
+  long long i0, i1;
+  rows_of(n, i0, i1);
+  for (int c0 = 0; c0 < k; c0 += 8) {
+    double2 acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = mk<double2>(0, 0);
+    const int nc = k - c0 < 8 ? k - c0 : 8;
+    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      const double2 wv = w[i];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < nc) {
+          const double2 v = V[(long long)(c0 + q) * n + i];
+          acc[q].x = fma(v.x, wv.x, fma(v.y, wv.y, acc[q].x));
+          acc[q].y = fma(v.x, wv.y, fma(-v.y, wv.x, acc[q].y));
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (q >= nc) break;
+      const double2 r = bsum2(acc[q]);
+      if (threadIdx.x == 0) part[((long long)s * 128 + c0 + q) * gridDim.x + blockIdx.x] = r;
+    }
+  }
+}
+
+// h[s][j] = sum_b part[s][j][b]  (grid k x S, one warp each)
+__global__ void kb_dots_fin(const double2* __restrict__ part, int G, int k, const int* __restrict__ stop,
+                            double2* __restrict__ h, int hld) {
+  const int j = blockIdx.x, s = blockIdx.y;
+  if (skip(stop, s, k)) return;
+  double2 a = mk<double2>(0, 0);
+  for (int b = threadIdx.x; b < G; b += 32) a = cadd(a, part[((long long)s * 128 + j) * G + b]);
+  a = wsum2(a);
+  if (threadIdx.x == 0) h[(long long)s * hld + j] = a;
+}
+
+// w_s -= V_s(:,0:k) h_s ; partial norms of the new w_s
+__global__ void __launch_bounds__(BT) kb_update(double2* __restrict__ Vb, long long vs, long long n, int k,
+                                                const double2* __restrict__ h, int hld, const int* __restrict__ stop,
+                                                double* __restrict__ part) {
+  const int s = blockIdx.y;
+  if (skip(stop, s, k)) return;
+  __shared__ double2 hs[128];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = h[(long long)s * hld + j];
+  __syncthreads();
+  double2* V = Vb + s * vs;
+  double2* w = V + (long long)k * n;
+  long long i0, i1;
+  rows_of(n, i0, i1);
+  double a = 0;
+  for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    double2 v = w[i];
+    for (int j = 0; j < k; ++j) {
+      const double2 b = V[(long long)j * n + i];
+      const double2 c = hs[j];
+      v.x = fma(-b.x, c.x, fma(b.y, c.y, v.x));
+      v.y = fma(-b.x, c.y, fma(-b.y, c.x, v.y));
+    }
+    w[i] = v;
+    a = fma(v.x, v.x, fma(v.y, v.y, a));
+  }
+  const double2 r = bsum2(mk<double2>(a, 0));
+  if (threadIdx.x == 0) part[(long long)s * gridDim.x + blockIdx.x] = r.x;
+}
+
+struct GState {
+  double2* H;    // [S][(m+1)*m] unrotated, column-major
+  double2* R;    // [S][(m+1)*m] rotated
+  double2* g;    // [S][m+1]
+  double* cs;    // [S][m]
+  double2* sn;   // [S][m]
+  double2* y;    // [S][m]
+  double2* res;  // [S][m+1]
+  double* resv;  // [S][m]
+  double* beta;  // [S]
+  double* tolabs;  // [S]
+  double* hn;    // [S]
+  int* stop;     // [S]: last step of the current cycle (0 = not iterating)
+};
+
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return mk<double2>((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+// one warp per system: H column k, rotations, y = R \ g, res = rhs - Hc y,
+// ||res||, stop test (pgmres_iter.m:106-125)
+__global__ void kb_givens(GState G, int m, int k, const double2* __restrict__ h, int hld,
+                          const double* __restrict__ npart, int NB) {
+  const int s = blockIdx.x;
+  const int lane = threadIdx.x;
+  if (G.stop[s] < k) return;
+  const int ld = m + 1;
+  double2* H = G.H + (long long)s * ld * m;
+  double2* R = G.R + (long long)s * ld * m;
+  double2* g = G.g + (long long)s * ld;
+  double* cs = G.cs + (long long)s * m;
+  double2* sn = G.sn + (long long)s * m;
+  double2* y = G.y + (long long)s * m;
+  double2* res = G.res + (long long)s * ld;
+  const int kk = k - 1;
+  double nn = 0;
+  for (int b = lane; b < NB; b += 32) nn += npart[(long long)s * NB + b];
+  nn = wsum(nn);
+  const double hnv = sqrt(nn);
+  for (int i = lane; i < k; i += 32) {
+    const double2 v = h[(long long)s * hld + i];
+    H[kk * ld + i] = v;
+    R[kk * ld + i] = v;
+  }
+  if (lane == 0) {
+    H[kk * ld + k] = mk<double2>(hnv, 0);
+    if (k == 1) {
+      g[0] = mk<double2>(G.beta[s], 0);
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    double2* col = R + kk * ld;
+    for (int i = 0; i < kk; ++i) {
+      const double2 a = col[i], b = col[i + 1];
+      const double c = cs[i];
+      const double2 sv = sn[i];
+      col[i] = cadd(cscale(a, c), cmul(sv, b));
+      col[i + 1] = csub(cscale(b, c), cmulc(a, sv));  // -conj(s) a + c b
+    }
+    const double2 a = col[kk];
+    const double aa = hypot(a.x, a.y), bb = hnv;
+    double c;
+    double2 sv;
+    if (aa == 0.0) {
+      c = 0.0;
+      sv = mk<double2>(1.0, 0.0);
+      col[kk] = mk<double2>(bb, 0);
+    } else {
+      const double rho = hypot(aa, bb);
+      const double2 ph = mk<double2>(a.x / aa, a.y / aa);
+      c = aa / rho;
+      sv = cscale(ph, bb / rho);  // ph * conj(b) / rho, b real
+      col[kk] = cscale(ph, rho);
+    }
+    col[k] = mk<double2>(0, 0);
+    cs[kk] = c;
+    sn[kk] = sv;
+    const double2 gk = g[kk];
+    g[kk] = cscale(gk, c);
+    g[k] = mk<double2>(-(sv.x * gk.x + sv.y * gk.y), -(sv.x * gk.y - sv.y * gk.x));  // -conj(s) g
+  }
+  __syncwarp();
+  // back-substitution y = R(0:k,0:k) \ g(0:k)
+  for (int i = k - 1; i >= 0; --i) {
+    double2 p = mk<double2>(0, 0);
+    for (int j = i + 1 + lane; j < k; j += 32) p = cadd(p, cmul(R[j * ld + i], y[j]));
+    p = wsum2(p);
+    if (lane == 0) y[i] = cdiv(csub(g[i], p), R[i * ld + i]);
+    __syncwarp();
+  }
+  // res = rhs - Hc y with rhs = [beta; 0], Hc = H(0:k+1, 0:k)
+  double rr = 0;
+  for (int i = lane; i <= k; i += 32) {
+    double2 v = i == 0 ? mk<double2>(G.beta[s], 0) : mk<double2>(0, 0);
+    for (int j = (i > 0 ? i - 1 : 0); j < k; ++j) v = csub(v, cmul(H[j * ld + i], y[j]));
+    res[i] = v;
+    rr = fma(v.x, v.x, fma(v.y, v.y, rr));
+  }
+  rr = wsum(rr);
+  if (lane == 0) {
+    const double rn = sqrt(rr);
+    G.resv[(long long)s * m + kk] = rn;
+    G.hn[s] = hnv;
+    if (rn < G.tolabs[s] || k == m) G.stop[s] = k;
+  }
+}
+
+// V_s(:,k) /= H(k+1,k)  (zero norm leaves a zero column instead of 0/0)
+__global__ void kb_scale(double2* __restrict__ Vb, long long vs, long long n, int k, const double* __restrict__ hn,
+                         const int* __restrict__ stop) {
+  const int s = blockIdx.y;
+  if (skip(stop, s, k)) return;
+  const double h = hn[s];
+  const double inv = h > 0 ? 1.0 / h : 0.0;
+  double2* w = Vb + s * vs + (long long)k * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    w[i] = mk<double2>(w[i].x * inv, w[i].y * inv);
+}
+
+// out_s = V_s(:, 0:c_s) coef_s with c_s = stop[s] + extra (skipped when stop[s] < 1)
+__global__ void kb_combine(const double2* __restrict__ Vb, long long vs, long long n, const double2* __restrict__ coef,
+                           int cld, const int* __restrict__ stop, int extra, double2* __restrict__ out, long long os,
+                           int accumulate) {
+  const int s = blockIdx.y;
+  const int k = stop[s];
+  if (k < 1) return;
+  const int nc = k + extra;
+  __shared__ double2 cf[129];
+  for (int j = threadIdx.x; j < nc; j += blockDim.x) cf[j] = coef[(long long)s * cld + j];
+  __syncthreads();
+  const double2* V = Vb + s * vs;
+  double2* o = out + s * os;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 v = accumulate ? o[i] : mk<double2>(0, 0);
+    for (int j = 0; j < nc; ++j) {
+      const double2 b = V[(long long)j * n + i];
+      v.x = fma(b.x, cf[j].x, fma(-b.y, cf[j].y, v.x));
+      v.y = fma(b.x, cf[j].y, fma(b.y, cf[j].x, v.y));
+    }
+    o[i] = v;
+  }
+}
+
+// y_s += x_s for systems in this cycle
+__global__ void kb_add(const double2* __restrict__ x, long long xs, double2* __restrict__ y, long long ys, long long n,
+                       const int* __restrict__ stop) {
+  const int s = blockIdx.y;
+  if (stop[s] < 1) return;
+  const double2* a = x + s * xs;
+  double2* b = y + s * ys;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = cadd(b[i], a[i]);
+}
+
+// y_s = b_s - y_s (all systems)
+__global__ void kb_sub_from(const double2* __restrict__ b, long long bs, double2* __restrict__ y, long long ys,
+                            long long n) {
+  const int s = blockIdx.y;
+  const double2* a = b + s * bs;
+  double2* c = y + s * ys;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    c[i] = csub(a[i], c[i]);
+}
+
+static inline int gx(long long n) {
+  long long g = (n + 255) / 256;
+  if (g > 152 * 4) g = 152 * 4;
+  return g < 1 ? 1 : (int)g;
+}
+
+struct BatchWork {
+  int S = 0, m = 0;
+  long long n = 0;
+  DBuf V, t1, t2, r, part_d, part_n, h, H, R, g, cs, sn, y, res, resv, beta, tol, hn, stop, norms;
+  GState gs{};
+  cudaGraphExec_t exec = nullptr;
+  long long graph_nodes = 0;
+  ~BatchWork() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+  int init(cudaStream_t st, int S_, int m_, long long n_) {
+    S = S_;
+    m = m_;
+    n = n_;
+    MARIE_TRY(V.alloc((size_t)S * (m + 1) * n * sizeof(double2), st));
+    MARIE_TRY(t1.alloc((size_t)S * n * sizeof(double2), st));
+    MARIE_TRY(t2.alloc((size_t)S * n * sizeof(double2), st));
+    MARIE_TRY(part_d.alloc((size_t)S * 128 * BG * sizeof(double2), st));
+    MARIE_TRY(part_n.alloc((size_t)S * BG * sizeof(double), st));
+    MARIE_TRY(h.alloc((size_t)S * (m + 1) * sizeof(double2), st));
+    MARIE_TRY(H.alloc((size_t)S * (m + 1) * m * sizeof(double2), st));
+    MARIE_TRY(R.alloc((size_t)S * (m + 1) * m * sizeof(double2), st));
+    MARIE_TRY(g.alloc((size_t)S * (m + 1) * sizeof(double2), st));
+    MARIE_TRY(cs.alloc((size_t)S * m * sizeof(double), st));
+    MARIE_TRY(sn.alloc((size_t)S * m * sizeof(double2), st));
+    MARIE_TRY(y.alloc((size_t)S * m * sizeof(double2), st));
+    MARIE_TRY(res.alloc((size_t)S * (m + 1) * sizeof(double2), st));
+    MARIE_TRY(resv.alloc((size_t)S * m * sizeof(double), st));
+    MARIE_TRY(beta.alloc((size_t)S * sizeof(double), st));
+    MARIE_TRY(tol.alloc((size_t)S * sizeof(double), st));
+    MARIE_TRY(hn.alloc((size_t)S * sizeof(double), st));
+    MARIE_TRY(stop.alloc((size_t)S * sizeof(int), st));
+    MARIE_TRY(norms.alloc((size_t)S * sizeof(double), st));
+    gs = GState{H.as<double2>(), R.as<double2>(), g.as<double2>(), cs.as<double>(), sn.as<double2>(),
+                y.as<double2>(), res.as<double2>(), resv.as<double>(), beta.as<double>(), tol.as<double>(),
+                hn.as<double>(), stop.as<int>()};
+    return MARIE_OK;
+  }
+  long long vs() const { return (long long)(m + 1) * n; }
+};
+
+// batched norms of X_s (stride xs) into host array
+static int bnorms(marie_plan* p, BatchWork& W, const double2* X, long long xs, std::vector<double>& out) {
+  cudaStream_t st = p->stream;
+  kb_norm_part<<<dim3(BG, W.S), BT, 0, st>>>(X, xs, W.n, nullptr, 0, W.part_n.as<double>());
+  kb_norm_fin<<<W.S, 32, 0, st>>>(W.part_n.as<double>(), BG, nullptr, 0, W.norms.as<double>());
+  count_launch(2);
+  MARIE_CUDA_TRY(cudaGetLastError());
+  out.resize(W.S);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(out.data(), W.norms.p, W.S * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+  return MARIE_OK;
+}
+
+// one restart cycle for all systems with stop[s] = m (others stop[s] = 0)
+static int cycle(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, double2* X,
+                 long long xs, double2* Rv, long long rs) {
+  cudaStream_t st = p->stream;
+  const int S = W.S, m = W.m;
+  const long long n = W.n, vs = W.vs();
+  double2* V = W.V.as<double2>();
+  int* stop = W.stop.as<int>();
+  kb_norm_part<<<dim3(BG, S), BT, 0, st>>>(Rv, rs, n, stop, 1, W.part_n.as<double>());
+  kb_norm_fin<<<S, 32, 0, st>>>(W.part_n.as<double>(), BG, stop, 1, W.beta.as<double>());
+  kb_cycle_init<<<dim3(gx(n), S), 256, 0, st>>>(Rv, rs, V, vs, n, W.beta.as<double>(), stop);
+  count_launch(3);
+  for (int k = 1; k <= m; ++k) {
+    const double2* src = V + (long long)(k - 1) * n;
+    long long ss = vs;
+    if (R1) {
+      MARIE_TRY(R1->apply(src, ss, W.t1.as<double2>(), n, S, stop, k));
+      src = W.t1.as<double2>();
+      ss = n;
+    }
+    double2* dst = V + (long long)k * n;
+    if (L1) {
+      MARIE_TRY(A.apply(src, ss, W.t2.as<double2>(), n, S, stop, k));
+      MARIE_TRY(L1->apply(W.t2.as<double2>(), n, dst, vs, S, stop, k));
+    } else {
+      MARIE_TRY(A.apply(src, ss, dst, vs, S, stop, k));
+    }
+    kb_dots<<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, stop, W.part_d.as<double2>());
+    kb_dots_fin<<<dim3(k, S), 32, 0, st>>>(W.part_d.as<double2>(), BG, k, stop, W.h.as<double2>(), m + 1);
+    kb_update<<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, W.h.as<double2>(), m + 1, stop, W.part_n.as<double>());
+    kb_givens<<<S, 32, 0, st>>>(W.gs, m, k, W.h.as<double2>(), m + 1, W.part_n.as<double>(), BG);
+    kb_scale<<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, k, W.hn.as<double>(), stop);
+    count_launch(5);
+  }
+  // x += R1(V y) ; r = V(:,1:k+1) res
+  kb_combine<<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, W.y.as<double2>(), m, stop, 0, W.t1.as<double2>(), n, 0);
+  count_launch();
+  const double2* upd = W.t1.as<double2>();
+  if (R1) {
+    MARIE_TRY(R1->apply(upd, n, W.t2.as<double2>(), n, S, stop, 1));
+    upd = W.t2.as<double2>();
+  }
+  kb_add<<<dim3(gx(n), S), 256, 0, st>>>(upd, n, X, xs, n, stop);
+  kb_combine<<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, W.res.as<double2>(), m + 1, stop, 1, Rv, rs, 0);
+  count_launch(2);
+  MARIE_CUDA_TRY(cudaGetLastError());
+  return MARIE_OK;
+}
+
+int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const double2* B,
+                long long bs, long long n, int S, int restart, double tol, int maxit, double2* X, long long xs,
+                std::vector<GmresResult>& out, bool use_graph, const std::vector<int>* active_in,
+                bool true_residual) {
+  if (restart < 1 || restart > 127) return set_error(MARIE_EINVAL, "restart must be in [1, 127]");
+  if (S < 1) return set_error(MARIE_EINVAL, "need at least one system");
+  cudaStream_t st = p->stream;
+  BatchWork W;
+  MARIE_TRY(W.init(st, S, restart, n));
+  DBuf rb, bpb;
+  MARIE_TRY(rb.alloc((size_t)S * n * sizeof(double2), st));
+  double2* Rv = rb.as<double2>();
+  const long long rs = n;
+  // x0 = 0 ; r = b ; left preconditioning of r and b (pgmres.m:118-150)
+  for (int s = 0; s < S; ++s) MARIE_CUDA_TRY(cudaMemsetAsync(X + s * xs, 0, n * sizeof(double2), st));
+  for (int s = 0; s < S; ++s)
+    MARIE_CUDA_TRY(cudaMemcpyAsync(Rv + s * rs, B + s * bs, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  std::vector<double> bnorm(S), rn(S);
+  std::vector<int> all(S, 1);
+  DBuf allstop;
+  MARIE_TRY(allstop.alloc(S * sizeof(int), st));
+  {
+    std::vector<int> big(S, 1 << 30);
+    MARIE_CUDA_TRY(cudaMemcpyAsync(allstop.p, big.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+  }
+  if (L1) {
+    MARIE_TRY(bpb.alloc((size_t)S * n * sizeof(double2), st));
+    MARIE_TRY(L1->apply(Rv, rs, W.t1.as<double2>(), n, S, allstop.as<int>(), 1));
+    MARIE_CUDA_TRY(cudaMemcpyAsync(Rv, W.t1.p, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    MARIE_CUDA_TRY(cudaMemcpyAsync(bpb.p, Rv, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    MARIE_TRY(bnorms(p, W, bpb.as<double2>(), n, bnorm));
+  } else {
+    MARIE_TRY(bnorms(p, W, B, bs, bnorm));
+  }
+  MARIE_TRY(bnorms(p, W, Rv, rs, rn));
+  out.assign(S, GmresResult());
+  std::vector<int> outit(S, 0), pk(S, 0), active(S, 0);
+  for (int s = 0; s < S; ++s) {
+    out[s].resvec.push_back(rn[s] / bnorm[s]);
+    active[s] = (out[s].resvec.back() > tol && maxit > 0 && (!active_in || (*active_in)[s])) ? 1 : 0;
+  }
+  std::vector<double> tolabs(S);
+  for (int s = 0; s < S; ++s) tolabs[s] = tol * bnorm[s];
+  MARIE_CUDA_TRY(cudaMemcpyAsync(W.tol.p, tolabs.data(), S * sizeof(double), cudaMemcpyHostToDevice, st));
+  std::vector<int> stop(S);
+  std::vector<double> resv((size_t)S * restart);
+  int cycles = 0;
+  while (true) {
+    bool any = false;
+    for (int s = 0; s < S; ++s) {
+      stop[s] = active[s] ? restart : 0;
+      any = any || active[s];
+    }
+    if (!any) break;
+    MARIE_CUDA_TRY(cudaMemcpyAsync(W.stop.p, stop.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (use_graph && cycles >= 1) {
+      if (!W.exec) {
+        cudaGraph_t graph;
+        MARIE_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int s1 = cycle(p, W, A, L1, R1, X, xs, Rv, rs);
+        cudaError_t e = cudaStreamEndCapture(st, &graph);
+        MARIE_TRY(s1);
+        MARIE_CUDA_TRY(e);
+        size_t nodes = 0;
+        cudaGraphGetNodes(graph, nullptr, &nodes);
+        W.graph_nodes = (long long)nodes;
+        e = cudaGraphInstantiate(&W.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        MARIE_CUDA_TRY(e);
+      }
+      MARIE_CUDA_TRY(cudaGraphLaunch(W.exec, st));
+      count_launch(W.graph_nodes);
+    } else {
+      MARIE_TRY(cycle(p, W, A, L1, R1, X, xs, Rv, rs));
+    }
+    ++cycles;
+    MARIE_CUDA_TRY(cudaMemcpyAsync(stop.data(), W.stop.p, S * sizeof(int), cudaMemcpyDeviceToHost, st));
+    MARIE_CUDA_TRY(cudaMemcpyAsync(resv.data(), W.resv.p, resv.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int s = 0; s < S; ++s) {
+      if (!active[s]) continue;
+      ++outit[s];
+      pk[s] = stop[s];
+      for (int j = 0; j < stop[s]; ++j) out[s].resvec.push_back(resv[(size_t)s * restart + j] / bnorm[s]);
+      active[s] = (out[s].resvec.back() > tol && outit[s] < maxit) ? 1 : 0;
+    }
+  }
+  for (int s = 0; s < S; ++s) {
+    out[s].iter[0] = pk[s];
+    out[s].iter[1] = outit[s];
+  }
+  if (!true_residual) {
+    for (int s = 0; s < S; ++s) {
+      out[s].relres = out[s].resvec.back();
+      out[s].flag = out[s].relres <= tol ? 0 : 1;
+    }
+    return MARIE_OK;
+  }
+  // true residuals (pgmres.m:175-180)
+  {
+    std::vector<int> big(S, 1 << 30);
+    MARIE_CUDA_TRY(cudaMemcpyAsync(allstop.p, big.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+  }
+  MARIE_TRY(A.apply(X, xs, W.t1.as<double2>(), n, S, allstop.as<int>(), 1));
+  kb_sub_from<<<dim3(gx(n), S), 256, 0, st>>>(B, bs, W.t1.as<double2>(), n, n);
+  count_launch();
+  std::vector<double> tr, bn;
+  MARIE_TRY(bnorms(p, W, W.t1.as<double2>(), n, tr));
+  MARIE_TRY(bnorms(p, W, B, bs, bn));
+  for (int s = 0; s < S; ++s) {
+    out[s].iter[0] = pk[s];
+    out[s].iter[1] = outit[s];
+    out[s].relres = tr[s] / bn[s];
+    out[s].flag = out[s].relres <= tol ? 0 : 1;
+  }
+  return MARIE_OK;
+}
+
+}  // namespace marie

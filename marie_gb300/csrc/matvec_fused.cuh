@@ -1,0 +1,236 @@
+// Fused x+y passes of the matvec, one (z, component) plane per thread-block
+// cluster, exchanging the x-transformed rows through distributed shared memory
+// instead of a round trip of the A spectrum through HBM.
+//
+//   k_xyfwd:  gather J (inv map) -> FFT_x of the M non-zero rows (CTA q of the
+//             cluster owns rows [q*M/CS, (q+1)*M/CS)) -> each output (kx, y) is
+//             stored into the shared memory of the CTA that owns column kx ->
+//             cluster barrier -> FFT_y of the owned 2L/CS columns -> B.
+//   k_yxinv:  B -> inverse FFT_y of the owned columns, keep y < M -> rows sent
+//             to their owners -> cluster barrier -> inverse FFT_x of the owned
+//             rows, keep x < L -> Gram*Mr*J - Mc*(N J) epilogue -> scatter.
+//
+// Both kernels write/read the spectrum B[c][z][ky][kx] of the z pass, so the
+// matvec is xyfwd -> zmul -> yxinv: 48V complex of spectrum traffic per RHS.
+#pragma once
+#include <cooperative_groups.h>
+
+#include "matvec_kernels.cuh"
+
+namespace marie {
+
+namespace cg = cooperative_groups;
+
+template <typename T, int NL, int NM, int CS> struct XYCfg {
+  using V = cplx<T>;
+  using FX = FFT<V, NL, false>;
+  using FXI = FFT<V, NL, true>;
+  using FY = FFT<V, NM, false>;
+  using FYI = FFT<V, NM, true>;
+  static constexpr int THREADS = 256;
+  static constexpr int L = NL / 2, M = NM / 2;
+  static constexpr int RY = M / CS;                 // rows per CTA
+  static constexpr int CW = NL / CS;                // columns per CTA
+  static constexpr int SX = THREADS / FX::T;        // rows per x sweep
+  static constexpr int SY = THREADS / FY::T;        // columns per y sweep
+  static constexpr int ROWP = NL + NL / 16;         // swizzled row pitch
+  static constexpr int RS = CW + 1;                 // pitch of the column receive buffer
+  static constexpr int RYP = ((RY + SX - 1) / SX) * SX;
+  static constexpr int XB = (SX * ROWP > NM * (SY + 1)) ? SX * ROWP : NM * (SY + 1);
+  static constexpr size_t fwd_smem = (size_t)(NL + NM + M * RS + XB) * sizeof(V);
+  static constexpr size_t inv_smem = (size_t)(NL + NM + RYP * ROWP + NM * (SY + 1)) * sizeof(V);
+  static constexpr bool ok = (M % CS == 0) && (NL % CS == 0) && RY >= 1 && FX::T <= THREADS &&
+                             FY::T <= THREADS;
+};
+
+template <typename T, int NL, int NM, int CS>
+__global__ void __launch_bounds__(256)
+k_xyfwd(const double2* __restrict__ J, long long js, const int* __restrict__ inv, Prologue pro,
+        cplx<T>* __restrict__ B, long long bs, Dims d, const cplx<T>* __restrict__ twx,
+        const cplx<T>* __restrict__ twy) {
+  if (rhs_skipped(d, blockIdx.y)) return;  // uniform over the cluster
+  using C = XYCfg<T, NL, NM, CS>;
+  using V = cplx<T>;
+  using FX = typename C::FX;
+  using FY = typename C::FY;
+  constexpr int L = C::L, M = C::M;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* twx_s = reinterpret_cast<V*>(smem_raw);
+  V* twy_s = twx_s + NL;
+  V* recv = twy_s + NM;    // [y][col], M x RS
+  V* xb = recv + M * C::RS;  // exchange buffer
+  cg::cluster_group cluster = cg::this_cluster();
+  const int q = (int)cluster.block_rank();
+  const int plane = blockIdx.x / CS;  // z + N*c
+  const double2* Jr = J + blockIdx.y * js;
+  for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
+  for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
+  cluster.sync();  // every CTA of the cluster runs before remote stores; twiddles staged
+
+  // ---- x transforms of the owned rows, results to the owners of their columns
+  {
+    constexpr int E = FX::E, R0 = FX::R0, RL = FX::RL;
+    const int t = threadIdx.x % FX::T, s = threadIdx.x / FX::T;
+    for (int row0 = 0; row0 < C::RY; row0 += C::SX) {
+      const int yl = row0 + s;
+      const bool valid = yl < C::RY;
+      const int y = q * C::RY + yl;
+      V reg[E];
+#pragma unroll
+      for (int b = 0; b < E / R0; ++b)
+#pragma unroll
+        for (int r = 0; r < R0; ++r) {
+          const int p = FX::in_pos(t, b, r);
+          V val = mk<V>(0, 0);
+          if (valid && r < R0 / 2 && p < L) {
+            const int k = inv[(long long)p + (long long)L * (y + (long long)M * plane)];
+            if (k >= 0) {
+              double2 jv = Jr[k];
+              if (pro.conjin) jv.y = -jv.y;
+              if (pro.pre) jv = cmul(pro.pre[k], jv);
+              val = cvt<V>(jv);
+            }
+          }
+          reg[b * R0 + r] = val;
+        }
+      FX::run_half(reg, xb + s * C::ROWP, SAddr(1, true), t, twx_s);
+      if (valid) {
+#pragma unroll
+        for (int b = 0; b < E / RL; ++b)
+#pragma unroll
+          for (int r = 0; r < RL; ++r) {
+            const int kx = FX::out_pos(t, b, r);
+            V* dst = cluster.map_shared_rank(recv, kx / C::CW);
+            dst[y * C::RS + (kx % C::CW)] = reg[b * RL + r];
+          }
+      }
+    }
+  }
+  cluster.sync();  // all rows delivered
+
+  // ---- y transforms of the owned columns, straight to B
+  {
+    constexpr int E = FY::E, R0 = FY::R0, RL = FY::RL;
+    const int s = threadIdx.x % C::SY, t = threadIdx.x / C::SY;
+    V* Bp = B + blockIdx.y * bs + (long long)plane * NM * NL + q * C::CW;
+    for (int c0 = 0; c0 < C::CW; c0 += C::SY) {
+      const int col = c0 + s;
+      const bool valid = col < C::CW;
+      V reg[E];
+#pragma unroll
+      for (int b = 0; b < E / R0; ++b)
+#pragma unroll
+        for (int r = 0; r < R0; ++r) {
+          const int p = FY::in_pos(t, b, r);
+          reg[b * R0 + r] = (valid && r < R0 / 2 && p < M) ? recv[p * C::RS + col] : mk<V>(0, 0);
+        }
+      FY::run_half(reg, xb + s, SAddr(C::SY + 1), t, twy_s);
+      if (valid) {
+#pragma unroll
+        for (int b = 0; b < E / RL; ++b)
+#pragma unroll
+          for (int r = 0; r < RL; ++r) {
+            const int ky = FY::out_pos(t, b, r);
+            Bp[(long long)ky * NL + col] = reg[b * RL + r];
+          }
+      }
+    }
+  }
+}
+
+template <typename T, int NL, int NM, int CS>
+__global__ void __launch_bounds__(256)
+k_yxinv(const cplx<T>* __restrict__ B, long long bs, const double2* __restrict__ J, long long js,
+        const int* __restrict__ inv, Epilogue ep, double2* __restrict__ out, long long os, Dims d,
+        const cplx<T>* __restrict__ twx, const cplx<T>* __restrict__ twy) {
+  if (rhs_skipped(d, blockIdx.y)) return;  // uniform over the cluster
+  using C = XYCfg<T, NL, NM, CS>;
+  using V = cplx<T>;
+  using FXI = typename C::FXI;
+  using FYI = typename C::FYI;
+  constexpr int L = C::L, M = C::M;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* twx_s = reinterpret_cast<V*>(smem_raw);
+  V* twy_s = twx_s + NL;
+  V* rows = twy_s + NM;             // [yl][swizzled kx], RYP x ROWP
+  V* xb = rows + C::RYP * C::ROWP;  // column exchange buffer
+  cg::cluster_group cluster = cg::this_cluster();
+  const int q = (int)cluster.block_rank();
+  const int plane = blockIdx.x / CS;
+  for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
+  for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
+  cluster.sync();
+  const SAddr rowa(1, true);
+
+  // ---- inverse y transforms of the owned columns, kept rows to their owners
+  {
+    constexpr int E = FYI::E, R0 = FYI::R0, RL = FYI::RL;
+    const int s = threadIdx.x % C::SY, t = threadIdx.x / C::SY;
+    const V* Bp = B + blockIdx.y * bs + (long long)plane * NM * NL + q * C::CW;
+    for (int c0 = 0; c0 < C::CW; c0 += C::SY) {
+      const int col = c0 + s;
+      const bool valid = col < C::CW;
+      const int kx = q * C::CW + col;
+      V reg[E];
+#pragma unroll
+      for (int b = 0; b < E / R0; ++b)
+#pragma unroll
+        for (int r = 0; r < R0; ++r)
+          reg[b * R0 + r] = valid ? Bp[(long long)FYI::in_pos(t, b, r) * NL + col] : mk<V>(0, 0);
+      FYI::run(reg, xb + s, SAddr(C::SY + 1), t, twy_s);
+#pragma unroll
+      for (int b = 0; b < E / RL; ++b)
+#pragma unroll
+        for (int r = 0; r < RL; ++r) {
+          const int y = FYI::out_pos(t, b, r);
+          if (valid && y < M) {
+            V* dst = cluster.map_shared_rank(rows, y / C::RY);
+            dst[(y % C::RY) * C::ROWP + rowa(kx)] = reg[b * RL + r];
+          }
+        }
+    }
+  }
+  cluster.sync();
+
+  // ---- inverse x transforms of the owned rows, epilogue, scatter
+  {
+    constexpr int E = FXI::E, RL = FXI::RL;
+    const int t = threadIdx.x % FXI::T, s = threadIdx.x / FXI::T;
+    const double2* Jr = J + blockIdx.y * js;
+    double2* outr = out + blockIdx.y * os;
+    for (int row0 = 0; row0 < C::RYP; row0 += C::SX) {
+      const int yl = row0 + s;
+      const bool valid = yl < C::RY;
+      const int y = q * C::RY + yl;
+      V* base = rows + yl * C::ROWP;
+      V reg[E];
+      FXI::load(reg, base, rowa, t, NL);
+      FXI::run(reg, base, rowa, t, twx_s);
+      if (valid) {
+#pragma unroll
+        for (int b = 0; b < E / RL; ++b)
+#pragma unroll
+          for (int r = 0; r < RL; ++r) {
+            const int x = FXI::out_pos(t, b, r);
+            if (x >= L) continue;
+            const int k = inv[(long long)x + (long long)L * (y + (long long)M * plane)];
+            if (k < 0) continue;
+            const double2 v = cvt<double2>(reg[b * RL + r]);
+            const double2 jv = Jr[k];
+            const double2 A_k = ep.a ? ep.a[k] : ep.a_s;
+            double2 res = cmul(A_k, jv);
+            if (ep.conjout) {
+              res.x -= v.x;
+              res.y += v.y;
+            } else {
+              const double2 B_k = ep.b ? ep.b[k] : ep.b_s;
+              res = csub(res, cmul(B_k, v));
+            }
+            outr[k] = res;
+          }
+      }
+    }
+  }
+}
+
+}  // namespace marie

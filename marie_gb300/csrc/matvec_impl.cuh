@@ -1,6 +1,7 @@
 // Definitions of the matvec launchers; included only by the two translation
 // units that instantiate them (matvec_f32.cu, matvec_f64.cu).
 #pragma once
+#include "matvec_fused.cuh"
 #include "matvec_launch.cuh"
 
 namespace marie {
@@ -11,44 +12,45 @@ template <typename T> struct MatvecImpl {
   template <int NL>
   static cudaError_t xfwd_n(const double2* J, long long js, const int* inv, Prologue pro, V* A, long long as,
                             const Dims& d, const V* tw, int nrhs, cudaStream_t st) {
-    constexpr int S = RowCfg<NL>::S;
+    constexpr int S = RowCfg<cplx<T>, NL>::S;
     const size_t smem = (size_t)(NL + NL * (S + 1)) * sizeof(V);
     cudaError_t e = opt_in_smem(k_xfwd<T, NL>, smem);
     if (e != cudaSuccess) return e;
     const int rows = d.M * d.N * 3;
     dim3 grid((rows + S - 1) / S, nrhs);
-    k_xfwd<T, NL><<<grid, RowCfg<NL>::THREADS, smem, st>>>(J, js, inv, pro, A, as, d, tw);
+    k_xfwd<T, NL><<<grid, RowCfg<cplx<T>, NL>::THREADS, smem, st>>>(J, js, inv, pro, A, as, d, tw);
     return cudaGetLastError();
   }
   template <int NL>
   static cudaError_t xinv_n(const V* A, long long as, const double2* J, long long js, const int* inv, Epilogue ep,
                             double2* out, long long os, const Dims& d, const V* tw, int nrhs, cudaStream_t st) {
-    constexpr int S = RowCfg<NL>::S;
+    constexpr int S = RowCfg<cplx<T>, NL>::S;
     const size_t smem = (size_t)(NL + NL * (S + 1)) * sizeof(V);
     cudaError_t e = opt_in_smem(k_xinv<T, NL>, smem);
     if (e != cudaSuccess) return e;
     const int rows = d.M * d.N * 3;
     dim3 grid((rows + S - 1) / S, nrhs);
-    k_xinv<T, NL><<<grid, RowCfg<NL>::THREADS, smem, st>>>(A, as, J, js, inv, ep, out, os, d, tw);
+    k_xinv<T, NL><<<grid, RowCfg<cplx<T>, NL>::THREADS, smem, st>>>(A, as, J, js, inv, ep, out, os, d, tw);
     return cudaGetLastError();
   }
   template <int NC, bool INV>
   static cudaError_t cols_n(const V* in, long long in_w, long long in_rhs, int n_in, V* out, long long out_w,
-                            long long out_rhs, int n_out, int Lp, int nw, const V* tw, int nrhs, cudaStream_t st) {
+                            long long out_rhs, int n_out, int Lp, int nw, const V* tw, int nrhs, cudaStream_t st,
+                            const int* stop, int step) {
     constexpr int S = ColS<T>::S;
     const size_t smem = (size_t)(NC + NC * (S + 1)) * sizeof(V);
     cudaError_t e = opt_in_smem(k_cols<T, NC, INV>, smem);
     if (e != cudaSuccess) return e;
     dim3 grid((Lp + S - 1) / S, nw, nrhs);
     k_cols<T, NC, INV><<<grid, S * FFT<V, NC, INV>::T, smem, st>>>(in, in_w, in_rhs, n_in, out, out_w, out_rhs,
-                                                                  n_out, Lp, tw);
+                                                                  n_out, Lp, tw, stop, step);
     return cudaGetLastError();
   }
   template <int NZ>
   static cudaError_t zmul_n(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
                             cudaStream_t st) {
     constexpr int S = ZS<T, NZ>::S;
-    const size_t smem = (size_t)ZS<T, NZ>::bytes(S);
+    const size_t smem = (size_t)ZS<T, NZ>::bytes(S);  // S columns, 3 component buffers
     cudaError_t e = opt_in_smem(k_zmul<T, NZ>, smem);
     if (e != cudaSuccess) return e;
     dim3 grid((d.Lp + S - 1) / S, d.Mp, nrhs);
@@ -76,18 +78,18 @@ template <typename T> struct MatvecImpl {
   }
   static cudaError_t cols(bool inv, int NC, const V* in, long long in_w, long long in_rhs, int n_in, V* out,
                           long long out_w, long long out_rhs, int n_out, int Lp, int nw, const V* tw, int nrhs,
-                          cudaStream_t st) {
+                          cudaStream_t st, const int* stop, int step) {
     if (inv) {
       switch (NC) {
 #define MARIE_CASE(n_) \
-  case n_: return cols_n<n_, true>(in, in_w, in_rhs, n_in, out, out_w, out_rhs, n_out, Lp, nw, tw, nrhs, st);
+  case n_: return cols_n<n_, true>(in, in_w, in_rhs, n_in, out, out_w, out_rhs, n_out, Lp, nw, tw, nrhs, st, stop, step);
         MARIE_FFT_LENGTHS(MARIE_CASE)
 #undef MARIE_CASE
       }
     } else {
       switch (NC) {
 #define MARIE_CASE(n_) \
-  case n_: return cols_n<n_, false>(in, in_w, in_rhs, n_in, out, out_w, out_rhs, n_out, Lp, nw, tw, nrhs, st);
+  case n_: return cols_n<n_, false>(in, in_w, in_rhs, n_in, out, out_w, out_rhs, n_out, Lp, nw, tw, nrhs, st, stop, step);
         MARIE_FFT_LENGTHS(MARIE_CASE)
 #undef MARIE_CASE
       }
@@ -106,6 +108,89 @@ template <typename T> struct MatvecImpl {
 };
 
 
+// (2L, 2M, cluster size) of the grids with fused x+y passes
+#define MARIE_FUSED_PAIRS(X) X(64, 64, 2) X(96, 96, 2) X(128, 128, 4) X(192, 192, 4) X(256, 256, 8) X(512, 384, 8)
+
+template <typename T> struct FusedImpl {
+  using V = cplx<T>;
+  template <int NL, int NM, int CS> static constexpr bool usable() {
+    using C = XYCfg<T, NL, NM, CS>;
+    // FP64 is FP64-pipe bound on GB300: the fused kernels' lower occupancy costs
+    // more than the saved spectrum traffic, so FP64 keeps the five-pass path.
+    return sizeof(T) == 4 && C::ok && C::fwd_smem <= 220 * 1024 && C::inv_smem <= 220 * 1024;
+  }
+  template <typename K>
+  static cudaError_t launch(K kern, int CS, int nblocks, int nrhs, size_t smem, cudaStream_t st, void** args) {
+    cudaError_t e = opt_in_smem(kern, smem);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nblocks, nrhs, 1);
+    cfg.blockDim = dim3(256, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)CS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, (const void*)kern, args);
+  }
+  template <int NL, int NM, int CS>
+  static cudaError_t xyfwd_n(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
+                             Dims d, const V* twx, const V* twy, int nrhs, cudaStream_t st) {
+    if constexpr (usable<NL, NM, CS>()) {
+      void* args[] = {(void*)&J, (void*)&js, (void*)&inv, (void*)&pro, (void*)&B, (void*)&bs, (void*)&d,
+                      (void*)&twx, (void*)&twy};
+      return launch(k_xyfwd<T, NL, NM, CS>, CS, CS * 3 * d.N, nrhs, XYCfg<T, NL, NM, CS>::fwd_smem, st, args);
+    } else {
+      return cudaErrorNotSupported;
+    }
+  }
+  template <int NL, int NM, int CS>
+  static cudaError_t yxinv_n(const V* B, long long bs, const double2* J, long long js, const int* inv, Epilogue ep,
+                             double2* out, long long os, Dims d, const V* twx, const V* twy, int nrhs,
+                             cudaStream_t st) {
+    if constexpr (usable<NL, NM, CS>()) {
+      void* args[] = {(void*)&B, (void*)&bs, (void*)&J, (void*)&js, (void*)&inv, (void*)&ep, (void*)&out,
+                      (void*)&os, (void*)&d, (void*)&twx, (void*)&twy};
+      return launch(k_yxinv<T, NL, NM, CS>, CS, CS * 3 * d.N, nrhs, XYCfg<T, NL, NM, CS>::inv_smem, st, args);
+    } else {
+      return cudaErrorNotSupported;
+    }
+  }
+};
+
+template <typename T> bool MatvecLaunch<T>::fused(const Dims& d) {
+#define MARIE_CASE(a_, b_, c_) \
+  if (d.Lp == a_ && d.Mp == b_) return FusedImpl<T>::template usable<a_, b_, c_>();
+  MARIE_FUSED_PAIRS(MARIE_CASE)
+#undef MARIE_CASE
+  return false;
+}
+template <typename T>
+cudaError_t MatvecLaunch<T>::xyfwd(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
+                                   const Dims& d, const V* twx, const V* twy, int nrhs, cudaStream_t st) {
+#define MARIE_CASE(a_, b_, c_)    \
+  if (d.Lp == a_ && d.Mp == b_) \
+    return FusedImpl<T>::template xyfwd_n<a_, b_, c_>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
+  MARIE_FUSED_PAIRS(MARIE_CASE)
+#undef MARIE_CASE
+  return cudaErrorNotSupported;
+}
+template <typename T>
+cudaError_t MatvecLaunch<T>::yxinv(const V* B, long long bs, const double2* J, long long js, const int* inv,
+                                   Epilogue ep, double2* out, long long os, const Dims& d, const V* twx, const V* twy,
+                                   int nrhs, cudaStream_t st) {
+#define MARIE_CASE(a_, b_, c_)    \
+  if (d.Lp == a_ && d.Mp == b_) \
+    return FusedImpl<T>::template yxinv_n<a_, b_, c_>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
+  MARIE_FUSED_PAIRS(MARIE_CASE)
+#undef MARIE_CASE
+  return cudaErrorNotSupported;
+}
+
 template <typename T>
 cudaError_t MatvecLaunch<T>::xfwd(const double2* J, long long js, const int* inv, Prologue pro, V* A, long long as,
                                   const Dims& d, const V* tw, int nrhs, cudaStream_t st) {
@@ -120,8 +205,9 @@ cudaError_t MatvecLaunch<T>::xinv(const V* A, long long as, const double2* J, lo
 template <typename T>
 cudaError_t MatvecLaunch<T>::cols(bool inv, int NC, const V* in, long long in_w, long long in_rhs, int n_in, V* out,
                                   long long out_w, long long out_rhs, int n_out, int Lp, int nw, const V* tw,
-                                  int nrhs, cudaStream_t st) {
-  return MatvecImpl<T>::cols(inv, NC, in, in_w, in_rhs, n_in, out, out_w, out_rhs, n_out, Lp, nw, tw, nrhs, st);
+                                  int nrhs, cudaStream_t st, const int* stop, int step) {
+  return MatvecImpl<T>::cols(inv, NC, in, in_w, in_rhs, n_in, out, out_w, out_rhs, n_out, Lp, nw, tw, nrhs, st, stop,
+                             step);
 }
 template <typename T>
 cudaError_t MatvecLaunch<T>::zmul(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,

@@ -25,7 +25,13 @@ namespace marie {
 struct Dims {
   int L, M, N, Lp, Mp, Np;
   long long V;  // L*M*N
+  // Batched solves: right-hand side r is skipped when stop[r] < step (a
+  // system that has left the current GMRES cycle).  stop == nullptr: none.
+  const int* stop = nullptr;
+  int step = 0;
 };
+
+__device__ __forceinline__ bool rhs_skipped(const Dims& d, int rhs) { return d.stop && d.stop[rhs] < d.step; }
 
 // Epilogue: out[k] = A_k * J[k] - (conjout ? conj(v) : B_k * v)
 struct Epilogue {
@@ -40,8 +46,8 @@ struct Prologue {
   int conjin;
 };
 
-template <int N> struct RowCfg {
-  static constexpr int T = FFT<float2, N, false>::T;
+template <typename V, int N> struct RowCfg {
+  static constexpr int T = FFT<V, N, false>::T;
   static constexpr int S = (256 / T) < 2 ? 2 : (256 / T);
   static constexpr int THREADS = S * T;
 };
@@ -56,16 +62,17 @@ __device__ __forceinline__ void stage_twiddles(V* tw_s, const V* __restrict__ tw
 // xfwd: gather + forward x transform.  grid.x = ceil(rows / S), grid.y = rhs
 // ---------------------------------------------------------------------------
 template <typename T, int NL>
-__global__ void __launch_bounds__(RowCfg<NL>::THREADS)
+__global__ void __launch_bounds__(RowCfg<cplx<T>, NL>::THREADS)
 k_xfwd(const double2* __restrict__ J, long long j_stride, const int* __restrict__ inv, Prologue pro,
        cplx<T>* __restrict__ A, long long a_stride, Dims d, const cplx<T>* __restrict__ tw) {
   using V = cplx<T>;
   using F = FFT<V, NL, false>;
-  constexpr int S = RowCfg<NL>::S;
+  constexpr int S = RowCfg<cplx<T>, NL>::S;
   constexpr int ES = S + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw_s = reinterpret_cast<V*>(smem_raw);
   V* buf = tw_s + NL;
+  if (rhs_skipped(d, blockIdx.y)) return;
   const int rows = d.M * d.N * 3;
   const int row0 = blockIdx.x * S;
   const double2* Jr = J + blockIdx.y * j_stride;
@@ -108,17 +115,18 @@ k_xfwd(const double2* __restrict__ J, long long j_stride, const int* __restrict_
 // xinv: inverse x transform + crop + epilogue + scatter to DOFs.
 // ---------------------------------------------------------------------------
 template <typename T, int NL>
-__global__ void __launch_bounds__(RowCfg<NL>::THREADS)
+__global__ void __launch_bounds__(RowCfg<cplx<T>, NL>::THREADS)
 k_xinv(const cplx<T>* __restrict__ A, long long a_stride, const double2* __restrict__ J, long long j_stride,
        const int* __restrict__ inv, Epilogue ep, double2* __restrict__ out, long long o_stride, Dims d,
        const cplx<T>* __restrict__ tw) {
   using V = cplx<T>;
   using F = FFT<V, NL, true>;
-  constexpr int S = RowCfg<NL>::S;
+  constexpr int S = RowCfg<cplx<T>, NL>::S;
   constexpr int ES = S + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw_s = reinterpret_cast<V*>(smem_raw);
   V* buf = tw_s + NL;
+  if (rhs_skipped(d, blockIdx.y)) return;
   const int rows = d.M * d.N * 3;
   const int row0 = blockIdx.x * S;
   const V* Ar = A + blockIdx.y * a_stride;
@@ -175,7 +183,8 @@ template <typename T, int NC, bool INV>
 __global__ void __launch_bounds__(ColS<T>::S * FFT<cplx<T>, NC, INV>::T)
 k_cols(const cplx<T>* __restrict__ in, long long in_w, long long in_rhs, int n_in,
        cplx<T>* __restrict__ out, long long out_w, long long out_rhs, int n_out, int Lp,
-       const cplx<T>* __restrict__ tw) {
+       const cplx<T>* __restrict__ tw, const int* __restrict__ stop, int step) {
+  if (stop && stop[blockIdx.z] < step) return;
   using V = cplx<T>;
   using F = FFT<V, NC, INV>;
   constexpr int S = ColS<T>::S;
@@ -231,10 +240,11 @@ k_cols(const cplx<T>* __restrict__ in, long long in_w, long long in_rhs, int n_i
 // fN[q][kz][ky][kx].
 // ---------------------------------------------------------------------------
 template <typename T, int NZ> struct ZS {
-  static constexpr int S0 = ColS<T>::S;
+  static constexpr int TT = FFT<cplx<T>, NZ, false>::T;   // threads per transform
+  static constexpr int S0 = sizeof(T) == 4 ? 8 : 4;        // columns per CTA
+  static constexpr int S = (3 * S0 * TT <= 1024) ? S0 : ((3 * (S0 / 2) * TT <= 1024) ? S0 / 2 : S0 / 4);
+  static constexpr int THREADS = 3 * S * TT;               // one thread group per component
   static constexpr long long bytes(int s) { return (long long)(NZ + 3 * NZ * (s + 1)) * sizeof(cplx<T>); }
-  static constexpr int S = bytes(S0) <= 220 * 1024 ? S0 : (bytes(S0 / 2) <= 220 * 1024 ? S0 / 2 : S0 / 4);
-  static constexpr int THREADS = S * FFT<cplx<T>, NZ, false>::T;
 };
 
 // odd components along x, y, z: xy (1), xz (2) | xy (1), yz (4) | xz (2), yz (4)
@@ -242,10 +252,15 @@ __device__ __forceinline__ bool odd_x(int q) { return q == 1 || q == 2; }
 __device__ __forceinline__ bool odd_y(int q) { return q == 1 || q == 4; }
 __device__ __forceinline__ bool odd_z(int q) { return q == 2 || q == 4; }
 
+// Thread group c (of three) transforms component c of the S columns.  After
+// the forward transforms the three spectra meet in shared memory; group c
+// forms row c of the symmetric product and runs its inverse transform from
+// the registers (the inverse radix order starts where the forward ended).
 template <typename T, int NZ>
 __global__ void __launch_bounds__(ZS<T, NZ>::THREADS)
 k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN, int oct, Dims d,
        const cplx<T>* __restrict__ tw) {
+  if (rhs_skipped(d, blockIdx.z)) return;
   using V = cplx<T>;
   using FF = FFT<V, NZ, false>;
   using FI = FFT<V, NZ, true>;
@@ -255,31 +270,34 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   static_assert(FI::R0 == RL, "inverse must start where the forward transform ended");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw_s = reinterpret_cast<V*>(smem_raw);
-  V* buf = tw_s + NZ;  // 3 exchange buffers of NZ x ES
+  V* buf = tw_s + NZ;  // 3 buffers of NZ x ES
   const int kx0 = blockIdx.x * S;
   const int ky = blockIdx.y;
   const long long plane = (long long)d.Lp * d.Mp;  // one z-plane of B
   const long long comp = plane * d.N;               // one component of B
-  V* Bp = B + blockIdx.z * b_rhs + (long long)ky * d.Lp + kx0;
+  const int c = threadIdx.x / (S * FF::T);
+  const int rem = threadIdx.x - c * S * FF::T;
+  const int s = rem % S, t = rem / S;
+  V* Bp = B + blockIdx.z * b_rhs + c * comp + (long long)ky * d.Lp + kx0;
   stage_twiddles(tw_s, tw, NZ);
-  const int s = threadIdx.x % S, t = threadIdx.x / S;
   const int kx = kx0 + s;
   const bool active = kx < d.Lp;
-  V reg[3][E];
+  V reg[E];
 #pragma unroll
-  for (int c = 0; c < 3; ++c)
+  for (int b = 0; b < E / R0; ++b)
 #pragma unroll
-    for (int b = 0; b < E / R0; ++b)
-#pragma unroll
-      for (int r = 0; r < R0; ++r) {
-        const int p = FF::in_pos(t, b, r);
-        reg[c][b * R0 + r] = (active && r < R0 / 2 && p < d.N) ? Bp[c * comp + p * plane + s] : mk<V>(0, 0);
-      }
+    for (int r = 0; r < R0; ++r) {
+      const int p = FF::in_pos(t, b, r);
+      reg[b * R0 + r] = (active && r < R0 / 2 && p < d.N) ? Bp[p * plane + s] : mk<V>(0, 0);
+    }
   __syncthreads();  // twiddles staged
-#pragma unroll
-  for (int c = 0; c < 3; ++c) FF::run_half(reg[c], buf + c * NZ * ES + s, ES, t, tw_s);
+  V* my = buf + c * NZ * ES + s;
+  FF::run_half(reg, my, ES, t, tw_s);
+  __syncthreads();
+  FF::store(reg, my, ES, t);
+  __syncthreads();
 
-  // symmetric tensor multiply on the registers
+  // row c of the symmetric product at this thread's positions
   int ox = kx, oy = ky;
   bool fx = false, fy = false;
   if (oct) {
@@ -290,6 +308,13 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   const long long fplane = oct ? (long long)(d.L + 1) * (d.M + 1) : plane;
   const long long frow = oct ? (long long)(d.L + 1) : d.Lp;
   const V* fp = fN + (long long)oy * frow + ox;
+  // components of row c: c=0 (xx,xy,xz), c=1 (xy,yy,yz), c=2 (xz,yz,zz)
+  const int q0 = c == 0 ? 0 : (c == 1 ? 1 : 2);
+  const int q1 = c == 0 ? 1 : (c == 1 ? 3 : 4);
+  const int q2 = c == 0 ? 2 : (c == 1 ? 4 : 5);
+  const V* b0 = buf + s;
+  const V* b1 = buf + NZ * ES + s;
+  const V* b2 = buf + 2 * NZ * ES + s;
 #pragma unroll
   for (int b = 0; b < E / RL; ++b)
 #pragma unroll
@@ -298,35 +323,26 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
       int oz = kz;
       bool fz = false;
       if (oct && kz > d.N) { oz = d.Np - kz; fz = true; }
-      V n6[6];
+      V y = mk<V>(0, 0);
       if (active) {
-#pragma unroll
-        for (int q = 0; q < 6; ++q) {
-          V v = fp[q * fq + oz * fplane];
-          const bool neg = (fx && odd_x(q)) ^ (fy && odd_y(q)) ^ (fz && odd_z(q));
-          n6[q] = neg ? mk<V>(-v.x, -v.y) : v;
-        }
-      } else {
-#pragma unroll
-        for (int q = 0; q < 6; ++q) n6[q] = mk<V>(0, 0);
+        const long long o = (long long)oz * fplane;
+        V n0 = fp[q0 * fq + o], n1 = fp[q1 * fq + o], n2 = fp[q2 * fq + o];
+        if ((fx && odd_x(q0)) ^ (fy && odd_y(q0)) ^ (fz && odd_z(q0))) n0 = mk<V>(-n0.x, -n0.y);
+        if ((fx && odd_x(q1)) ^ (fy && odd_y(q1)) ^ (fz && odd_z(q1))) n1 = mk<V>(-n1.x, -n1.y);
+        if ((fx && odd_x(q2)) ^ (fy && odd_y(q2)) ^ (fz && odd_z(q2))) n2 = mk<V>(-n2.x, -n2.y);
+        const int e = kz * ES;
+        y = cadd(cadd(cmul(n0, b0[e]), cmul(n1, b1[e])), cmul(n2, b2[e]));
       }
-      const int i = b * RL + r;
-      const V jx = reg[0][i], jy = reg[1][i], jz = reg[2][i];
-      reg[0][i] = cadd(cadd(cmul(n6[0], jx), cmul(n6[1], jy)), cmul(n6[2], jz));
-      reg[1][i] = cadd(cadd(cmul(n6[1], jx), cmul(n6[3], jy)), cmul(n6[4], jz));
-      reg[2][i] = cadd(cadd(cmul(n6[2], jx), cmul(n6[4], jy)), cmul(n6[5], jz));
+      reg[b * RL + r] = y;
     }
+  FI::run(reg, my, ES, t, tw_s);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) FI::run(reg[c], buf + c * NZ * ES + s, ES, t, tw_s);
+  for (int b = 0; b < E / RLI; ++b)
 #pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int b = 0; b < E / RLI; ++b)
-#pragma unroll
-      for (int r = 0; r < RLI; ++r) {
-        const int z = FI::out_pos(t, b, r);
-        if (active && z < d.N) Bp[c * comp + z * plane + s] = reg[c][b * RLI + r];
-      }
+    for (int r = 0; r < RLI; ++r) {
+      const int z = FI::out_pos(t, b, r);
+      if (active && z < d.N) Bp[z * plane + s] = reg[b * RLI + r];
+    }
 }
 
 }  // namespace marie

@@ -15,9 +15,15 @@ inline bool fft_length_supported(int n) {
   return false;
 }
 
+// Raises the kernel's dynamic shared-memory limit once per kernel and device
+// (never again afterwards, so launches inside a stream capture stay pure).
+bool smem_opted_in(const void* kernel, size_t bytes);
+void smem_mark_opted_in(const void* kernel, size_t bytes);
 template <typename K> inline cudaError_t opt_in_smem(K kernel, size_t bytes) {
-  if (bytes <= 48 * 1024) return cudaSuccess;
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (bytes <= 48 * 1024 || smem_opted_in((const void*)kernel, bytes)) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) smem_mark_opted_in((const void*)kernel, bytes);
+  return e;
 }
 
 template <typename T> struct MatvecLaunch {
@@ -28,9 +34,16 @@ template <typename T> struct MatvecLaunch {
                           double2* out, long long os, const Dims& d, const V* tw, int nrhs, cudaStream_t st);
   static cudaError_t cols(bool inv, int NC, const V* in, long long in_w, long long in_rhs, int n_in, V* out,
                           long long out_w, long long out_rhs, int n_out, int Lp, int nw, const V* tw, int nrhs,
-                          cudaStream_t st);
+                          cudaStream_t st, const int* stop = nullptr, int step = 0);
   static cudaError_t zmul(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
                           cudaStream_t st);
+  // fused x+y passes (thread-block clusters); fused() says whether this grid has them
+  static bool fused(const Dims& d);
+  static cudaError_t xyfwd(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
+                           const Dims& d, const V* twx, const V* twy, int nrhs, cudaStream_t st);
+  static cudaError_t yxinv(const V* B, long long bs, const double2* J, long long js, const int* inv, Epilogue ep,
+                           double2* out, long long os, const Dims& d, const V* twx, const V* twy, int nrhs,
+                           cudaStream_t st);
 };
 
 }  // namespace marie

@@ -18,6 +18,7 @@ struct marie_plan {
   double2* fN64 = nullptr;
   float2* fN32 = nullptr;
   bool has_op = false;
+  bool fuse = true;  // fused x+y / y+x passes when the grid has them
   int oct = 0;  // 1: fN64/fN32 hold the (L+1)(M+1)(N+1) octant, 0: the full array
 
   // Twiddle tables exp(-2*pi*i*k/n) for the three padded axis lengths.
@@ -66,7 +67,7 @@ int stage_in(const void* user, size_t bytes, cudaStream_t st, DBuf& tmp, const v
 int stage_out(void* user, size_t bytes, cudaStream_t st, DBuf& tmp, void** dev);
 int finish_out(void* user, const void* dev, size_t bytes, cudaStream_t st);
 
-int ensure_workspace(marie_plan* p, int prec, long long nrhs);
+int ensure_workspace(marie_plan* p, int prec, long long nrhs, bool with_A = true);
 int ensure_pinned(marie_plan* p, size_t n_doubles);
 
 // Build the inverse map inv[g] = k for 1-based idx[k]; -1 elsewhere.  Fails on
@@ -76,6 +77,10 @@ int build_inverse_index(marie_plan* p, const int64_t* idx_dev, long long n, int*
 // One circulant matvec (nrhs columns of length n, device pointers).
 int run_matvec(marie_plan* p, int prec, const double2* J, double2* out, long long n, int nrhs, const int* inv,
                const Prologue& pro, const Epilogue& ep);
+// Same with column strides js / os and the batched-solve skip mask: column r
+// is left untouched when stop[r] < step.
+int run_matvec(marie_plan* p, int prec, const double2* J, long long js, double2* out, long long os, long long n,
+               int nrhs, const int* inv, const Prologue& pro, const Epilogue& ep, const int* stop, int step);
 
 // Scale fN by 1/(8LMN) into the plan's FP64/FP32 copies (fN_dev: full layout).
 int install_operator(marie_plan* p, const double2* fN_dev);
@@ -97,6 +102,22 @@ struct GmresResult {
   int iter[2] = {0, 0};
   std::vector<double> resvec;
 };
+
+// A batched linear operator: out_s = Op(in_s) for the systems s whose stop[s]
+// is not below step (in_s = in + s*is, out_s = out + s*os).
+struct BatchOp {
+  std::function<int(const double2* in, long long is, double2* out, long long os, int S, const int* stop, int step)>
+      apply;
+};
+
+// pgmres semantics for S systems sharing one operator, device-driven (one
+// graph launch per restart cycle when use_graph).  x0 = 0.  active_in (may be
+// null) selects the systems to solve (others return x = 0); true_residual
+// adds the final ||b - A x|| / ||b|| (pgmres.m:175).
+int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const double2* B,
+                long long bs, long long n, int S, int restart, double tol, int maxit, double2* X, long long xs,
+                std::vector<GmresResult>& out, bool use_graph, const std::vector<int>* active_in,
+                bool true_residual);
 
 // pgmres semantics (pgmres.m:70-181) on device vectors.
 int gmres(marie_plan* p, const DevOp& A, const DevOp* L1, const DevOp* L2, const DevOp* R1, const DevOp* R2,

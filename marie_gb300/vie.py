@@ -401,6 +401,40 @@ def JVIE_Solver(Einc, e_r, r, freq, fN, tol=None, form=None, solver="G", precond
             opr.close()
 
 
+def JVIE_Solver_batch(Einc, e_r, r, freq, fN, tol=None, form=None, precond=None, inner_it=None, outer_it=None):
+    """JVIE_Solver for several excitations of one body solved together.
+
+    Einc: (L, M, N, 3, nexc) column-major.  The excitations advance in lockstep
+    (one batched matvec per GMRES step, one graph launch per restart cycle).
+    Returns (Je (L, M, N, 3, nexc), flag[nexc], relres[nexc], iter[nexc, 2], solvert)."""
+    tol = 1e-3 if tol is None else tol
+    form = 2 if form is None else form
+    pc = {None: b"\0", 0: b"\0", "L": b"L", "R": b"R"}.get(precond, b"\0")
+    inner_it = 50 if inner_it is None or inner_it < 1 else inner_it
+    outer_it = 200 if outer_it is None or outer_it < 1 else outer_it
+    opr, tmp = (fN, False) if isinstance(fN, Operator) else (Operator.from_array(fN), True)
+    try:
+        L, M, N = e_r.shape
+        nexc = Einc.shape[4]
+        dx = float(r[1, 0, 0, 0] - r[0, 0, 0, 0]) if not _is_cuda(r) else float((r[1, 0, 0, 0] - r[0, 0, 0, 0]).item())
+        cuda = _is_cuda(Einc)
+        ep, ek = _in(Einc)
+        erp, erk = _in(e_r)
+        jp, Je = _out((L, M, N, 3, nexc), cuda)
+        flag = np.zeros(nexc, np.int32)
+        relres = np.zeros(nexc)
+        it = np.zeros(2 * nexc, np.int32)
+        solvert = C.c_double()
+        check(opr.lib.marie_jvie_solve_batch(opr.plan, ep, nexc, erp, dx, float(freq), int(form), pc, float(tol),
+                                             int(inner_it), int(outer_it), jp,
+                                             flag.ctypes.data_as(_lib._ip), relres.ctypes.data_as(_lib._dp),
+                                             it.ctypes.data_as(_lib._ip), C.byref(solvert)))
+        return Je, flag, relres, it.reshape(nexc, 2), solvert.value
+    finally:
+        if tmp:
+            opr.close()
+
+
 # ---------------------------------------------------------------------------
 # excitations
 # ---------------------------------------------------------------------------

@@ -142,3 +142,32 @@ def test_deterministic_fp64():
     a = mg.mv_AN(J, op, Mr, Mc, 0.3, "notransp", idx)
     b = mg.mv_AN(J, op, Mr, Mc, 0.3, "notransp", idx)
     np.testing.assert_array_equal(a, b)
+
+
+FUSED = [(32, 32, 4), (48, 48, 4), (64, 64, 8), (96, 96, 4), (128, 128, 4), (256, 192, 4)]
+
+
+@pytest.mark.parametrize("shape", FUSED)
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_fused_xy_passes_match_oracle(shape, precision):
+    """Grids with the cluster-fused x+y passes, both flags."""
+    import marie_gb300 as mg
+
+    fN, Mr, Mc, idx, J = problem(*shape, seed=3, physical=True)
+    op = mg.Operator.from_array(fN, precision="mixed")
+    for flag in ("notransp", "transp"):
+        ref = vo.mv_AN(J, fN, Mr, Mc, 1e-7, flag, idx)
+        out = mg.mv_AN(J, op, Mr, Mc, 1e-7, flag, idx, precision=precision)
+        assert relerr(out, ref) < TOL[precision], flag
+
+
+def test_fused_and_five_pass_paths_agree(monkeypatch):
+    import marie_gb300 as mg
+
+    fN, Mr, Mc, idx, J = problem(64, 64, 8, seed=4, physical=True)
+    op_f = mg.Operator.from_array(fN)
+    monkeypatch.setenv("MARIE_NO_FUSED", "1")
+    op_u = mg.Operator.from_array(fN)
+    a = mg.mv_AN(J, op_f, Mr, Mc, 1e-7, "notransp", idx)
+    b = mg.mv_AN(J, op_u, Mr, Mc, 1e-7, "notransp", idx)
+    assert relerr(a, b) < 1e-13

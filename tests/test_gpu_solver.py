@@ -81,6 +81,36 @@ def test_jvie_solver_matches_oracle(form, precond):
     assert np.max(np.abs(out[0] - ref[0])) < 1e-8 * np.max(np.abs(ref[0]))
 
 
+@pytest.mark.parametrize("precision,precond", [("fp64", 0), ("fp64", "R"), ("mixed", 0)])
+def test_batched_excitations_match_single_solves(precision, precond):
+    """Several excitations of one body in one lockstep batch give the same
+    fields and iteration counts as one-at-a-time solves (c3 structure)."""
+    import marie_gb300 as mg
+
+    L, dx = 8, 5e-3
+    r, er, E1 = sphere_problem(L, dx, 0.018)
+    em = vo.EMconstants(FREQ)
+    E2, _ = vo.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [0, 1, 0])
+    E3 = vo.Dipole_Excitation(r, em["ko"], np.array([[0, 0, 1.0]]), np.array([[0.05, 0.0, 0.01]]))
+    Eb = np.asfortranarray(np.stack([E1, E2, E3], axis=4))
+    op = mg.Operator.assemble(L, L, L, dx, FREQ, precision=precision, nrhs_max=3)
+    Jb, flags, relres, iters, _ = mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, tol=1e-8, precond=precond,
+                                                      inner_it=15)
+    for e in range(3):
+        Js, fs, rs, its, _, _ = mg.JVIE_Solver(np.asfortranarray(Eb[..., e]), er, r, FREQ, op, tol=1e-8,
+                                               precond=precond, inner_it=15)
+        assert flags[e] == fs == 0
+        assert list(iters[e]) == list(its)
+        assert np.max(np.abs(Jb[..., e] - Js)) <= 1e-9 * np.max(np.abs(Js))
+    if precision == "fp64":
+        fN = op.to_array()
+        for e in range(3):
+            ref = vo.JVIE_Solver(np.asfortranarray(Eb[..., e]), er, r, FREQ, fN, tol=1e-8, precond=precond,
+                                 inner_it=15)
+            assert ref[3] == list(iters[e])
+            assert np.max(np.abs(Jb[..., e] - ref[0])) < 1e-7 * np.max(np.abs(ref[0]))
+
+
 def test_mixed_precision_solve_matches_fp64():
     import marie_gb300 as mg
 
