@@ -133,6 +133,18 @@ int marie_jvie_solve(marie_plan* plan, const double* Einc, const double* e_r, do
  * (one batched matvec per GMRES step, one graph launch per restart cycle).
  * Per excitation: flag[e], relres[e], iter[2e..2e+1].  The reference solves
  * excitations one at a time (JVIE_Solver.m is called per port/excitation). */
+/* Adjoint gradient of a body-field objective with respect to the per-voxel
+ * eps_r and sigma (no counterpart in the reference, which has no derivatives;
+ * it reuses the J-VIE operator: K^T of the E-field system is the reference's
+ * form-1 operator).  objective 0: F = sum 0.5 sigma |E|^2 (absorbed power);
+ * 1: F = sum |E - E_target|^2 (E_target: L x M x N x 3).  Sums over the
+ * non-air voxels.  Outputs F, dF_deps and dF_dsigma (L x M x N, zero in air),
+ * flags {forward, adjoint} and iteration counts {forward, adjoint}. */
+int marie_jvie_adjoint_grad(marie_plan* plan, const double* Einc, const double* e_r, double dx,
+                            double freq, int objective, const double* E_target, double tol,
+                            int inner_it, int outer_it, double* F, double* dF_deps,
+                            double* dF_dsigma, int* flags, int* iters);
+
 int marie_jvie_solve_batch(marie_plan* plan, const double* Einc, int64_t nexc, const double* e_r,
                            double dx, double freq, int form, char precond, double tol, int inner_it,
                            int outer_it, double* Je, int* flag, double* relres, int* iter,

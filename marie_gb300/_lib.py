@@ -53,6 +53,8 @@ SIGNATURES = {
                                _vp, _vp, _ip, _dp, _ip, _dp, C.c_int64, _i64p]),
     "marie_jvie_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_int, C.c_char, C.c_double,
                                    C.c_int, C.c_int, _vp, _ip, _dp, _ip, _dp, C.c_int64, _i64p, _dp]),
+    "marie_jvie_adjoint_grad": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_int, _vp, C.c_double, C.c_int,
+                                          C.c_int, _dp, _vp, _vp, _ip, _ip]),
     "marie_jvie_solve_batch": (C.c_int, [_vp, _vp, C.c_int64, _vp, C.c_double, C.c_double, C.c_int, C.c_char,
                                          C.c_double, C.c_int, C.c_int, _vp, _ip, _dp, _ip, _dp]),
     "marie_e_field_nop": (C.c_int, [_vp, _vp, C.c_double, C.c_double, _vp, _vp, C.c_int]),

@@ -254,6 +254,9 @@ struct SolveOut {
   std::vector<GmresResult> r;
 };
 
+static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, int S_exc, double2* X, char precond,
+                         double tol, int inner_it, int outer_it, SolveOut& out);
+
 // Solves the S excitations E (3V x S, column stride es) of one body.
 static int jvie_solve_core(marie_plan* p, const double2* E, long long es, int S_exc, const double2* er, double dx,
                            double freq, int form, char precond, double tol, int inner_it, int outer_it, double2* Je,
@@ -272,15 +275,26 @@ static int jvie_solve_core(marie_plan* p, const double2* E, long long es, int S_
     return MARIE_OK;
   }
   const long long n = S.n;
-  if (p->nrhs_max < S_exc) {
-    // workspaces for the batch are sized by nrhs_max; batches above it run in chunks
-  }
   DBuf rhs, x;
   MARIE_TRY(rhs.alloc((size_t)S_exc * n * sizeof(double2), st));
   MARIE_TRY(x.alloc((size_t)S_exc * n * sizeof(double2), st));
   k_jvie_rhs<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(S.f.as<double2>(), S.idx3.as<int64_t>(), n, E, es,
                                                       rhs.as<double2>());
   count_launch();
+  MARIE_TRY(solve_systems(p, S, rhs.as<double2>(), S_exc, x.as<double2>(), precond, tol, inner_it, outer_it, out));
+  k_scatter_dofs<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(x.as<double2>(), S.idx3.as<int64_t>(), n, Je, js);
+  count_launch();
+  MARIE_CUDA_TRY(cudaGetLastError());
+  return MARIE_OK;
+}
+
+// Solves A2 x_e = B_e (form-2 J-VIE operator of the state S) for S_exc
+// right-hand sides: FP64 pgmres, or GMRES-IR on a MARIE_MIXED plan.
+static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, int S_exc, double2* X, char precond,
+                         double tol, int inner_it, int outer_it, SolveOut& out) {
+  cudaStream_t st = p->stream;
+  const long long n = S.n;
+  out.r.assign(S_exc, GmresResult());
   bool pb_nz = true;
   MARIE_TRY(any_nonzero(p, S.pb.as<double2>(), n, &pb_nz));
   const int prec_main = (p->precision == MARIE_FP32) ? MARIE_FP32 : MARIE_FP64;
@@ -288,8 +302,6 @@ static int jvie_solve_core(marie_plan* p, const double2* E, long long es, int S_
   BatchOp P64 = make_bop(p, prec_main, S, S.pa.as<double2>(), S.pb.as<double2>(), !pb_nz);
   const BatchOp* L1 = precond == 'L' ? &P64 : nullptr;
   const BatchOp* R1 = precond == 'R' ? &P64 : nullptr;
-  double2* X = x.as<double2>();
-  const double2* Bv = rhs.as<double2>();
   if (p->precision != MARIE_MIXED) {
     MARIE_TRY(gmres_batch(p, A64, L1, R1, Bv, n, n, S_exc, inner_it, tol, outer_it, X, n, out.r, true, nullptr,
                           true));
@@ -355,9 +367,77 @@ static int jvie_solve_core(marie_plan* p, const double2* E, long long es, int S_
       out.r[e].iter[1] = inner_total[e];
     }
   }
-  k_scatter_dofs<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(X, S.idx3.as<int64_t>(), n, Je, js);
+  return MARIE_OK;
+}
+
+// adjoint-gradient kernels (adjoint.cu)
+__global__ void k_adj_fields(const double2* __restrict__ J, const int64_t* __restrict__ idx3, long long n,
+                             long long V, const double2* __restrict__ er, double omega_eps0, int objective,
+                             const double2* __restrict__ Et, double2* __restrict__ E, double2* __restrict__ w,
+                             double* __restrict__ Fpart);
+__global__ void k_adj_grad(const double2* __restrict__ q, const double2* __restrict__ E, const int* __restrict__ idxS,
+                           long long nS, const double2* __restrict__ er, double omega_eps0, int objective,
+                           double* __restrict__ g_eps, double* __restrict__ g_sig);
+
+// Forward solve, objective, adjoint solve with the same J-VIE operator, and
+// the fused gradient (derivation in adjoint.cu).  g_eps, g_sig: L x M x N.
+int jvie_adjoint_core(marie_plan* p, const double2* Einc, const double2* er, double dx, double freq, int objective,
+                      const double2* Et, double tol, int inner_it, int outer_it, double* F, double* g_eps,
+                      double* g_sig, int* flags, int* iters) {
+  cudaStream_t st = p->stream;
+  const long long V = p->d.V;
+  JvieState S;
+  MARIE_TRY(jvie_setup(p, er, dx, freq, 2, S));
+  MARIE_CUDA_TRY(cudaMemsetAsync(g_eps, 0, V * sizeof(double), st));
+  MARIE_CUDA_TRY(cudaMemsetAsync(g_sig, 0, V * sizeof(double), st));
+  *F = 0;
+  if (S.n == 0) return MARIE_OK;
+  const long long n = S.n;
+  const double omega_eps0 = 2.0 * M_PI * freq * eps0();
+  DBuf rhs, J, E, w, lam, q, Fp;
+  MARIE_TRY(rhs.alloc(n * sizeof(double2), st));
+  MARIE_TRY(J.alloc(n * sizeof(double2), st));
+  MARIE_TRY(E.alloc(n * sizeof(double2), st));
+  MARIE_TRY(w.alloc(n * sizeof(double2), st));
+  MARIE_TRY(lam.alloc(n * sizeof(double2), st));
+  MARIE_TRY(q.alloc(n * sizeof(double2), st));
+  const int nb = grid_n(n);
+  MARIE_TRY(Fp.alloc(nb * sizeof(double), st));
+  k_jvie_rhs<<<dim3(nb, 1), 256, 0, st>>>(S.f.as<double2>(), S.idx3.as<int64_t>(), n, Einc, 0, rhs.as<double2>());
+  count_launch();
+  SolveOut fwd, adj;
+  MARIE_TRY(solve_systems(p, S, rhs.as<double2>(), 1, J.as<double2>(), 0, tol, inner_it, outer_it, fwd));
+  k_adj_fields<<<nb, 256, 0, st>>>(J.as<double2>(), S.idx3.as<int64_t>(), n, V, er, omega_eps0, objective, Et,
+                                   E.as<double2>(), w.as<double2>(), Fp.as<double>());
   count_launch();
   MARIE_CUDA_TRY(cudaGetLastError());
+  std::vector<double> hF(nb);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hF.data(), Fp.p, nb * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+  double Fs = 0;
+  for (double v : hF) Fs += v;
+  *F = Fs;
+  // adjoint solve A lambda = w (rows divided by eps_c, like the forward form 2)
+  MARIE_TRY(solve_systems(p, S, w.as<double2>(), 1, lam.as<double2>(), 0, tol, inner_it, outer_it, adj));
+  // q = (Gram - N) lambda in FP64
+  Prologue pro{nullptr, 0};
+  Epilogue ep{};
+  ep.a_s = mk<double2>(dx * dx * dx, 0.0);
+  ep.b_s = mk<double2>(1.0, 0.0);
+  const int prec = p->fN64 ? MARIE_FP64 : MARIE_FP32;
+  MARIE_TRY(run_matvec(p, prec, lam.as<double2>(), q.as<double2>(), n, 1, S.inv.as<int>(), pro, ep));
+  k_adj_grad<<<grid_n(S.nS), 256, 0, st>>>(q.as<double2>(), E.as<double2>(), S.idxS.as<int>(), S.nS, er, omega_eps0,
+                                           objective, g_eps, g_sig);
+  count_launch();
+  MARIE_CUDA_TRY(cudaGetLastError());
+  if (flags) {
+    flags[0] = fwd.r[0].flag;
+    flags[1] = adj.r[0].flag;
+  }
+  if (iters) {
+    iters[0] = (int)fwd.r[0].resvec.size() - 1;
+    iters[1] = (int)adj.r[0].resvec.size() - 1;
+  }
   return MARIE_OK;
 }
 

@@ -244,7 +244,12 @@ template <typename T, int NZ> struct ZS {
   static constexpr int S0 = sizeof(T) == 4 ? 8 : 4;        // columns per CTA
   static constexpr int S = (3 * S0 * TT <= 1024) ? S0 : ((3 * (S0 / 2) * TT <= 1024) ? S0 / 2 : S0 / 4);
   static constexpr int THREADS = 3 * S * TT;               // one thread group per component
-  static constexpr long long bytes(int s) { return (long long)(NZ + 3 * NZ * (s + 1)) * sizeof(cplx<T>); }
+  // rows of 64 B use the half-line swizzle, others one pad element per row
+  static constexpr bool HALF = S * (int)sizeof(cplx<T>) == 64;
+  static constexpr int ES = HALF ? S : S + 1;
+  static constexpr int BUF = NZ * ES + (HALF ? S : 0);     // one component's exchange buffer
+  static constexpr long long bytes(int) { return (long long)(NZ + 3 * BUF) * sizeof(cplx<T>); }
+  __device__ static SAddr addr() { return SAddr(ES, false, HALF ? S : 0); }
 };
 
 // odd components along x, y, z: xy (1), xz (2) | xy (1), yz (4) | xz (2), yz (4)
@@ -265,12 +270,13 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   using FF = FFT<V, NZ, false>;
   using FI = FFT<V, NZ, true>;
   constexpr int S = ZS<T, NZ>::S;
-  constexpr int ES = S + 1;
+  constexpr int BUF = ZS<T, NZ>::BUF;
+  const SAddr ad = ZS<T, NZ>::addr();
   constexpr int E = FF::E, R0 = FF::R0, RL = FF::RL, RLI = FI::RL;
   static_assert(FI::R0 == RL, "inverse must start where the forward transform ended");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw_s = reinterpret_cast<V*>(smem_raw);
-  V* buf = tw_s + NZ;  // 3 buffers of NZ x ES
+  V* buf = tw_s + NZ;  // 3 exchange buffers of BUF elements
   const int kx0 = blockIdx.x * S;
   const int ky = blockIdx.y;
   const long long plane = (long long)d.Lp * d.Mp;  // one z-plane of B
@@ -291,10 +297,10 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
       reg[b * R0 + r] = (active && r < R0 / 2 && p < d.N) ? Bp[p * plane + s] : mk<V>(0, 0);
     }
   __syncthreads();  // twiddles staged
-  V* my = buf + c * NZ * ES + s;
-  FF::run_half(reg, my, ES, t, tw_s);
+  V* my = buf + c * BUF + s;
+  FF::run_half(reg, my, ad, t, tw_s);
   __syncthreads();
-  FF::store(reg, my, ES, t);
+  FF::store(reg, my, ad, t);
   __syncthreads();
 
   // row c of the symmetric product at this thread's positions
@@ -313,8 +319,8 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   const int q1 = c == 0 ? 1 : (c == 1 ? 3 : 4);
   const int q2 = c == 0 ? 2 : (c == 1 ? 4 : 5);
   const V* b0 = buf + s;
-  const V* b1 = buf + NZ * ES + s;
-  const V* b2 = buf + 2 * NZ * ES + s;
+  const V* b1 = buf + BUF + s;
+  const V* b2 = buf + 2 * BUF + s;
 #pragma unroll
   for (int b = 0; b < E / RL; ++b)
 #pragma unroll
@@ -330,12 +336,12 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
         if ((fx && odd_x(q0)) ^ (fy && odd_y(q0)) ^ (fz && odd_z(q0))) n0 = mk<V>(-n0.x, -n0.y);
         if ((fx && odd_x(q1)) ^ (fy && odd_y(q1)) ^ (fz && odd_z(q1))) n1 = mk<V>(-n1.x, -n1.y);
         if ((fx && odd_x(q2)) ^ (fy && odd_y(q2)) ^ (fz && odd_z(q2))) n2 = mk<V>(-n2.x, -n2.y);
-        const int e = kz * ES;
+        const int e = ad(kz);
         y = cadd(cadd(cmul(n0, b0[e]), cmul(n1, b1[e])), cmul(n2, b2[e]));
       }
       reg[b * RL + r] = y;
     }
-  FI::run(reg, my, ES, t, tw_s);
+  FI::run(reg, my, ad, t, tw_s);
 #pragma unroll
   for (int b = 0; b < E / RLI; ++b)
 #pragma unroll

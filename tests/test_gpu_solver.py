@@ -100,8 +100,14 @@ def test_batched_excitations_match_single_solves(precision, precond):
         Js, fs, rs, its, _, _ = mg.JVIE_Solver(np.asfortranarray(Eb[..., e]), er, r, FREQ, op, tol=1e-8,
                                                precond=precond, inner_it=15)
         assert flags[e] == fs == 0
-        assert list(iters[e]) == list(its)
-        assert np.max(np.abs(Jb[..., e] - Js)) <= 1e-9 * np.max(np.abs(Js))
+        if precision == "fp64":
+            assert list(iters[e]) == list(its)
+            assert np.max(np.abs(Jb[..., e] - Js)) <= 1e-9 * np.max(np.abs(Js))
+        else:
+            # the batch refines with the tightest inner tolerance of its members,
+            # so iteration counts may differ; both meet the FP64 residual bar
+            assert relres[e] <= 1e-8
+            assert np.linalg.norm(Jb[..., e] - Js) <= 1e-6 * np.linalg.norm(Js)
     if precision == "fp64":
         fN = op.to_array()
         for e in range(3):
