@@ -393,6 +393,100 @@ def run_reference(args, world, rank):
             "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ---------------------------------------------------------------------------
+# the other workloads (reported beside the headline; not the default line)
+# ---------------------------------------------------------------------------
+def _timed(fn, steps, warmup):
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = None
+    for _ in range(steps):
+        out = fn()
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / steps, out
+
+
+def run_extra(args):
+    """c1: Mie sphere; c3: 16 dipoles on one 128^3 body + 3 uneven bodies;
+    c4: 64^3 adjoint gradient; c5: 256x192x160, 8 dipoles + gradient."""
+    import marie_gb300 as mg
+    from marie_gb300 import phantoms
+    from marie_gb300.autograd import adjoint_gradient
+
+    em = mg.EMconstants(FREQ)
+    res = {"config": args.config}
+    if args.config == "c1":
+        from oracle import mie
+
+        Lc, dx, R = 32, 5e-3, 0.075
+        r, er = phantoms.sphere(Lc, Lc, Lc, dx, R, 50.0, 0.5, FREQ)
+        E, _ = mg.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
+        for prec in ("fp64", "mixed"):
+            op = mg.Operator.assemble(Lc, Lc, Lc, dx, FREQ, precision=prec)
+            t, out = _timed(lambda: mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-6), args.steps, args.warmup)
+            res[prec] = {"seconds": t, "iter": out[3], "relres": out[2], "matvecs": len(out[4]) - 1}
+            if prec == "fp64":
+                Et = mg.E_field_Nop(out[0], op, dx**3, FREQ, E)
+                rad = np.sqrt(np.sum(r * r, axis=3))
+                core = rad < R - 0.01
+                Em = mie.MIE_SERIES(r[core][:, None, None, :], R, 50.0, 0.5, FREQ)[:, 0, 0, :]
+                res["mie_rel_l2_error_core"] = float(np.linalg.norm(Et[core] - Em) / np.linalg.norm(Em))
+    elif args.config == "c3":
+        r, er = make_problem(0)
+        pos = phantoms.dipole_ring(0.15, [-0.05, 0.0, 0.05, 0.10], 4)
+        Es = [mg.Dipole_Excitation(r, em["ko"], np.array([[0, 0, 1.0]]), p[None]) for p in pos]
+        Eb = np.asfortranarray(np.stack(Es, axis=4))
+        del Es
+        op = mg.Operator.assemble(L, M, N, DX, FREQ, precision="mixed", nrhs_max=16)
+        t, out = _timed(lambda: mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, tol=TOL), args.steps, args.warmup)
+        res["batch16"] = {"seconds": t, "excitation_solves_per_s": 16 / t, "flags": out[1].tolist(),
+                          "max_relres": float(out[2].max()), "iters": out[3].tolist()}
+        del Eb, op
+        bodies = []
+        for seed, Lb in ((1, 48), (2, 64), (3, 96)):
+            rb, erb, _ = phantoms.ellipsoids(Lb, Lb, Lb, DX, N_ELL, seed, FREQ)
+            pb = phantoms.dipole_ring(0.15, [0.0], 4)
+            Eb = np.asfortranarray(np.stack([mg.Dipole_Excitation(rb, em["ko"], np.array([[0, 0, 1.0]]), p[None])
+                                             for p in pb], axis=4))
+            bodies.append((Eb, erb, rb, mg.Operator.assemble(Lb, Lb, Lb, DX, FREQ, precision="mixed", nrhs_max=4)))
+        t, out = _timed(lambda: mg.JVIE_Solver_bodies(bodies, FREQ, tol=TOL), args.steps, args.warmup)
+        res["bodies_48_64_96x4"] = {"seconds": t, "excitation_solves_per_s": 12 / t,
+                                    "flags": [o[1].tolist() for o in out[0]]}
+    elif args.config == "c4":
+        Lc, dx = 64, 3e-3
+        r, er, _ = phantoms.ellipsoids(Lc, Lc, Lc, dx, N_ELL, 0, FREQ)
+        E, _ = mg.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
+        for prec in ("fp64", "mixed"):
+            op = mg.Operator.assemble(Lc, Lc, Lc, dx, FREQ, precision=prec)
+            t, out = _timed(lambda: adjoint_gradient(op, E, er, dx, FREQ, "power", None, TOL), args.steps,
+                            args.warmup)
+            res[prec] = {"seconds_per_gradient": t, "F": out[0], "flags": out[3], "iters": out[4]}
+            res[prec + "_grad"] = out[1:3]
+        g64, gm = res.pop("fp64_grad"), res.pop("mixed_grad")
+        res["grad_rel_diff_mixed_vs_fp64"] = [float(np.linalg.norm(a - b) / np.linalg.norm(a)) for a, b in
+                                              zip(g64, gm)]
+    elif args.config == "c5":
+        Lc, Mc, Nc = 256, 192, 160
+        r, er, _ = phantoms.ellipsoids(Lc, Mc, Nc, DX, 40, 0, FREQ)
+        pos = phantoms.dipole_ring(0.2, [-0.05, 0.05], 4)
+        Es = [mg.Dipole_Excitation(r, em["ko"], np.array([[0, 0, 1.0]]), p[None]) for p in pos]
+        Eb = np.asfortranarray(np.stack(Es, axis=4))
+        t0 = time.perf_counter()
+        op = mg.Operator.assemble(Lc, Mc, Nc, DX, FREQ, precision="mixed", nrhs_max=8)
+        res["assembly_s"] = time.perf_counter() - t0
+        t, out = _timed(lambda: mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, tol=TOL), 1, 0)
+        res["batch8"] = {"seconds": t, "flags": out[1].tolist(), "max_relres": float(out[2].max()),
+                         "iters": out[3].tolist()}
+        Esum = np.asfortranarray(sum(Es))
+        t, g = _timed(lambda: adjoint_gradient(op, Esum, er, DX, FREQ, "power", None, TOL), 1, 0)
+        res["gradient"] = {"seconds": t, "F": g[0], "flags": g[3], "iters": g[4]}
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -401,8 +495,13 @@ def main():
     ap.add_argument("--impl", default="marie", choices=["marie", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     args = ap.parse_args()
     world, rank, local = dist_init()
+    if args.config != "c2":
+        if rank == 0:
+            print(json.dumps(run_extra(args), default=float))
+        return
     if args.impl == "reference":
         out = run_reference(args, world, rank)
     else:

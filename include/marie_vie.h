@@ -133,6 +133,17 @@ int marie_jvie_solve(marie_plan* plan, const double* Einc, const double* e_r, do
  * (one batched matvec per GMRES step, one graph launch per restart cycle).
  * Per excitation: flag[e], relres[e], iter[2e..2e+1].  The reference solves
  * excitations one at a time (JVIE_Solver.m is called per port/excitation). */
+/* Several bodies of uneven grid size (one plan each), each with nexc[b]
+ * excitations, solved concurrently: every body's batch runs on its plan's
+ * stream from its own host thread.  Outputs are concatenated over bodies
+ * (flag, relres: sum(nexc); iter: 2 per excitation).  The reference solves one
+ * body at a time. */
+int marie_jvie_solve_bodies(int nbody, marie_plan* const* plans, const double* const* Einc,
+                            const int64_t* nexc, const double* const* e_r, const double* dx,
+                            double freq, int form, char precond, double tol, int inner_it,
+                            int outer_it, double* const* Je, int* flag, double* relres, int* iter,
+                            double* solvert);
+
 /* Adjoint gradient of a body-field objective with respect to the per-voxel
  * eps_r and sigma (no counterpart in the reference, which has no derivatives;
  * it reuses the J-VIE operator: K^T of the E-field system is the reference's
@@ -172,6 +183,9 @@ int marie_dipole_field(const double* r, int64_t L, int64_t M, int64_t N, double 
  * forward, z multiply, y inverse, x inverse) over the matvecs run since the
  * previous call, then resets and switches recording on or off. */
 int64_t marie_launch_count(void);
+/* Host-side fault injection for tests (no reference counterpart): the nth
+ * device allocation from now on fails with MARIE_ENOMEM (0 switches it off). */
+void marie_inject_alloc_failure(int64_t nth);
 int marie_plan_profile(marie_plan* plan, int enable, double* pass_ms, int64_t* count);
 
 #ifdef __cplusplus

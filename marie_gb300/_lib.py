@@ -53,6 +53,8 @@ SIGNATURES = {
                                _vp, _vp, _ip, _dp, _ip, _dp, C.c_int64, _i64p]),
     "marie_jvie_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_int, C.c_char, C.c_double,
                                    C.c_int, C.c_int, _vp, _ip, _dp, _ip, _dp, C.c_int64, _i64p, _dp]),
+    "marie_jvie_solve_bodies": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, C.c_char,
+                                          C.c_double, C.c_int, C.c_int, _vp, _ip, _dp, _ip, _dp]),
     "marie_jvie_adjoint_grad": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_int, _vp, C.c_double, C.c_int,
                                           C.c_int, _dp, _vp, _vp, _ip, _ip]),
     "marie_jvie_solve_batch": (C.c_int, [_vp, _vp, C.c_int64, _vp, C.c_double, C.c_double, C.c_int, C.c_char,
@@ -60,6 +62,7 @@ SIGNATURES = {
     "marie_e_field_nop": (C.c_int, [_vp, _vp, C.c_double, C.c_double, _vp, _vp, C.c_int]),
     "marie_plane_wave": (C.c_int, [_vp, C.c_int64, C.c_int64, C.c_int64, _vp, _vp, _vp]),
     "marie_launch_count": (C.c_int64, []),
+    "marie_inject_alloc_failure": (None, [C.c_int64]),
     "marie_plan_profile": (C.c_int, [_vp, C.c_int, _dp, _i64p]),
     "marie_dipole_field": (C.c_int, [_vp, C.c_int64, C.c_int64, C.c_int64, C.c_double, _vp, _vp, C.c_int64,
                                      _vp]),

@@ -45,9 +45,19 @@ int set_error(int code, const char* fmt, ...) {
   return code;
 }
 
+// host-side fault injection: the n-th allocation from now fails (0 = off)
+static std::atomic<long long> g_fail_alloc_in{0};
+
 int DBuf::alloc(size_t bytes, cudaStream_t st) {
   s = st;
   if (bytes == 0) bytes = 16;
+  long long left = g_fail_alloc_in.load();
+  while (left > 0 && !g_fail_alloc_in.compare_exchange_weak(left, left - 1)) {
+  }
+  if (left == 1) {
+    p = nullptr;
+    return set_error(MARIE_ENOMEM, "device allocation of %zu bytes failed (injected)", bytes);
+  }
   cudaError_t e = cudaMallocAsync(&p, bytes, st);
   if (e != cudaSuccess) {
     p = nullptr;
@@ -498,6 +508,8 @@ int marie_plan_destroy(marie_plan* p) {
 void* marie_plan_stream(marie_plan* p) { return p ? (void*)p->stream : nullptr; }
 
 int64_t marie_launch_count(void) { return g_launches.load(); }
+
+void marie_inject_alloc_failure(int64_t nth) { g_fail_alloc_in.store(nth > 0 ? nth : 0); }
 
 int marie_plan_profile(marie_plan* p, int enable, double* pass_ms, int64_t* count) {
   if (!p) return set_error(MARIE_EINVAL, "NULL plan");

@@ -27,17 +27,15 @@ template <int... Rs> struct RList {};
 // element every 16 positions when swz is set (row layouts, where the first
 // pass writes with stride R and would otherwise hit one bank).
 // half: column layouts whose rows are half a bank line (S * sizeof(V) = 64 B)
-// shift every other block of 16 rows by half a line, so that the radix-16
-// passes (which write rows 16 apart from neighbouring thread groups and read
-// consecutive rows) use both halves of the banks.
+// insert half a line after every block of 16 rows, so that rows 16 apart
+// (written at once by neighbouring thread groups of a radix-16 pass) fall in
+// alternate halves of the banks; consecutive rows stay contiguous.
 struct SAddr {
   int es, m, half;
   __host__ __device__ SAddr(int e) : es(e), m(0), half(0) {}
   __host__ __device__ SAddr(int e, bool swz) : es(e), m(swz ? -1 : 0), half(0) {}
   __host__ __device__ SAddr(int e, bool swz, int h) : es(e), m(swz ? -1 : 0), half(h) {}
-  __device__ __forceinline__ int operator()(int p) const {
-    return p * es + ((p >> 4) & m) + ((p >> 4) & 1) * half;
-  }
+  __device__ __forceinline__ int operator()(int p) const { return p * es + ((p >> 4) & m) + (p >> 4) * half; }
 };
 
 // Reversed radix list: the inverse transform runs the forward schedule

@@ -13,6 +13,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "plan.h"
@@ -524,6 +526,40 @@ int marie_jvie_solve_batch(marie_plan* p, const double* Einc, int64_t nexc, cons
       iter[2 * e + 1] = so.r[e].iter[1];
     }
   }
+  if (solvert) *solvert = std::chrono::duration<double>(t1 - t0).count();
+  return MARIE_OK;
+}
+
+int marie_jvie_solve_bodies(int nbody, marie_plan* const* plans, const double* const* Einc, const int64_t* nexc,
+                            const double* const* e_r, const double* dx, double freq, int form, char precond,
+                            double tol, int inner_it, int outer_it, double* const* Je, int* flag, double* relres,
+                            int* iter, double* solvert) {
+  if (nbody < 1 || !plans || !Einc || !nexc || !e_r || !dx || !Je) return set_error(MARIE_EINVAL, "NULL argument");
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<int> status(nbody, MARIE_OK);
+  std::vector<std::string> msg(nbody);
+  std::vector<long long> off(nbody + 1, 0);
+  for (int b = 0; b < nbody; ++b) off[b + 1] = off[b] + nexc[b];
+  // one host thread per body; each body's plan stream runs its own batch, so
+  // the bodies execute concurrently on the device
+  std::vector<std::thread> th;
+  for (int b = 0; b < nbody; ++b) {
+    th.emplace_back([&, b]() {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaSetDevice(plans[b]->device);
+      const int s = marie_jvie_solve_batch(plans[b], Einc[b], nexc[b], e_r[b], dx[b], freq, form, precond, tol,
+                                           inner_it, outer_it, Je[b], flag ? flag + off[b] : nullptr,
+                                           relres ? relres + off[b] : nullptr, iter ? iter + 2 * off[b] : nullptr,
+                                           nullptr);
+      status[b] = s;
+      if (s != MARIE_OK) msg[b] = marie_last_error();
+    });
+  }
+  for (auto& t : th) t.join();
+  for (int b = 0; b < nbody; ++b)
+    if (status[b] != MARIE_OK) return set_error(status[b], "body %d: %s", b, msg[b].c_str());
+  const auto t1 = std::chrono::steady_clock::now();
   if (solvert) *solvert = std::chrono::duration<double>(t1 - t0).count();
   return MARIE_OK;
 }

@@ -485,8 +485,12 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
   out.assign(S, GmresResult());
   std::vector<int> outit(S, 0), pk(S, 0), active(S, 0);
   for (int s = 0; s < S; ++s) {
-    out[s].resvec.push_back(rn[s] / bnorm[s]);
-    active[s] = (out[s].resvec.back() > tol && maxit > 0 && (!active_in || (*active_in)[s])) ? 1 : 0;
+    const bool wanted = !active_in || (*active_in)[s];
+    if (wanted && !std::isfinite(bnorm[s]))
+      return set_error(MARIE_EBREAKDOWN, "non-finite right-hand side (system %d)", s);
+    // b = 0 has the exact solution x = 0 (the reference's pgmres errors out)
+    out[s].resvec.push_back(bnorm[s] > 0 ? rn[s] / bnorm[s] : 0.0);
+    active[s] = (out[s].resvec.back() > tol && maxit > 0 && wanted) ? 1 : 0;
   }
   std::vector<double> tolabs(S);
   for (int s = 0; s < S; ++s) tolabs[s] = tol * bnorm[s];
@@ -531,6 +535,8 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
       ++outit[s];
       pk[s] = stop[s];
       for (int j = 0; j < stop[s]; ++j) out[s].resvec.push_back(resv[(size_t)s * restart + j] / bnorm[s]);
+      if (!std::isfinite(out[s].resvec.back()))
+        return set_error(MARIE_EBREAKDOWN, "non-finite GMRES residual (system %d, cycle %d)", s, outit[s]);
       active[s] = (out[s].resvec.back() > tol && outit[s] < maxit) ? 1 : 0;
     }
   }
@@ -559,7 +565,7 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
   for (int s = 0; s < S; ++s) {
     out[s].iter[0] = pk[s];
     out[s].iter[1] = outit[s];
-    out[s].relres = tr[s] / bn[s];
+    out[s].relres = bn[s] > 0 ? tr[s] / bn[s] : 0.0;
     out[s].flag = out[s].relres <= tol ? 0 : 1;
   }
   return MARIE_OK;

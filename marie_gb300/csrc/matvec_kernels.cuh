@@ -247,7 +247,7 @@ template <typename T, int NZ> struct ZS {
   // rows of 64 B use the half-line swizzle, others one pad element per row
   static constexpr bool HALF = S * (int)sizeof(cplx<T>) == 64;
   static constexpr int ES = HALF ? S : S + 1;
-  static constexpr int BUF = NZ * ES + (HALF ? S : 0);     // one component's exchange buffer
+  static constexpr int BUF = NZ * ES + (HALF ? (NZ / 16 + 1) * S : 0);  // one component's exchange buffer
   static constexpr long long bytes(int) { return (long long)(NZ + 3 * BUF) * sizeof(cplx<T>); }
   __device__ static SAddr addr() { return SAddr(ES, false, HALF ? S : 0); }
 };

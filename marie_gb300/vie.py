@@ -435,6 +435,54 @@ def JVIE_Solver_batch(Einc, e_r, r, freq, fN, tol=None, form=None, precond=None,
             opr.close()
 
 
+def JVIE_Solver_bodies(bodies, freq, tol=None, form=None, precond=None, inner_it=None, outer_it=None):
+    """Several bodies of uneven grid size solved concurrently.
+
+    bodies: list of (Einc (L,M,N,3,nexc), e_r (L,M,N), r, Operator).  Returns a
+    list of (Je, flag, relres, iter) per body and the wall time."""
+    tol = 1e-3 if tol is None else tol
+    form = 2 if form is None else form
+    pc = {None: b"\0", 0: b"\0", "L": b"L", "R": b"R"}.get(precond, b"\0")
+    inner_it = 50 if inner_it is None or inner_it < 1 else inner_it
+    outer_it = 200 if outer_it is None or outer_it < 1 else outer_it
+    nb = len(bodies)
+    keep, Ep, Erp, Jp, outs = [], [], [], [], []
+    nexc = np.zeros(nb, np.int64)
+    dxs = np.zeros(nb)
+    plans = (C.c_void_p * nb)()
+    for b, (Einc, e_r, r, op) in enumerate(bodies):
+        L, M, N = e_r.shape
+        nexc[b] = Einc.shape[4]
+        dxs[b] = float(r[1, 0, 0, 0] - r[0, 0, 0, 0])
+        ep, ek = _in(Einc)
+        erp, erk = _in(e_r)
+        jp, Je = _out((L, M, N, 3, int(nexc[b])), _is_cuda(Einc))
+        keep += [ek, erk]
+        Ep.append(ep.value)
+        Erp.append(erp.value)
+        Jp.append(jp.value)
+        outs.append(Je)
+        plans[b] = op.plan.value
+    tot = int(nexc.sum())
+    flag = np.zeros(tot, np.int32)
+    relres = np.zeros(tot)
+    it = np.zeros(2 * tot, np.int32)
+    solvert = C.c_double()
+    arr = lambda v: (C.c_void_p * nb)(*v)
+    lib = _lib.load()
+    check(lib.marie_jvie_solve_bodies(nb, plans, arr(Ep), nexc.ctypes.data_as(_lib._i64p), arr(Erp),
+                                      dxs.ctypes.data_as(_lib._dp), float(freq), int(form), pc, float(tol),
+                                      int(inner_it), int(outer_it), arr(Jp), flag.ctypes.data_as(_lib._ip),
+                                      relres.ctypes.data_as(_lib._dp), it.ctypes.data_as(_lib._ip),
+                                      C.byref(solvert)))
+    res, o = [], 0
+    for b in range(nb):
+        k = int(nexc[b])
+        res.append((outs[b], flag[o:o + k], relres[o:o + k], it.reshape(-1, 2)[o:o + k]))
+        o += k
+    return res, solvert.value
+
+
 # ---------------------------------------------------------------------------
 # excitations
 # ---------------------------------------------------------------------------

@@ -1,0 +1,75 @@
+"""Failure handling on the device path, with every failure made on the host
+(no kernel is made to fault, trap or hang): non-convergence is a flag,
+non-finite inputs and allocation failures are error statuses, and the
+library stays usable afterwards."""
+import numpy as np
+import pytest
+
+from oracle import vie_oracle as vo
+
+pytestmark = pytest.mark.gpu
+FREQ = 298e6
+
+
+def sphere(L=8, dx=5e-3, R=0.018):
+    r = vo.grid(L, L, L, dx)
+    er = np.ones((L, L, L), complex)
+    er[np.sum(r * r, axis=3) < R**2] = 50 - 30j
+    em = vo.EMconstants(FREQ)
+    E, _ = vo.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
+    return r, np.asfortranarray(er), np.asfortranarray(E)
+
+
+def test_non_convergence_is_a_flag_not_an_error():
+    import marie_gb300 as mg
+
+    r, er, E = sphere()
+    op = mg.Operator.assemble(8, 8, 8, 5e-3, FREQ)
+    Je, flag, relres, it, resvec, _ = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-12, inner_it=2, outer_it=1)
+    assert flag == 1 and relres > 1e-12
+    assert it == [2, 1] and len(resvec) == 3
+
+
+def test_non_finite_input_is_reported_and_library_recovers():
+    import marie_gb300 as mg
+
+    r, er, E = sphere()
+    op = mg.Operator.assemble(8, 8, 8, 5e-3, FREQ)
+    Ebad = E.copy(order="F")
+    Ebad[3, 3, 3, 0] = np.nan
+    with pytest.raises(mg.MarieError, match="non-finite"):
+        mg.JVIE_Solver(Ebad, er, r, FREQ, op, tol=1e-8)
+    out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8)
+    assert out[1] == 0
+
+
+def test_air_only_and_zero_excitation():
+    import marie_gb300 as mg
+
+    r, er, E = sphere()
+    op = mg.Operator.assemble(8, 8, 8, 5e-3, FREQ)
+    air = np.ones_like(er)
+    Je, flag, relres, *_ = mg.JVIE_Solver(E, air, r, FREQ, op, tol=1e-8)
+    assert flag == 0 and not np.any(Je)
+    Je, flag, relres, *_ = mg.JVIE_Solver(np.zeros_like(E), er, r, FREQ, op, tol=1e-8)
+    assert flag == 0 and relres == 0 and not np.any(Je)
+
+
+@pytest.mark.parametrize("nth", [1, 3, 6, 12])
+def test_allocation_failure_is_enomem_and_plan_stays_usable(nth):
+    """An allocation failure (injected on the host at the nth device allocation
+    of the solve) surfaces as MARIE_ENOMEM; the next solve succeeds."""
+    import marie_gb300 as mg
+
+    r, er, E = sphere()
+    op = mg.Operator.assemble(8, 8, 8, 5e-3, FREQ)
+    lib = mg.load()
+    lib.marie_inject_alloc_failure(nth)
+    try:
+        with pytest.raises(mg.MarieError) as ei:
+            mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8)
+        assert ei.value.code == -2
+    finally:
+        lib.marie_inject_alloc_failure(0)
+    out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8)
+    assert out[1] == 0
