@@ -248,9 +248,24 @@ template <typename T, int NZ> struct ZS {
   static constexpr bool HALF = S * (int)sizeof(cplx<T>) == 64;
   static constexpr int ES = HALF ? S : S + 1;
   static constexpr int BUF = NZ * ES + (HALF ? (NZ / 16 + 1) * S : 0);  // one component's exchange buffer
-  static constexpr long long bytes(int) { return (long long)(NZ + 3 * BUF) * sizeof(cplx<T>); }
+  // octant operator tile of the CTA's columns: 6 components x (N+1) planes x S
+  static constexpr int TILE = 6 * (NZ / 2 + 1) * S;
+  static constexpr long long bytes(int) { return (long long)(NZ + 3 * BUF + TILE) * sizeof(cplx<T>); }
   __device__ static SAddr addr() { return SAddr(ES, false, HALF ? S : 0); }
 };
+
+// asynchronous global -> shared copy of one complex value (no register staging)
+template <typename V> __device__ __forceinline__ void cp_async_val(V* dst, const V* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(V) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src));
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::);
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
 
 // odd components along x, y, z: xy (1), xz (2) | xy (1), yz (4) | xz (2), yz (4)
 __device__ __forceinline__ bool odd_x(int q) { return q == 1 || q == 2; }
@@ -285,9 +300,33 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   const int rem = threadIdx.x - c * S * FF::T;
   const int s = rem % S, t = rem / S;
   V* Bp = B + blockIdx.z * b_rhs + c * comp + (long long)ky * d.Lp + kx0;
-  stage_twiddles(tw_s, tw, NZ);
+  V* tile = buf + 3 * BUF;  // octant operator of the CTA's columns, [q][oz][s]
   const int kx = kx0 + s;
   const bool active = kx < d.Lp;
+  int ox = kx, oy = ky;
+  bool fx = false, fy = false;
+  if (oct) {
+    if (kx > d.L) { ox = d.Lp - kx; fx = true; }
+    if (ky > d.M) { oy = d.Mp - ky; fy = true; }
+  }
+  const long long fq = oct ? (long long)(d.L + 1) * (d.M + 1) * (d.N + 1) : (long long)d.Lp * d.Mp * d.Np;
+  const long long fplane = oct ? (long long)(d.L + 1) * (d.M + 1) : plane;
+  const long long frow = oct ? (long long)(d.L + 1) : d.Lp;
+  if (oct) {
+    // the operator tile streams into shared memory while the forward
+    // transforms run (its latency was the z pass's main stall)
+    const int NO = d.N + 1;
+    for (int i = threadIdx.x; i < 6 * NO * S; i += blockDim.x) {
+      const int ss = i % S, rest = i / S;
+      const int oz = rest % NO, q = rest / NO;
+      const int kxs = kx0 + ss;
+      if (kxs < d.Lp) {
+        const int oxs = kxs > d.L ? d.Lp - kxs : kxs;
+        cp_async_val(tile + i, fN + q * fq + (long long)oz * fplane + (long long)oy * frow + oxs);
+      }
+    }
+  }
+  stage_twiddles(tw_s, tw, NZ);
   V reg[E];
 #pragma unroll
   for (int b = 0; b < E / R0; ++b)
@@ -301,19 +340,12 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   FF::run_half(reg, my, ad, t, tw_s);
   __syncthreads();
   FF::store(reg, my, ad, t);
+  if (oct) cp_async_wait_all();
   __syncthreads();
 
   // row c of the symmetric product at this thread's positions
-  int ox = kx, oy = ky;
-  bool fx = false, fy = false;
-  if (oct) {
-    if (kx > d.L) { ox = d.Lp - kx; fx = true; }
-    if (ky > d.M) { oy = d.Mp - ky; fy = true; }
-  }
-  const long long fq = oct ? (long long)(d.L + 1) * (d.M + 1) * (d.N + 1) : (long long)d.Lp * d.Mp * d.Np;
-  const long long fplane = oct ? (long long)(d.L + 1) * (d.M + 1) : plane;
-  const long long frow = oct ? (long long)(d.L + 1) : d.Lp;
   const V* fp = fN + (long long)oy * frow + ox;
+  const int NO = d.N + 1;
   // components of row c: c=0 (xx,xy,xz), c=1 (xy,yy,yz), c=2 (xz,yz,zz)
   const int q0 = c == 0 ? 0 : (c == 1 ? 1 : 2);
   const int q1 = c == 0 ? 1 : (c == 1 ? 3 : 4);
@@ -331,8 +363,17 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
       if (oct && kz > d.N) { oz = d.Np - kz; fz = true; }
       V y = mk<V>(0, 0);
       if (active) {
-        const long long o = (long long)oz * fplane;
-        V n0 = fp[q0 * fq + o], n1 = fp[q1 * fq + o], n2 = fp[q2 * fq + o];
+        V n0, n1, n2;
+        if (oct) {
+          n0 = tile[(q0 * NO + oz) * S + s];
+          n1 = tile[(q1 * NO + oz) * S + s];
+          n2 = tile[(q2 * NO + oz) * S + s];
+        } else {
+          const long long o = (long long)oz * fplane;
+          n0 = fp[q0 * fq + o];
+          n1 = fp[q1 * fq + o];
+          n2 = fp[q2 * fq + o];
+        }
         if ((fx && odd_x(q0)) ^ (fy && odd_y(q0)) ^ (fz && odd_z(q0))) n0 = mk<V>(-n0.x, -n0.y);
         if ((fx && odd_x(q1)) ^ (fy && odd_y(q1)) ^ (fz && odd_z(q1))) n1 = mk<V>(-n1.x, -n1.y);
         if ((fx && odd_x(q2)) ^ (fy && odd_y(q2)) ^ (fz && odd_z(q2))) n2 = mk<V>(-n2.x, -n2.y);
