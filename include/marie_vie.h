@@ -99,6 +99,20 @@ int marie_mv_AN(marie_plan* plan, const double* JIn0, const double* Mr, const do
                 double Gram, int transp, const int64_t* idx, int64_t n_idx, double* JOut,
                 int64_t nrhs, int precision);
 
+/* No counterpart in the reference: marie_mv_AN (one right-hand side) that
+ * allocates nothing, for callers that cannot let a library allocate device
+ * memory when they ask for a matvec (a host whose device memory belongs to
+ * another allocator, such as MATLAB's gpuArray pool or a serving runtime's
+ * fixed arena, or a loop that must not block in cudaMalloc).  Its scratch is a
+ * 64 MiB static device array that every GPU loading this library holds until
+ * exit; grids needing more (about 204-252 bytes per voxel in FP32, 396 in FP64)
+ * are rejected with MARIE_EINVAL.  Device pointers only.  The first call on a
+ * device looks up the array's address; make it before any stream capture.
+ * Calls share the array, so calls that overlap on the GPU race. */
+int marie_mv_AN_static(marie_plan* plan, const double* JIn0, const double* Mr,
+                       const double* Mc, double Gram, int transp, const int64_t* idx,
+                       int64_t n_idx, double* JOut, int precision);
+
 /* Replaces mv_L(JIn0, fN, r, Gram, idx, GPU_flag) (src_vie/src_mvp/mv_L.m:1-97):
  * JOut = crop(N J) - Gram*J on the entries idx. */
 int marie_mv_L(marie_plan* plan, const double* JIn0, double Gram, const int64_t* idx,

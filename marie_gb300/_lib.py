@@ -47,6 +47,7 @@ SIGNATURES = {
     "marie_plan_assemble": (C.c_int, [_vp, C.c_double, C.c_double, C.c_char, _vp]),
     "marie_get_plan_operator": (C.c_int, [_vp, _vp]),
     "marie_mv_AN": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, C.c_int, _vp, C.c_int64, _vp, C.c_int64, C.c_int]),
+    "marie_mv_AN_static": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, C.c_int, _vp, C.c_int64, _vp, C.c_int]),
     "marie_mv_L": (C.c_int, [_vp, _vp, C.c_double, _vp, C.c_int64, _vp, C.c_int64, C.c_int]),
     "marie_pgmres": (C.c_int, [_vp, OP_FN, _vp, _vp, C.c_int64, C.c_int, C.c_double, C.c_int,
                                OP_FN, _vp, OP_FN, _vp, OP_FN, _vp, OP_FN, _vp,
