@@ -339,8 +339,15 @@ template <typename V, int N, bool INV> struct FFT {
   static constexpr int RL = LP::R_last;
   static constexpr int NSL = LP::NS_last;
 
+  static_assert((T & (T - 1)) == 0, "threads per transform must be a power of two");
+  // Every caller launches exactly T threads per transform, so t < T.  Masking
+  // states that range to the compiler, which then folds the position
+  // arithmetic (carries out of the low bits, the first/second-half tests of a
+  // zero-padded input) into per-thread constants.
+  __device__ __forceinline__ static int lane(int t) { return t & (T - 1); }
+
   // Input position of reg[b*R0 + r] for the first pass.
-  __device__ __forceinline__ static int in_pos(int t, int b, int r) { return t + b * T + r * (N / R0); }
+  __device__ __forceinline__ static int in_pos(int t, int b, int r) { return lane(t) + b * T + r * (N / R0); }
 
   // Load the first pass's inputs from shared memory.  Positions >= n_valid are
   // treated as zero without being read (zero padding).
@@ -367,16 +374,16 @@ template <typename V, int N, bool INV> struct FFT {
     }
   }
   __device__ __forceinline__ static void run(V* reg, V* base, SAddr es, int t, const V* tw) {
-    Passes<V, N, E, INV, 1, false, RL_>::run(reg, base, es, t, tw);
+    Passes<V, N, E, INV, 1, false, RL_>::run(reg, base, es, lane(t), tw);
   }
   // First pass on inputs with a zero upper half (R0 even).
   __device__ __forceinline__ static void run_half(V* reg, V* base, SAddr es, int t, const V* tw) {
     static_assert(R0 % 2 == 0, "zero-half skipping needs an even first radix");
-    Passes<V, N, E, INV, 1, true, RL_>::run(reg, base, es, t, tw);
+    Passes<V, N, E, INV, 1, true, RL_>::run(reg, base, es, lane(t), tw);
   }
   // Output position of reg[b*RL + r] after run().
   __device__ __forceinline__ static int out_pos(int t, int b, int r) {
-    const int j = t + b * T;
+    const int j = lane(t) + b * T;
     return (j / NSL) * NSL * RL + (j % NSL) + r * NSL;
   }
   // Store all outputs (natural order) back to shared memory.  Caller syncs.

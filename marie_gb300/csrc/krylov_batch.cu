@@ -192,8 +192,12 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
   return mk<double2>((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
 }
 
-// one warp per system: H column k, rotations, y = R \ g, res = rhs - Hc y,
-// ||res||, stop test (pgmres_iter.m:106-125)
+// One warp per system: store H column k, apply the previous rotations to it,
+// form the new rotation and update g (pgmres_iter.m:106-125).  The LSQ
+// residual norm ||rhs - Hc y|| equals |g(k+1)| after the rotations, so the
+// per-step stop test needs no solve; y = R \ g and the explicit residual
+// res = rhs - Hc y (which restarts the next cycle as V*res) are formed once,
+// at the step that ends the cycle.
 __global__ void kb_givens(GState G, int m, int k, const double2* __restrict__ h, int hld,
                           const double* __restrict__ npart, int NB) {
   const int s = blockIdx.x;
@@ -207,6 +211,8 @@ __global__ void kb_givens(GState G, int m, int k, const double2* __restrict__ h,
   double2* sn = G.sn + (long long)s * m;
   double2* y = G.y + (long long)s * m;
   double2* res = G.res + (long long)s * ld;
+  __shared__ double2 col_s[128], sn_s[128];
+  __shared__ double cs_s[128];
   const int kk = k - 1;
   double nn = 0;
   for (int b = lane; b < NB; b += 32) nn += npart[(long long)s * NB + b];
@@ -215,25 +221,29 @@ __global__ void kb_givens(GState G, int m, int k, const double2* __restrict__ h,
   for (int i = lane; i < k; i += 32) {
     const double2 v = h[(long long)s * hld + i];
     H[kk * ld + i] = v;
-    R[kk * ld + i] = v;
+    col_s[i] = v;
+  }
+  for (int i = lane; i < kk; i += 32) {
+    cs_s[i] = cs[i];
+    sn_s[i] = sn[i];
   }
   if (lane == 0) {
     H[kk * ld + k] = mk<double2>(hnv, 0);
-    if (k == 1) {
-      g[0] = mk<double2>(G.beta[s], 0);
-    }
+    if (k == 1) g[0] = mk<double2>(G.beta[s], 0);
   }
   __syncwarp();
+  double rn = 0;
   if (lane == 0) {
     double2* col = R + kk * ld;
+    // the rotated entry i+1 is carried in a register along the chain
+    double2 a = col_s[0];
     for (int i = 0; i < kk; ++i) {
-      const double2 a = col[i], b = col[i + 1];
-      const double c = cs[i];
-      const double2 sv = sn[i];
+      const double2 b = col_s[i + 1];
+      const double c = cs_s[i];
+      const double2 sv = sn_s[i];
       col[i] = cadd(cscale(a, c), cmul(sv, b));
-      col[i + 1] = csub(cscale(b, c), cmulc(a, sv));  // -conj(s) a + c b
+      a = csub(cscale(b, c), cmulc(a, sv));  // -conj(s) a + c b
     }
-    const double2 a = col[kk];
     const double aa = hypot(a.x, a.y), bb = hnv;
     double c;
     double2 sv;
@@ -253,8 +263,14 @@ __global__ void kb_givens(GState G, int m, int k, const double2* __restrict__ h,
     sn[kk] = sv;
     const double2 gk = g[kk];
     g[kk] = cscale(gk, c);
-    g[k] = mk<double2>(-(sv.x * gk.x + sv.y * gk.y), -(sv.x * gk.y - sv.y * gk.x));  // -conj(s) g
+    const double2 gn = mk<double2>(-(sv.x * gk.x + sv.y * gk.y), -(sv.x * gk.y - sv.y * gk.x));  // -conj(s) g
+    g[k] = gn;
+    rn = hypot(gn.x, gn.y);
+    G.resv[(long long)s * m + kk] = rn;
+    G.hn[s] = hnv;
   }
+  rn = __shfl_sync(0xffffffffu, rn, 0);
+  if (!(rn < G.tolabs[s] || k == m)) return;
   __syncwarp();
   // back-substitution y = R(0:k,0:k) \ g(0:k)
   for (int i = k - 1; i >= 0; --i) {
@@ -265,20 +281,12 @@ __global__ void kb_givens(GState G, int m, int k, const double2* __restrict__ h,
     __syncwarp();
   }
   // res = rhs - Hc y with rhs = [beta; 0], Hc = H(0:k+1, 0:k)
-  double rr = 0;
   for (int i = lane; i <= k; i += 32) {
     double2 v = i == 0 ? mk<double2>(G.beta[s], 0) : mk<double2>(0, 0);
     for (int j = (i > 0 ? i - 1 : 0); j < k; ++j) v = csub(v, cmul(H[j * ld + i], y[j]));
     res[i] = v;
-    rr = fma(v.x, v.x, fma(v.y, v.y, rr));
   }
-  rr = wsum(rr);
-  if (lane == 0) {
-    const double rn = sqrt(rr);
-    G.resv[(long long)s * m + kk] = rn;
-    G.hn[s] = hnv;
-    if (rn < G.tolabs[s] || k == m) G.stop[s] = k;
-  }
+  if (lane == 0) G.stop[s] = k;
 }
 
 // V_s(:,k) /= H(k+1,k)  (zero norm leaves a zero column instead of 0/0)

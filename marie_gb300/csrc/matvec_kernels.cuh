@@ -268,9 +268,58 @@ __device__ __forceinline__ void cp_async_wait_all() {
 }
 
 // odd components along x, y, z: xy (1), xz (2) | xy (1), yz (4) | xz (2), yz (4)
-__device__ __forceinline__ bool odd_x(int q) { return q == 1 || q == 2; }
-__device__ __forceinline__ bool odd_y(int q) { return q == 1 || q == 4; }
-__device__ __forceinline__ bool odd_z(int q) { return q == 2 || q == 4; }
+__host__ __device__ constexpr bool odd_x(int q) { return q == 1 || q == 2; }
+__host__ __device__ constexpr bool odd_y(int q) { return q == 1 || q == 4; }
+__host__ __device__ constexpr bool odd_z(int q) { return q == 2 || q == 4; }
+
+// Components of row c of the symmetric tensor [xx xy xz; xy yy yz; xz yz zz].
+template <int C> struct ZRow {
+  static constexpr int q0 = C == 0 ? 0 : (C == 1 ? 1 : 2);
+  static constexpr int q1 = C == 0 ? 1 : (C == 1 ? 3 : 4);
+  static constexpr int q2 = C == 0 ? 2 : (C == 1 ? 4 : 5);
+};
+
+template <typename V> __device__ __forceinline__ V neg_if(V v, bool f) { return f ? mk<V>(-v.x, -v.y) : v; }
+
+// Row C of the product at this thread's output positions of the forward
+// transform.  With the octant operator the tile already carries the x and y
+// reflection signs; the z reflection (positions kz > NZ/2) flips the two
+// z-odd components.  Without it the full operator is read from global memory.
+template <int C, typename FF, typename V, int NZ, int S>
+__device__ __forceinline__ void zrow(V* reg, int t, int s, bool active, int oct, const V* tile, const V* fp,
+                                     long long fq, long long fplane, const V* b0, const V* b1, const V* b2,
+                                     SAddr ad) {
+  using RW = ZRow<C>;
+  constexpr int NH = NZ / 2, NO = NH + 1, RL = FF::RL;
+#pragma unroll
+  for (int b = 0; b < FF::E / RL; ++b)
+#pragma unroll
+    for (int r = 0; r < RL; ++r) {
+      const int kz = FF::out_pos(t, b, r);
+      V y = mk<V>(0, 0);
+      if (active) {
+        V n0, n1, n2;
+        if (oct) {
+          const bool fz = kz > NH;
+          const int oz = fz ? NZ - kz : kz;
+          n0 = tile[(RW::q0 * NO + oz) * S + s];
+          n1 = tile[(RW::q1 * NO + oz) * S + s];
+          n2 = tile[(RW::q2 * NO + oz) * S + s];
+          if constexpr (odd_z(RW::q0)) n0 = neg_if(n0, fz);
+          if constexpr (odd_z(RW::q1)) n1 = neg_if(n1, fz);
+          if constexpr (odd_z(RW::q2)) n2 = neg_if(n2, fz);
+        } else {
+          const long long o = (long long)kz * fplane;
+          n0 = fp[RW::q0 * fq + o];
+          n1 = fp[RW::q1 * fq + o];
+          n2 = fp[RW::q2 * fq + o];
+        }
+        const int e = ad(kz);
+        y = cadd(cadd(cmul(n0, b0[e]), cmul(n1, b1[e])), cmul(n2, b2[e]));
+      }
+      reg[b * RL + r] = y;
+    }
+}
 
 // Thread group c (of three) transforms component c of the S columns.  After
 // the forward transforms the three spectra meet in shared memory; group c
@@ -286,43 +335,46 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   using FI = FFT<V, NZ, true>;
   constexpr int S = ZS<T, NZ>::S;
   constexpr int BUF = ZS<T, NZ>::BUF;
+  constexpr int NH = NZ / 2, NO = NH + 1;  // N non-zero planes; N+1 octant planes
   const SAddr ad = ZS<T, NZ>::addr();
-  constexpr int E = FF::E, R0 = FF::R0, RL = FF::RL, RLI = FI::RL;
-  static_assert(FI::R0 == RL, "inverse must start where the forward transform ended");
+  constexpr int E = FF::E, R0 = FF::R0, RLI = FI::RL;
+  static_assert(FI::R0 == FF::RL, "inverse must start where the forward transform ended");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw_s = reinterpret_cast<V*>(smem_raw);
   V* buf = tw_s + NZ;  // 3 exchange buffers of BUF elements
   const int kx0 = blockIdx.x * S;
   const int ky = blockIdx.y;
   const long long plane = (long long)d.Lp * d.Mp;  // one z-plane of B
-  const long long comp = plane * d.N;               // one component of B
+  const long long comp = plane * NH;                // one component of B
   const int c = threadIdx.x / (S * FF::T);
   const int rem = threadIdx.x - c * S * FF::T;
   const int s = rem % S, t = rem / S;
   V* Bp = B + blockIdx.z * b_rhs + c * comp + (long long)ky * d.Lp + kx0;
   V* tile = buf + 3 * BUF;  // octant operator of the CTA's columns, [q][oz][s]
-  const int kx = kx0 + s;
-  const bool active = kx < d.Lp;
-  int ox = kx, oy = ky;
-  bool fx = false, fy = false;
-  if (oct) {
-    if (kx > d.L) { ox = d.Lp - kx; fx = true; }
-    if (ky > d.M) { oy = d.Mp - ky; fy = true; }
-  }
-  const long long fq = oct ? (long long)(d.L + 1) * (d.M + 1) * (d.N + 1) : (long long)d.Lp * d.Mp * d.Np;
+  const bool active = kx0 + s < d.Lp;
+  const bool fy = oct && ky > d.M;
+  const int oy = fy ? d.Mp - ky : ky;
+  const long long fq = oct ? (long long)(d.L + 1) * (d.M + 1) * NO : (long long)d.Lp * d.Mp * d.Np;
   const long long fplane = oct ? (long long)(d.L + 1) * (d.M + 1) : plane;
   const long long frow = oct ? (long long)(d.L + 1) : d.Lp;
-  if (oct) {
+  // Tile rows (q, oz) of S columns: this thread copies column s of rows
+  // row0, row0 + STEP, ... (THREADS is a multiple of S).
+  constexpr int ROWS = 6 * NO, STEP = ZS<T, NZ>::THREADS / S;
+  const int row0 = threadIdx.x / S;
+  if (oct && active) {
     // the operator tile streams into shared memory while the forward
     // transforms run (its latency was the z pass's main stall)
-    const int NO = d.N + 1;
-    for (int i = threadIdx.x; i < 6 * NO * S; i += blockDim.x) {
-      const int ss = i % S, rest = i / S;
-      const int oz = rest % NO, q = rest / NO;
-      const int kxs = kx0 + ss;
-      if (kxs < d.Lp) {
-        const int oxs = kxs > d.L ? d.Lp - kxs : kxs;
-        cp_async_val(tile + i, fN + q * fq + (long long)oz * fplane + (long long)oy * frow + oxs);
+    const int kx = kx0 + s;
+    const int ox = kx > d.L ? d.Lp - kx : kx;
+    int q = row0 / NO, oz = row0 - q * NO;
+    const V* src = fN + q * fq + (long long)oz * fplane + (long long)oy * frow + ox;
+    for (int row = row0; row < ROWS; row += STEP) {
+      cp_async_val(tile + row * S + s, src);
+      oz += STEP;
+      src += STEP * fplane;
+      while (oz >= NO) {
+        oz -= NO;
+        src += fq - NO * fplane;
       }
     }
   }
@@ -333,62 +385,57 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
 #pragma unroll
     for (int r = 0; r < R0; ++r) {
       const int p = FF::in_pos(t, b, r);
-      reg[b * R0 + r] = (active && r < R0 / 2 && p < d.N) ? Bp[p * plane + s] : mk<V>(0, 0);
+      reg[b * R0 + r] = (active && r < R0 / 2 && p < NH) ? Bp[p * plane + s] : mk<V>(0, 0);
     }
   __syncthreads();  // twiddles staged
   V* my = buf + c * BUF + s;
   FF::run_half(reg, my, ad, t, tw_s);
   __syncthreads();
   FF::store(reg, my, ad, t);
-  if (oct) cp_async_wait_all();
+  if (oct && active) {
+    // each thread signs the tile entries it copied: reflections in x and y
+    // flip the components odd along that axis
+    cp_async_wait_all();
+    const bool fx = kx0 + s > d.L;
+    unsigned flip = 0;
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+      if ((fx && odd_x(q)) != (fy && odd_y(q))) flip |= 1u << q;
+    if (flip) {
+      int q = row0 / NO, oz = row0 - q * NO;
+      for (int row = row0; row < ROWS; row += STEP) {
+        if ((flip >> q) & 1u) {
+          V* e = tile + row * S + s;
+          *e = mk<V>(-e->x, -e->y);
+        }
+        oz += STEP;
+        while (oz >= NO) {
+          oz -= NO;
+          ++q;
+        }
+      }
+    }
+  }
   __syncthreads();
 
-  // row c of the symmetric product at this thread's positions
-  const V* fp = fN + (long long)oy * frow + ox;
-  const int NO = d.N + 1;
-  // components of row c: c=0 (xx,xy,xz), c=1 (xy,yy,yz), c=2 (xz,yz,zz)
-  const int q0 = c == 0 ? 0 : (c == 1 ? 1 : 2);
-  const int q1 = c == 0 ? 1 : (c == 1 ? 3 : 4);
-  const int q2 = c == 0 ? 2 : (c == 1 ? 4 : 5);
+  const V* fp = fN + (long long)oy * frow + (kx0 + s);
   const V* b0 = buf + s;
   const V* b1 = buf + BUF + s;
   const V* b2 = buf + 2 * BUF + s;
-#pragma unroll
-  for (int b = 0; b < E / RL; ++b)
-#pragma unroll
-    for (int r = 0; r < RL; ++r) {
-      const int kz = FF::out_pos(t, b, r);
-      int oz = kz;
-      bool fz = false;
-      if (oct && kz > d.N) { oz = d.Np - kz; fz = true; }
-      V y = mk<V>(0, 0);
-      if (active) {
-        V n0, n1, n2;
-        if (oct) {
-          n0 = tile[(q0 * NO + oz) * S + s];
-          n1 = tile[(q1 * NO + oz) * S + s];
-          n2 = tile[(q2 * NO + oz) * S + s];
-        } else {
-          const long long o = (long long)oz * fplane;
-          n0 = fp[q0 * fq + o];
-          n1 = fp[q1 * fq + o];
-          n2 = fp[q2 * fq + o];
-        }
-        if ((fx && odd_x(q0)) ^ (fy && odd_y(q0)) ^ (fz && odd_z(q0))) n0 = mk<V>(-n0.x, -n0.y);
-        if ((fx && odd_x(q1)) ^ (fy && odd_y(q1)) ^ (fz && odd_z(q1))) n1 = mk<V>(-n1.x, -n1.y);
-        if ((fx && odd_x(q2)) ^ (fy && odd_y(q2)) ^ (fz && odd_z(q2))) n2 = mk<V>(-n2.x, -n2.y);
-        const int e = ad(kz);
-        y = cadd(cadd(cmul(n0, b0[e]), cmul(n1, b1[e])), cmul(n2, b2[e]));
-      }
-      reg[b * RL + r] = y;
-    }
+  // c is uniform over whole warps (groups of S * T threads) for the long transforms
+  if (c == 0)
+    zrow<0, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, b0, b1, b2, ad);
+  else if (c == 1)
+    zrow<1, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, b0, b1, b2, ad);
+  else
+    zrow<2, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, b0, b1, b2, ad);
   FI::run(reg, my, ad, t, tw_s);
 #pragma unroll
   for (int b = 0; b < E / RLI; ++b)
 #pragma unroll
     for (int r = 0; r < RLI; ++r) {
       const int z = FI::out_pos(t, b, r);
-      if (active && z < d.N) Bp[z * plane + s] = reg[b * RLI + r];
+      if (active && z < NH) Bp[z * plane + s] = reg[b * RLI + r];
     }
 }
 
