@@ -45,9 +45,24 @@ N_ELL = 12
 TOL = 1e-6
 RESTART = 50
 # FP64 GMRES iterations of this workload (seed 0), measured by the FP64 arm on
-# GB300 (the CPU restatement takes the same iterations by parity); used only to
-# scale the CPU arm's per-iteration time to solves/s.
-FP64_ITERATIONS_C2 = None
+# GB300 (iter = [20, 5]: four full cycles of 50 and 20 steps; the CPU
+# restatement takes the same iterations by parity); used only to scale the CPU
+# arm's per-iteration time to solves/s.
+FP64_ITERATIONS_C2 = 220
+# DRAM traffic of one z-pass launch (k_zmul<float,256>) at this workload, read
+# from the committed ncu summary of that kernel.
+ZMUL_PROFILE = ROOT / "profiles" / "k_zmul_f32_128cube.md"
+
+
+def zmul_traffic():
+    """dram__bytes_read.sum + dram__bytes_write.sum per launch, or None."""
+    try:
+        for line in ZMUL_PROFILE.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":")[1].split()[0])
+    except OSError:
+        pass
+    return None
 
 
 def peaks():
@@ -174,7 +189,14 @@ def run_gpu(args, world, rank, local):
     stream = torch.cuda.ExternalStream(lib.marie_plan_stream(op.plan))
 
     def solve(opr, Ein, e_r, rr):
-        return mg.JVIE_Solver(Ein, e_r, rr, FREQ, opr, tol=TOL, form=2, inner_it=RESTART, outer_it=200)
+        return mg.JVIE_Solver(Ein, e_r, rr, FREQ, opr, tol=TOL, form=2, inner_it=RESTART, outer_it=200, solver="G")
+
+    if args.solve_only:
+        # profiling entry: the mixed solves of the timed region and nothing else
+        for _ in range(args.warmup + args.steps):
+            res = solve(op, Ed, erd, r)
+        torch.cuda.synchronize()
+        return {"solve_only": True, "flag": res[1], "relres": res[2], "iter": res[3]} if rank == 0 else {}
 
     # --- timed region: mixed-precision solves, inputs resident in HBM --------
     for _ in range(args.warmup):
@@ -209,6 +231,18 @@ def run_gpu(args, world, rank, local):
         n_it64 = len(resvec64) - 1
         field_err = float((torch.linalg.norm(Jm - J64) / torch.linalg.norm(J64)).item())
 
+        # --- the other solvers of JVIE_Solver, mixed precision, one solve each
+        variants = {}
+        for sv in ("B", "D"):
+            t0 = time.perf_counter()
+            Jv, fv, rv, itv, resv, _ = mg.JVIE_Solver(Ed, erd, r, FREQ, op, tol=TOL, form=2, solver=sv,
+                                                      inner_it=RESTART, outer_it=200)
+            torch.cuda.synchronize()
+            tv = time.perf_counter() - t0
+            variants["bicgstab" if sv == "B" else "pgmresDR"] = {
+                "flag": fv, "relres": rv, "iter": itv, "seconds": round(tv, 4),
+                "field_rel_err_vs_fp64_gmres": float((torch.linalg.norm(Jv - J64) / torch.linalg.norm(J64)).item())}
+
         # --- matvec times on the solver's DOFs ------------------------------
         mv = matvec_times(mg, op, op64, er, lib)
 
@@ -239,12 +273,13 @@ def run_gpu(args, world, rank, local):
                       "fp64": {"flag": flag64, "relres": relres64, "iter": it64, "iterations": n_it64,
                                "seconds": round(t64, 4), "solves_per_s": round(1 / t64, 4)},
                       "speedup_mixed_vs_fp64": round(t64 / (ms_per_step / 1e3), 3),
-                      "field_rel_err_mixed_vs_fp64": field_err},
+                      "field_rel_err_mixed_vs_fp64": field_err, "mixed_other_solvers": variants},
             "matvec_ms": {"fp32": mv["fp32_ms"], "fp64": mv["fp64_ms"], "fp32_passes_ms": mv["fp32_passes"],
                           "fp64_passes_ms": mv["fp64_passes"]},
             "assembly_s": round(t_asm, 3),
             "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": round(dom["gbs"], 1), "peak": hbm,
-                         "unit": "GB/s", "frac": round(dom["gbs"] / hbm, 4), "traffic": None,
+                         "unit": "GB/s", "frac": round(dom["gbs"] / hbm, 4),
+                         "traffic": zmul_traffic() if dom["name"] == "z_multiply" else None,
                          "peak_kind": kind, "alg_bytes_per_launch": dom["bytes"]},
             "matvec_roofline": {"alg_bytes": mv["alg_bytes"], "gbs": round(mv["alg_bytes"] / (mv["fp32_ms"] / 1e3) / 1e9, 1),
                                 "frac": round(mv["alg_bytes"] / (mv["fp32_ms"] / 1e3) / 1e9 / hbm, 4)},
@@ -427,7 +462,7 @@ def run_extra(args):
         E, _ = mg.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
         for prec in ("fp64", "mixed"):
             op = mg.Operator.assemble(Lc, Lc, Lc, dx, FREQ, precision=prec)
-            t, out = _timed(lambda: mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-6), args.steps, args.warmup)
+            t, out = _timed(lambda: mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-6, solver="G"), args.steps, args.warmup)
             res[prec] = {"seconds": t, "iter": out[3], "relres": out[2], "matvecs": len(out[4]) - 1}
             if prec == "fp64":
                 Et = mg.E_field_Nop(out[0], op, dx**3, FREQ, E)
@@ -495,6 +530,7 @@ def main():
     ap.add_argument("--impl", default="marie", choices=["marie", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--solve-only", action="store_true", help="run the mixed solves only (for profilers)")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     args = ap.parse_args()
     world, rank, local = dist_init()

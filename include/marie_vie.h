@@ -131,16 +131,49 @@ int marie_pgmres(marie_plan* plan, marie_op_fn A, void* A_ctx, const double* b, 
                  void* R2_ctx, const double* x0, double* x, int* flag, double* relres,
                  int* iter, double* resvec, int64_t resvec_cap, int64_t* resvec_len);
 
-/* Replaces JVIE_Solver(Einc, e_r, r, freq, fN, tol, form, solver, precond, ...)
- * (src_vie/src_solver/JVIE_Solver.m:1-521) with solver 'G' (pgmres) using the
- * plan's operator.  Einc: L x M x N x 3, e_r: L x M x N (complex), dx the voxel
- * edge.  form 1 or 2; precond 0, 'L' or 'R'.  With a MARIE_MIXED plan the
- * matvec runs in FP32 inside FP64 GMRES, refined by FP64 true residuals until
- * relres <= tol.  Je: L x M x N x 3.  iter = {inner, outer}. */
+/* Replaces pgmresDR(A, b, restart, tol, maxit, ritz, L1, L2, R1, R2, x0)
+ * (src_numeric/src_iterative/pgmresDR.m:1-282, pgmresDR_iter.m:1-142,
+ * getHarmVecs1.m, getHarmVecs2.m): GMRES(restart) that deflates ritz harmonic
+ * Ritz vectors of each cycle into the next (ritz < 1: min(10, restart/2);
+ * restart + ritz <= 127).  Arguments and outputs as marie_pgmres. */
+int marie_pgmres_dr(marie_plan* plan, marie_op_fn A, void* A_ctx, const double* b, int64_t n,
+                    int restart, double tol, int maxit, int ritz, marie_op_fn L1, void* L1_ctx,
+                    marie_op_fn L2, void* L2_ctx, marie_op_fn R1, void* R1_ctx, marie_op_fn R2,
+                    void* R2_ctx, const double* x0, double* x, int* flag, double* relres,
+                    int* iter, double* resvec, int64_t resvec_cap, int64_t* resvec_len);
+
+/* Replaces MATLAB's bicgstab(A, b, tol, maxit, M1, M2, x0), the solver 'B'
+ * of JVIE_Solver.m:451-499 (a MATLAB built-in, outside the reference
+ * sources): BiCGSTAB with MATLAB's outputs.  Vectors device or host (n
+ * complex); A/M1/M2 receive device vectors, M1/M2 applied as ph = M2(M1(p)),
+ * NULL = none; NULL x0 = zero start.  flag 0 converged / 1 maxit / 2
+ * preconditioner output not finite / 3 stagnation / 4 breakdown; iter in half
+ * steps; resvec the absolute residual norms (initial, then one per half
+ * step). */
+int marie_bicgstab(marie_plan* plan, marie_op_fn A, void* A_ctx, const double* b, int64_t n,
+                   double tol, int maxit, marie_op_fn M1, void* M1_ctx, marie_op_fn M2,
+                   void* M2_ctx, const double* x0, double* x, int* flag, double* relres,
+                   double* iter, double* resvec, int64_t resvec_cap, int64_t* resvec_len);
+
+/* Replaces JVIE_Solver(Einc, e_r, r, freq, fN, tol, form, solver, precond,
+ * max_it, inner_it, outer_it, ritz, gpu_flag) (src_vie/src_solver/
+ * JVIE_Solver.m:1-521) with the plan's operator.  Einc: L x M x N x 3, e_r:
+ * L x M x N (complex), dx the voxel edge (r enters only through dx).
+ * Arguments are clamped as JVIE_Solver.m:71-122 does: tol outside
+ * [1e-15, 1) -> 1e-3; form 1 or 2; solver 'G' (pgmres with restart
+ * inner_it and outer_it cycles), 'D' (pgmresDR, deflating ritz harmonic Ritz
+ * vectors) or anything else 'B' (bicgstab with max_it iterations); precond 0,
+ * 'L' or 'R' (bicgstab takes either as its M1).  With a MARIE_MIXED plan the
+ * circulant part of every Krylov matvec runs in FP32 inside FP64 iterations,
+ * refined by FP64 true residuals until relres <= tol.  Je: L x M x N x 3.
+ * iter: 2 doubles, {inner, outer} for 'G' and 'D', {iterations, 0} for 'B'
+ * (half steps count 0.5).  resvec as the solver returns it: relative for 'G'
+ * and 'D', absolute for 'B'. */
 int marie_jvie_solve(marie_plan* plan, const double* Einc, const double* e_r, double dx,
-                     double freq, int form, char precond, double tol, int inner_it,
-                     int outer_it, double* Je, int* flag, double* relres, int* iter,
-                     double* resvec, int64_t resvec_cap, int64_t* resvec_len, double* solvert);
+                     double freq, double tol, int form, char solver, char precond, int max_it,
+                     int inner_it, int outer_it, int ritz, double* Je, int* flag, double* relres,
+                     double* iter, double* resvec, int64_t resvec_cap, int64_t* resvec_len,
+                     double* solvert);
 
 /* JVIE_Solver for nexc excitations of one body solved together: Einc and Je
  * are nexc consecutive L x M x N x 3 arrays; the solves advance in lockstep

@@ -52,8 +52,14 @@ SIGNATURES = {
     "marie_pgmres": (C.c_int, [_vp, OP_FN, _vp, _vp, C.c_int64, C.c_int, C.c_double, C.c_int,
                                OP_FN, _vp, OP_FN, _vp, OP_FN, _vp, OP_FN, _vp,
                                _vp, _vp, _ip, _dp, _ip, _dp, C.c_int64, _i64p]),
-    "marie_jvie_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_int, C.c_char, C.c_double,
-                                   C.c_int, C.c_int, _vp, _ip, _dp, _ip, _dp, C.c_int64, _i64p, _dp]),
+    "marie_pgmres_dr": (C.c_int, [_vp, OP_FN, _vp, _vp, C.c_int64, C.c_int, C.c_double, C.c_int, C.c_int,
+                                  OP_FN, _vp, OP_FN, _vp, OP_FN, _vp, OP_FN, _vp,
+                                  _vp, _vp, _ip, _dp, _ip, _dp, C.c_int64, _i64p]),
+    "marie_bicgstab": (C.c_int, [_vp, OP_FN, _vp, _vp, C.c_int64, C.c_double, C.c_int, OP_FN, _vp, OP_FN, _vp,
+                                 _vp, _vp, _ip, _dp, _dp, _dp, C.c_int64, _i64p]),
+    "marie_jvie_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_char, C.c_char,
+                                   C.c_int, C.c_int, C.c_int, C.c_int, _vp, _ip, _dp, _dp, _dp, C.c_int64, _i64p,
+                                   _dp]),
     "marie_jvie_solve_bodies": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, C.c_char,
                                           C.c_double, C.c_int, C.c_int, _vp, _ip, _dp, _ip, _dp]),
     "marie_jvie_adjoint_grad": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_int, _vp, C.c_double, C.c_int,

@@ -1,5 +1,6 @@
-// JVIE_Solver (src_vie/src_solver/JVIE_Solver.m:1-521, solver 'G') on the
-// device, for one excitation or a batch of excitations of one body:
+// JVIE_Solver (src_vie/src_solver/JVIE_Solver.m:1-521) on the device, for one
+// excitation (solvers 'G' pgmres, 'D' pgmresDR, 'B' bicgstab) or a batch of
+// excitations of one body (lockstep pgmres):
 //   set-up (JVIE_Solver.m:131-156, 242-244): non-air voxel compaction, the
 //   local DOF order [idxS; V+idxS; 2V+idxS], the right-hand sides
 //   Gram*j*omega*eps0*Mc*Einc, the form-2 scaling, the preconditioner
@@ -9,7 +10,8 @@
 // arithmetic); MARIE_MIXED plans run GMRES-IR: the inner pgmres uses the FP32
 // circulant matvec (Krylov basis, Arnoldi, Givens and the diagonal Gram*Mr
 // term in FP64) and the outer loop refines with FP64 true residuals until
-// ||b - A x|| / ||b|| <= tol.
+// ||b - A x|| / ||b|| <= tol.  The single-excitation solvers 'B' and 'D' refine
+// the same way around an FP32-matvec bicgstab / pgmresDR.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -254,26 +256,40 @@ static BatchOp make_bop(marie_plan* p, int prec, const JvieState& S, const doubl
 
 struct SolveOut {
   std::vector<GmresResult> r;
+  BicgResult b;      // solver 'B'
+  char solver = 'G';
+};
+
+// Krylov choice of JVIE_Solver.m:86-93, 300-499 for one excitation.
+struct SolverArgs {
+  char solver = 'G';  // 'G', 'D' or 'B'
+  int max_it = 1000;  // bicgstab iterations
+  int ritz = 5;       // pgmresDR deflation vectors
 };
 
 static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, int S_exc, double2* X, char precond,
                          double tol, int inner_it, int outer_it, SolveOut& out);
+static int solve_single(marie_plan* p, const JvieState& S, const double2* Bv, double2* X, char precond, double tol,
+                        int inner_it, int outer_it, const SolverArgs& sa, SolveOut& out);
 
 // Solves the S excitations E (3V x S, column stride es) of one body.
 static int jvie_solve_core(marie_plan* p, const double2* E, long long es, int S_exc, const double2* er, double dx,
                            double freq, int form, char precond, double tol, int inner_it, int outer_it, double2* Je,
-                           long long js, SolveOut& out) {
+                           long long js, SolveOut& out, const SolverArgs& sa = SolverArgs()) {
   cudaStream_t st = p->stream;
   const long long V = p->d.V;
   JvieState S;
   MARIE_TRY(jvie_setup(p, er, dx, freq, form, S));
   for (int e = 0; e < S_exc; ++e) MARIE_CUDA_TRY(cudaMemsetAsync(Je + e * js, 0, 3 * V * sizeof(double2), st));
   out.r.assign(S_exc, GmresResult());
+  out.solver = sa.solver;
   if (S.n == 0) {
     for (auto& r : out.r) {
       r.flag = 0;
       r.relres = 0;
     }
+    out.b.flag = 0;
+    out.b.relres = 0;
     return MARIE_OK;
   }
   const long long n = S.n;
@@ -283,7 +299,10 @@ static int jvie_solve_core(marie_plan* p, const double2* E, long long es, int S_
   k_jvie_rhs<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(S.f.as<double2>(), S.idx3.as<int64_t>(), n, E, es,
                                                       rhs.as<double2>());
   count_launch();
-  MARIE_TRY(solve_systems(p, S, rhs.as<double2>(), S_exc, x.as<double2>(), precond, tol, inner_it, outer_it, out));
+  if (sa.solver == 'G')
+    MARIE_TRY(solve_systems(p, S, rhs.as<double2>(), S_exc, x.as<double2>(), precond, tol, inner_it, outer_it, out));
+  else
+    MARIE_TRY(solve_single(p, S, rhs.as<double2>(), x.as<double2>(), precond, tol, inner_it, outer_it, sa, out));
   k_scatter_dofs<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(x.as<double2>(), S.idx3.as<int64_t>(), n, Je, js);
   count_launch();
   MARIE_CUDA_TRY(cudaGetLastError());
@@ -372,6 +391,94 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
   return MARIE_OK;
 }
 
+static DevOp single(const BatchOp& op, long long n) {
+  return [op, n](const double2* x, double2* y) -> int { return op.apply(x, n, y, n, 1, nullptr, 0); };
+}
+
+// One excitation with bicgstab ('B', JVIE_Solver.m:451-499: the preconditioner,
+// 'L' or 'R' alike, is bicgstab's M1) or pgmresDR ('D', :400-446).  MARIE_MIXED
+// plans refine: FP32-matvec solves of A d = r, x += d, FP64 r = b - A x.
+static int solve_single(marie_plan* p, const JvieState& S, const double2* Bv, double2* X, char precond, double tol,
+                        int inner_it, int outer_it, const SolverArgs& sa, SolveOut& out) {
+  cudaStream_t st = p->stream;
+  const long long n = S.n;
+  bool pb_nz = true;
+  MARIE_TRY(any_nonzero(p, S.pb.as<double2>(), n, &pb_nz));
+  const int prec_main = (p->precision == MARIE_FP32) ? MARIE_FP32 : MARIE_FP64;
+  const DevOp A64 = single(make_bop(p, prec_main, S, S.a.as<double2>(), S.b.as<double2>(), false), n);
+  const DevOp P64 = single(make_bop(p, prec_main, S, S.pa.as<double2>(), S.pb.as<double2>(), !pb_nz), n);
+  auto run = [&](const DevOp& A, const DevOp& P, const double2* b, double t, double2* x, BicgResult& rb,
+                 GmresResult& rg) -> int {
+    if (sa.solver == 'B') return bicgstab(p, A, precond ? &P : nullptr, nullptr, b, n, t, sa.max_it, nullptr, x, rb);
+    const DevOp* L1 = precond == 'L' ? &P : nullptr;
+    const DevOp* R1 = precond == 'R' ? &P : nullptr;
+    return gmres_dr(p, A, L1, nullptr, R1, nullptr, b, n, inner_it, t, outer_it, sa.ritz, nullptr, x, rg);
+  };
+  if (p->precision != MARIE_MIXED) {
+    GmresResult rg;
+    MARIE_TRY(run(A64, P64, Bv, tol, X, out.b, rg));
+    out.r[0] = rg;
+    return MARIE_OK;
+  }
+  const DevOp A32 = single(make_bop(p, MARIE_FP32, S, S.a.as<double2>(), S.b.as<double2>(), false), n);
+  const DevOp P32 = single(make_bop(p, MARIE_FP32, S, S.pa.as<double2>(), S.pb.as<double2>(), !pb_nz), n);
+  DBuf rb, db, one;
+  MARIE_TRY(rb.alloc((size_t)n * sizeof(double2), st));
+  MARIE_TRY(db.alloc((size_t)n * sizeof(double2), st));
+  MARIE_TRY(one.alloc(sizeof(int), st));
+  const int on = 1;
+  MARIE_CUDA_TRY(cudaMemcpyAsync(one.p, &on, sizeof(int), cudaMemcpyHostToDevice, st));
+  double2* Rr = rb.as<double2>();
+  double2* D = db.as<double2>();
+  MARIE_CUDA_TRY(cudaMemsetAsync(X, 0, (size_t)n * sizeof(double2), st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(Rr, Bv, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  double bn = 0;
+  MARIE_TRY(dev_norm2(p, Bv, n, &bn));
+  double rn = bn;
+  BicgResult& B = out.b;
+  GmresResult& G = out.r[0];
+  B = BicgResult();
+  G = GmresResult();
+  B.resvec.push_back(bn);
+  G.resvec.push_back(1.0);
+  double biter = 0;
+  int inner_total = 0, last_p = 0, last_flag = 1;
+  for (int it = 0; it < 20 && rn > tol * bn; ++it) {
+    // half of what is still missing, not below the FP32 floor
+    const double inner_tol = std::max(0.5 * tol * bn / rn, 1e-5);
+    BicgResult ib;
+    GmresResult ig;
+    MARIE_TRY(run(A32, P32, Rr, inner_tol, D, ib, ig));
+    k_add_b<<<dim3(grid_n(n), 1), 256, 0, st>>>(D, X, n, one.as<int>());
+    count_launch();
+    MARIE_TRY(A64(X, Rr));
+    k_sub_b<<<dim3(grid_n(n), 1), 256, 0, st>>>(Bv, Rr, n, one.as<int>());
+    count_launch();
+    MARIE_CUDA_TRY(cudaGetLastError());
+    const double rprev = rn;
+    MARIE_TRY(dev_norm2(p, Rr, n, &rn));
+    if (sa.solver == 'B') {
+      for (size_t i = 1; i < ib.resvec.size(); ++i) B.resvec.push_back(ib.resvec[i]);
+      B.resvec.push_back(rn);
+      biter += ib.iter;
+      last_flag = ib.flag;
+    } else {
+      for (size_t i = 1; i < ig.resvec.size(); ++i) G.resvec.push_back(ig.resvec[i] * rprev / bn);
+      G.resvec.push_back(rn / bn);
+      inner_total += ig.iter[1];
+      last_p = ig.iter[0];
+    }
+    if (!std::isfinite(rn)) return set_error(MARIE_EBREAKDOWN, "non-finite residual in the refinement");
+  }
+  const int fl = rn <= tol * bn ? 0 : (sa.solver == 'B' && last_flag > 1 ? last_flag : 1);
+  B.flag = G.flag = fl;
+  B.relres = G.relres = rn / bn;
+  B.iter = biter;
+  G.iter[0] = last_p;
+  G.iter[1] = inner_total;
+  return MARIE_OK;
+}
+
 // adjoint-gradient kernels (adjoint.cu)
 __global__ void k_adj_fields(const double2* __restrict__ J, const int64_t* __restrict__ idx3, long long n,
                              long long V, const double2* __restrict__ er, double omega_eps0, int objective,
@@ -454,19 +561,35 @@ static int clamp_args(double& tol, int& form, char& precond, int& inner_it, int&
   return MARIE_OK;
 }
 
+// solver ('G', 'D', else 'B'), max_it (default 1000), ritz (default 5):
+// JVIE_Solver.m:86-93, 99-101, 108-110
+static void clamp_solver(SolverArgs& sa, int inner_it) {
+  if (sa.solver != 'G' && sa.solver != 'D') sa.solver = 'B';
+  if (sa.max_it < 1) sa.max_it = 1000;
+  if (sa.ritz < 1) sa.ritz = 5;
+  // pgmresDR.m:55-60
+  if (sa.ritz > inner_it - 1) sa.ritz = inner_it - 1;
+}
+
 }  // namespace marie
 
 using namespace marie;
 
 extern "C" {
 
-int marie_jvie_solve(marie_plan* p, const double* Einc, const double* e_r, double dx, double freq, int form,
-                     char precond, double tol, int inner_it, int outer_it, double* Je, int* flag, double* relres,
-                     int* iter, double* resvec, int64_t resvec_cap, int64_t* resvec_len, double* solvert) {
+int marie_jvie_solve(marie_plan* p, const double* Einc, const double* e_r, double dx, double freq, double tol,
+                     int form, char solver, char precond, int max_it, int inner_it, int outer_it, int ritz,
+                     double* Je, int* flag, double* relres, double* iter, double* resvec, int64_t resvec_cap,
+                     int64_t* resvec_len, double* solvert) {
   if (!p || !Einc || !e_r || !Je) return set_error(MARIE_EINVAL, "NULL argument");
   if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator");
   if (!(dx > 0) || !(freq > 0)) return set_error(MARIE_EINVAL, "dx and freq must be positive");
   MARIE_TRY(clamp_args(tol, form, precond, inner_it, outer_it));
+  SolverArgs sa;
+  sa.solver = solver;
+  sa.max_it = max_it;
+  sa.ritz = ritz;
+  clamp_solver(sa, inner_it);
   const auto t0 = std::chrono::steady_clock::now();
   cudaStream_t st = p->stream;
   const long long V = p->d.V;
@@ -478,20 +601,22 @@ int marie_jvie_solve(marie_plan* p, const double* Einc, const double* e_r, doubl
   MARIE_TRY(stage_out(Je, 3 * V * sizeof(double2), st, tJe, &Je_d));
   SolveOut so;
   MARIE_TRY(jvie_solve_core(p, (const double2*)E_d, 3 * V, 1, (const double2*)er_d, dx, freq, form, precond, tol,
-                            inner_it, outer_it, (double2*)Je_d, 3 * V, so));
+                            inner_it, outer_it, (double2*)Je_d, 3 * V, so, sa));
   MARIE_TRY(finish_out(Je, Je_d, 3 * V * sizeof(double2), st));
   MARIE_CUDA_TRY(cudaStreamSynchronize(st));
   const auto t1 = std::chrono::steady_clock::now();
+  const bool bi = sa.solver == 'B';
   const GmresResult& R = so.r[0];
-  if (flag) *flag = R.flag;
-  if (relres) *relres = R.relres;
+  const std::vector<double>& rv = bi ? so.b.resvec : R.resvec;
+  if (flag) *flag = bi ? so.b.flag : R.flag;
+  if (relres) *relres = bi ? so.b.relres : R.relres;
   if (iter) {
-    iter[0] = R.iter[0];
-    iter[1] = R.iter[1];
+    iter[0] = bi ? so.b.iter : R.iter[0];
+    iter[1] = bi ? 0.0 : R.iter[1];
   }
-  if (resvec_len) *resvec_len = (int64_t)R.resvec.size();
+  if (resvec_len) *resvec_len = (int64_t)rv.size();
   if (resvec)
-    for (int64_t i = 0; i < (int64_t)R.resvec.size() && i < resvec_cap; ++i) resvec[i] = R.resvec[i];
+    for (int64_t i = 0; i < (int64_t)rv.size() && i < resvec_cap; ++i) resvec[i] = rv[i];
   if (solvert) *solvert = std::chrono::duration<double>(t1 - t0).count();
   return MARIE_OK;
 }

@@ -119,6 +119,23 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
                 std::vector<GmresResult>& out, bool use_graph, const std::vector<int>* active_in,
                 bool true_residual);
 
+// MATLAB bicgstab semantics (the solver 'B' of JVIE_Solver.m:451-499) on
+// device vectors: iter in half steps, resvec absolute (bicgstab.cu).
+struct BicgResult {
+  int flag = 1;
+  double relres = 0;
+  double iter = 0;
+  std::vector<double> resvec;
+};
+int bicgstab(marie_plan* p, const DevOp& A, const DevOp* M1, const DevOp* M2, const double2* b, long long n,
+             double tol, int maxit, const double2* x0, double2* x, BicgResult& out);
+
+// pgmresDR semantics (pgmresDR.m, pgmresDR_iter.m: GMRES with deflated
+// restarting by ritz harmonic Ritz vectors) on device vectors (gmres_dr.cu).
+int gmres_dr(marie_plan* p, const DevOp& A, const DevOp* L1, const DevOp* L2, const DevOp* R1, const DevOp* R2,
+             const double2* b, long long n, int restart, double tol, int maxit, int ritz, const double2* x0,
+             double2* x, GmresResult& res);
+
 // pgmres semantics (pgmres.m:70-181) on device vectors.
 int gmres(marie_plan* p, const DevOp& A, const DevOp* L1, const DevOp* L2, const DevOp* R1, const DevOp* R2,
           const double2* b, long long n, int restart, double tol, int maxit, const double2* x0, double2* x,

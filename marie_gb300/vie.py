@@ -9,6 +9,9 @@ argument order, defaults and return tuples:
     mv_L(JIn0, fN, r, Gram, idx, GPU_flag)       src_vie/src_mvp/mv_L.m:1
     pgmres(A, b, restart, tol, maxit, L1, L2, R1, R2, x0)
                                                  src_numeric/src_iterative/pgmres.m:70
+    pgmresDR(A, b, restart, tol, maxit, ritz, L1, L2, R1, R2, x0)
+                                                 src_numeric/src_iterative/pgmresDR.m:1
+    bicgstab(A, b, tol, maxit, M1, M2, x0)       MATLAB built-in, JVIE_Solver.m:451-499
     JVIE_Solver(Einc, e_r, r, freq, fN, tol, form, solver, precond, max_it,
                 inner_it, outer_it, ritz, gpu_flag, logfile)
                                                  src_vie/src_solver/JVIE_Solver.m:1
@@ -310,68 +313,119 @@ def _vector_plan():
     return _vec_plan
 
 
+def _handles(A, others, host):
+    cbs = [_wrap_handle(A, host)]
+    slots = []
+    for h in others:
+        if h is None:
+            slots.append(_lib.OP_FN())
+        else:
+            f = _wrap_handle(h, host)
+            cbs.append(f)
+            slots.append(f)
+    return cbs, slots
+
+
+def _call(lib_fn, *args):
+    _wrap_handle.last_exc = None
+    st = lib_fn(*args)
+    if st != 0 and _wrap_handle.last_exc is not None:
+        raise _wrap_handle.last_exc
+    check(st)
+
+
 def pgmres(A, b, restart=50, tol=1e-3, maxit=10, L1=None, L2=None, R1=None, R2=None, x0=None):
     """pgmres.m:70-181 on the device.  A, L1, L2, R1, R2 are function handles
     (preconditioners are applied as products, like the reference).  With a
     numpy b the handles receive and return numpy vectors; with a CUDA tensor b
     they receive and return CUDA tensors.  Returns (x, flag, relres, iter, resvec)."""
-    if restart is None:
-        restart = 50
-    if tol is None:
-        tol = 1e-3
-    if maxit is None:
-        maxit = 10
+    restart = 50 if restart is None else restart
+    tol = 1e-3 if tol is None else tol
+    maxit = 10 if maxit is None else maxit
     host = not _is_cuda(b)
     opr = _vector_plan()
-    lib = opr.lib
     n = b.shape[0]
-    cbs = [_wrap_handle(A, host)]
-    nulls = []
-    for h in (L1, L2, R1, R2):
-        if h is None:
-            nulls.append(_lib.OP_FN())
-        else:
-            f = _wrap_handle(h, host)
-            cbs.append(f)
-            nulls.append(f)
+    cbs, h = _handles(A, (L1, L2, R1, R2), host)
     bp, bk = _in(b)
     x0p, x0k = _in(x0) if x0 is not None else (None, None)
     xp, x = _out((n,), not host)
-    flag = C.c_int()
-    relres = C.c_double()
-    it = (C.c_int * 2)()
+    flag, relres, it = C.c_int(), C.c_double(), (C.c_int * 2)()
     cap = restart * maxit + 1
     resvec = np.zeros(cap)
     rlen = C.c_int64()
-    _wrap_handle.last_exc = None
-    st = lib.marie_pgmres(opr.plan, cbs[0], None, bp, n, int(restart), float(tol), int(maxit),
-                          nulls[0], None, nulls[1], None, nulls[2], None, nulls[3], None,
-                          x0p, xp, C.byref(flag), C.byref(relres), it, resvec.ctypes.data_as(_lib._dp), cap,
-                          C.byref(rlen))
-    if st != 0 and _wrap_handle.last_exc is not None:
-        raise _wrap_handle.last_exc
-    check(st)
+    _call(opr.lib.marie_pgmres, opr.plan, cbs[0], None, bp, n, int(restart), float(tol), int(maxit),
+          h[0], None, h[1], None, h[2], None, h[3], None, x0p, xp, C.byref(flag), C.byref(relres), it,
+          resvec.ctypes.data_as(_lib._dp), cap, C.byref(rlen))
     return x, flag.value, relres.value, [it[0], it[1]], resvec[:rlen.value]
+
+
+def pgmresDR(A, b, restart=50, tol=1e-3, maxit=10, ritz=None, L1=None, L2=None, R1=None, R2=None, x0=None):
+    """pgmresDR.m (GMRES with deflated restarting by ritz harmonic Ritz
+    vectors) on the device; handles and returns as pgmres."""
+    restart = 50 if restart is None else restart
+    tol = 1e-3 if tol is None else tol
+    maxit = 10 if maxit is None else maxit
+    host = not _is_cuda(b)
+    opr = _vector_plan()
+    n = b.shape[0]
+    cbs, h = _handles(A, (L1, L2, R1, R2), host)
+    bp, bk = _in(b)
+    x0p, x0k = _in(x0) if x0 is not None else (None, None)
+    xp, x = _out((n,), not host)
+    flag, relres, it = C.c_int(), C.c_double(), (C.c_int * 2)()
+    cap = restart * (maxit + 1) + 1
+    resvec = np.zeros(cap)
+    rlen = C.c_int64()
+    _call(opr.lib.marie_pgmres_dr, opr.plan, cbs[0], None, bp, n, int(restart), float(tol), int(maxit),
+          int(ritz) if ritz is not None else 0, h[0], None, h[1], None, h[2], None, h[3], None, x0p, xp,
+          C.byref(flag), C.byref(relres), it, resvec.ctypes.data_as(_lib._dp), cap, C.byref(rlen))
+    return x, flag.value, relres.value, [it[0], it[1]], resvec[:rlen.value]
+
+
+def bicgstab(A, b, tol=1e-6, maxit=None, M1=None, M2=None, x0=None):
+    """MATLAB's bicgstab (the solver 'B' of JVIE_Solver.m:451-499) on the
+    device; M1, M2 are function handles applied as ph = M2(M1(p)).  Returns
+    (x, flag, relres, iter, resvec): iter in half steps, resvec absolute."""
+    tol = 1e-6 if tol is None else tol
+    n = b.shape[0]
+    maxit = min(n, 20) if maxit is None else maxit
+    host = not _is_cuda(b)
+    opr = _vector_plan()
+    cbs, h = _handles(A, (M1, M2), host)
+    bp, bk = _in(b)
+    x0p, x0k = _in(x0) if x0 is not None else (None, None)
+    xp, x = _out((n,), not host)
+    flag, relres, it = C.c_int(), C.c_double(), C.c_double()
+    cap = 2 * maxit + 1
+    resvec = np.zeros(cap)
+    rlen = C.c_int64()
+    _call(opr.lib.marie_bicgstab, opr.plan, cbs[0], None, bp, n, float(tol), int(maxit), h[0], None, h[1], None,
+          x0p, xp, C.byref(flag), C.byref(relres), C.byref(it), resvec.ctypes.data_as(_lib._dp), cap,
+          C.byref(rlen))
+    return x, flag.value, relres.value, it.value, resvec[:rlen.value]
 
 
 # ---------------------------------------------------------------------------
 # JVIE_Solver
 # ---------------------------------------------------------------------------
-def JVIE_Solver(Einc, e_r, r, freq, fN, tol=None, form=None, solver="G", precond=None, max_it=None, inner_it=None,
+def JVIE_Solver(Einc, e_r, r, freq, fN, tol=None, form=None, solver=None, precond=None, max_it=None, inner_it=None,
                 outer_it=None, ritz=None, gpu_flag=1, logfile=None, precision=None):
-    """JVIE_Solver.m with solver 'G' (restarted GMRES) on the device.
+    """JVIE_Solver.m on the device: solver 'G' (pgmres), 'D' (pgmresDR) or,
+    as in the reference, anything else (the default) 'B' (bicgstab).
 
     fN is an Operator (or a 2L x 2M x 2N x 6 array).  precision: 'fp64' (the
     reference arithmetic), 'fp32', or 'mixed' (FP32 circulant matvec inside FP64
-    GMRES with FP64 iterative refinement); defaults to the Operator's.
-    Returns (Je, flag, relres, iter, resvec, solvert)."""
-    if solver not in ("G", None):
-        raise NotImplementedError("only solver 'G' (pgmres) is on this path")
+    Krylov iterations with FP64 iterative refinement); defaults to the
+    Operator's.  Returns (Je, flag, relres, iter, resvec, solvert): iter is
+    [inner, outer] for 'G' and 'D' and the half-step count for 'B'."""
     tol = 1e-3 if tol is None else tol
     form = 2 if form is None else form
+    solver = solver if solver in ("G", "D") else "B"
     pc = {None: b"\0", 0: b"\0", "L": b"L", "R": b"R"}.get(precond, b"\0")
+    max_it = 1000 if max_it is None else max_it
     inner_it = 50 if inner_it is None or inner_it < 1 else inner_it
     outer_it = 200 if outer_it is None or outer_it < 1 else outer_it
+    ritz = 5 if ritz is None or ritz < 1 else ritz
     if isinstance(fN, Operator):
         opr, tmp = fN, False
         if precision is not None and _PREC[precision] != opr.precision:
@@ -387,15 +441,17 @@ def JVIE_Solver(Einc, e_r, r, freq, fN, tol=None, form=None, solver="G", precond
         jp, Je = _out((L, M, N, 3), cuda)
         flag = C.c_int()
         relres = C.c_double()
-        it = (C.c_int * 2)()
-        cap = 1 + inner_it * outer_it * 4
+        it = (C.c_double * 2)()
+        cap = 1 + max(inner_it * (outer_it + 1) * 4, 2 * max_it * 4)
         resvec = np.zeros(cap)
         rlen = C.c_int64()
         solvert = C.c_double()
-        check(opr.lib.marie_jvie_solve(opr.plan, ep, erp, dx, float(freq), int(form), pc, float(tol), int(inner_it),
-                                       int(outer_it), jp, C.byref(flag), C.byref(relres), it,
-                                       resvec.ctypes.data_as(_lib._dp), cap, C.byref(rlen), C.byref(solvert)))
-        return Je, flag.value, relres.value, [it[0], it[1]], resvec[:min(rlen.value, cap)], solvert.value
+        check(opr.lib.marie_jvie_solve(opr.plan, ep, erp, dx, float(freq), float(tol), int(form), solver.encode(), pc,
+                                       int(max_it), int(inner_it), int(outer_it), int(ritz), jp, C.byref(flag),
+                                       C.byref(relres), it, resvec.ctypes.data_as(_lib._dp), cap, C.byref(rlen),
+                                       C.byref(solvert)))
+        iters = it[0] if solver == "B" else [int(it[0]), int(it[1])]
+        return Je, flag.value, relres.value, iters, resvec[:min(rlen.value, cap)], solvert.value
     finally:
         if tmp:
             opr.close()

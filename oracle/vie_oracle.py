@@ -177,6 +177,286 @@ def pgmres(A, b, restart=50, tol=1e-3, maxit=10, L1=None, L2=None, R1=None, R2=N
 
 
 # ---------------------------------------------------------------------------
+# GMRES with deflated restarting: src_numeric/src_iterative/pgmresDR.m:84-282,
+# pgmresDR_iter.m:36-142, getHarmVecs1.m, getHarmVecs2.m
+# ---------------------------------------------------------------------------
+def _lsq(A, b):
+    """MATLAB A \\ b for a tall full-rank A (least squares)."""
+    return np.linalg.lstsq(A, b, rcond=None)[0]
+
+
+def pgmresDR_iter(A, r, m, L1, L2, R1, R2, C, tol):
+    """pgmresDR_iter.m:76-142: GMRES cycle on A R1 R2 (left L1, L2) with the
+    Krylov vectors kept orthogonal to the columns of C (B = C' w).  Returns
+    (V, H, B, k, resvec) truncated to the k steps taken."""
+    n = r.shape[0]
+    V = np.zeros((n, m + 1), dtype=complex)
+    nr = np.linalg.norm(r)
+    V[:, 0] = r / nr
+    nc = 0 if C is None else C.shape[1]
+    Bm = np.zeros((nc, m), dtype=complex)
+    H = np.zeros((m + 1, m), dtype=complex)
+    resvec = np.zeros(m)
+    k = 0
+    for k in range(1, m + 1):
+        w = V[:, k - 1]
+        if R2 is not None:
+            w = R2(w)
+        if R1 is not None:
+            w = R1(w)
+        w = A(w)
+        if L1 is not None:
+            w = L1(w)
+        if L2 is not None:
+            w = L2(w)
+        if nc:
+            Bm[:, k - 1] = C.conj().T @ w
+            w = w - C @ Bm[:, k - 1]
+        H[:k, k - 1] = V[:, :k].conj().T @ w
+        w = w - V[:, :k] @ H[:k, k - 1]
+        H[k, k - 1] = np.linalg.norm(w)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            V[:, k] = w / H[k, k - 1]
+        rhs = np.zeros(k + 1, dtype=complex)
+        rhs[0] = nr
+        Hc = H[:k + 1, :k]
+        res = rhs - Hc @ _lsq(Hc, rhs)
+        resvec[k - 1] = np.linalg.norm(res)
+        if resvec[k - 1] < tol:
+            return V[:, :k + 1], H[:k + 1, :k], Bm[:, :k], k, resvec[:k]
+    return V, H, Bm, k, resvec
+
+
+def _sorted_eig(evals, evecs):
+    """Eigenpairs ordered by ascending |eigenvalue| (the sortrows on
+    [abs(diag(D)) V'] of getHarmVecs1.m:25-27 / getHarmVecs2.m:31-33)."""
+    order = np.argsort(np.abs(evals), kind="stable")
+    return evecs[:, order]
+
+
+def getHarmVecs1(m, k, H):
+    """getHarmVecs1.m:17-28: the k harmonic Ritz vectors of smallest |theta|
+    from H_m + h_{m+1,m}^2 f e_m^T with f = H_m^{-H} e_m."""
+    Hm = H[:m, :]
+    F = np.linalg.solve(Hm.conj().T, np.eye(m))
+    F[:, :m - 1] = 0
+    Mh = Hm + H[m, m - 1] ** 2 * F
+    evals, evecs = np.linalg.eig(Mh)
+    return _sorted_eig(evals, evecs)[:, :k]
+
+
+def getHarmVecs2(m, k, H2, V, U, C):
+    """getHarmVecs2.m:17-34: generalized problem (H2' W) g = theta (H2' H2) g,
+    W = [C'U, 0; V'U, I; 0 0]; the k eigenvectors of largest |theta|."""
+    import scipy.linalg
+
+    Bm = H2.conj().T @ H2
+    W = np.zeros((m + 1, m), dtype=complex)
+    W[:k, :k] = C.conj().T @ U
+    W[k:m + 1, :k] = V.conj().T @ U
+    W[k:m, k:m] = np.eye(m - k)
+    Am = H2.conj().T @ W
+    evals, evecs = scipy.linalg.eig(Am, Bm)
+    return _sorted_eig(evals, evecs)[:, m - k:]
+
+
+def pgmresDR(A, b, restart=50, tol=1e-3, maxit=10, ritz=None, L1=None, L2=None, R1=None, R2=None, x0=None):
+    """Returns (x, flag, relres, iter, resvec) like pgmresDR.m: GMRES(restart)
+    that carries ritz harmonic Ritz vectors of each cycle into the next."""
+    if ritz is None:
+        ritz = min(10, int(np.floor(restart / 2 + 0.5)))
+    else:
+        ritz = min(ritz, restart - 1)
+    if x0 is None:
+        x0 = np.zeros_like(b)
+    r = b - A(x0)
+    bp = b.copy()
+    if L1 is not None:
+        r = L1(r)
+        bp = L1(bp)
+    if L2 is not None:
+        r = L2(r)
+        bp = L2(bp)
+    bnorm = np.linalg.norm(bp)
+    resvec = [np.linalg.norm(r) / bnorm]
+    outit = 0
+    V, H, _, p, rin = pgmresDR_iter(A, r, restart, L1, L2, R1, R2, None, tol * bnorm)
+    resvec.extend(list(rin / bnorm))
+    y = _lsq(H, V.conj().T @ r)
+    x = V[:, :p] @ y
+    r = r - V @ (H @ y)
+    U = C = None
+    if resvec[-1] > tol:
+        P = getHarmVecs1(p, min(ritz, p - 1), H)
+        U = V[:, :p] @ P
+        Cq, R = np.linalg.qr(H @ P)
+        C = V @ Cq
+        U = np.linalg.solve(R.T, U.T).T  # U / R
+    while resvec[-1] > tol and outit < maxit:
+        outit += 1
+        V, H, Bm, p, rin = pgmresDR_iter(A, r, restart, L1, L2, R1, R2, C, tol * bnorm)
+        resvec.extend(list(rin / bnorm))
+        kr = U.shape[1]
+        d = np.linalg.norm(U, axis=0)
+        D = np.diag(1.0 / d)
+        U = U @ D
+        H2 = np.zeros((kr + H.shape[0], kr + H.shape[1]), dtype=complex)
+        H2[:kr, :kr] = D
+        H2[:kr, kr:] = Bm
+        H2[kr:, kr:] = H
+        CV = np.concatenate([C, V], axis=1)
+        y = _lsq(H2, CV.conj().T @ r)
+        x = x + np.concatenate([U, V[:, :p]], axis=1) @ y
+        r = r - CV @ (H2 @ y)
+        if resvec[-1] > tol:
+            P = getHarmVecs2(p + kr, kr, H2, V, U, C)
+            U = np.concatenate([U, V[:, :p]], axis=1) @ P
+            Q, R = np.linalg.qr(H2 @ P)
+            C = CV @ Q
+            U = np.linalg.solve(R.T, U.T).T
+    if R2 is not None:
+        x = R2(x)
+    if R1 is not None:
+        x = R1(x)
+    x = x0 + x
+    relres = np.linalg.norm(b - A(x)) / np.linalg.norm(b)
+    flag = 0 if relres <= tol else 1
+    return x, flag, relres, [p, outit], np.array(resvec)
+
+
+def bicgstab(A, b, tol=1e-6, maxit=None, M1=None, M2=None, x0=None):
+    """Returns (x, flag, relres, iter, resvec) like MATLAB's bicgstab, which
+    JVIE_Solver.m:451-499 calls for its default solver 'B'.
+
+    bicgstab is a MATLAB built-in (about R2014a, the release getOPERATORS.m:55
+    tests for), not part of the reference sources.  This restates the published
+    BiCGSTAB iteration (van der Vorst, SIAM J. Sci. Stat. Comput. 13, 1992) with
+    the documented MATLAB interface: preconditioner applied as ph = M2(M1(p))
+    (function handles), iter counted in half steps, resvec the absolute
+    residual norm after every half step (initial residual first), flag 0
+    converged / 1 maxit / 2 non-finite preconditioner output / 3 stagnation /
+    4 a breakdown scalar (rho, beta, r~'v, t't zero or infinite).  Convergence
+    reported by the recurrence is confirmed with a true residual b - A x, which
+    then replaces the recurrence residual; up to min(n/50, 5, n - maxit)
+    confirmations may fail before flag 3.  Without convergence the iterate with
+    the smallest residual norm is returned."""
+    n = b.size
+    maxit = min(n, 20) if maxit is None else int(maxit)
+    eps = np.finfo(float).eps
+    nrm = np.linalg.norm
+
+    def prec(v):
+        if M1 is not None:
+            v = M1(v)
+        if M2 is not None:
+            v = M2(v)
+        return v
+
+    nb = nrm(b)
+    if nb == 0:
+        return np.zeros_like(b), 0, 0.0, 0.0, np.array([0.0])
+    x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=complex)
+    r = b - A(x) if np.count_nonzero(x) else b.copy()
+    tolb = tol * nb
+    nr = nrm(r)
+    resvec = [nr]
+    if nr <= tolb:
+        return x, 0, nr / nb, 0.0, np.array(resvec)
+    rt = r.copy()
+    best_nr, best_x, best_it = nr, x.copy(), 0.0
+    rho_old = alpha = omega = 1.0
+    p = v = np.zeros_like(b)
+    flag, it, stag, extra = 1, float(maxit), 0, 0
+    max_extra = min(n // 50, 5, n - maxit)
+    nr_act = nr
+
+    def confirm(xc, rc, nrc):
+        """True-residual check behind a small recurrence residual; returns
+        (residual vector, its norm, outcome) with outcome 'ok', 'go' or 'stop'."""
+        nonlocal stag, extra
+        if not (nrc <= tolb or stag >= 3 or extra):
+            return rc, nrc, "go"
+        rc = b - A(xc)
+        nrc = nrm(rc)
+        if nrc <= tolb:
+            return rc, nrc, "ok"
+        if stag >= 3 and extra == 0:
+            stag = 0
+        extra += 1
+        return rc, nrc, ("stop" if extra >= max_extra else "go")
+
+    for i in range(1, maxit + 1):
+        rho = np.vdot(rt, r)
+        if rho == 0 or not np.isfinite(rho):
+            flag = 4
+            break
+        if i == 1:
+            p = r.copy()
+        else:
+            beta = (rho / rho_old) * (alpha / omega)
+            if beta == 0 or not np.isfinite(beta):
+                flag = 4
+                break
+            p = r + beta * (p - omega * v)
+        ph = prec(p)
+        if not np.all(np.isfinite(ph)):
+            flag = 2
+            break
+        v = A(ph)
+        rtv = np.vdot(rt, v)
+        if rtv == 0 or not np.isfinite(rtv):
+            flag = 4
+            break
+        alpha = rho / rtv
+        stag = stag + 1 if abs(alpha) * nrm(ph) < eps * nrm(x) else 0
+        xh = x + alpha * ph
+        s = r - alpha * v
+        s, nr_act, out = confirm(xh, s, nrm(s))
+        resvec.append(nr_act)
+        if out != "go":
+            x = xh
+            flag, it = (0, i - 0.5) if out == "ok" else (3, i - 0.5)
+            break
+        if nr_act < best_nr:
+            best_nr, best_x, best_it = nr_act, xh.copy(), i - 0.5
+        sh = prec(s)
+        if not np.all(np.isfinite(sh)):
+            flag = 2
+            break
+        t = A(sh)
+        tt = np.vdot(t, t).real
+        if tt == 0 or not np.isfinite(tt):
+            flag = 4
+            break
+        omega = np.vdot(t, s) / tt
+        stag = stag + 1 if abs(omega) * nrm(sh) < eps * nrm(xh) else 0
+        x = xh + omega * sh
+        r = s - omega * t
+        r, nr_act, out = confirm(x, r, nrm(r))
+        resvec.append(nr_act)
+        if out != "go":
+            flag, it = (0, float(i)) if out == "ok" else (3, float(i))
+            break
+        if nr_act < best_nr:
+            best_nr, best_x, best_it = nr_act, x.copy(), float(i)
+        if omega == 0:
+            flag = 4
+            break
+        rho_old = rho
+    if flag == 0:
+        relres = nr_act / nb
+    else:
+        if flag in (2, 4):
+            it = len(resvec) / 2 - 0.5
+        nb_best = nrm(b - A(best_x))
+        if nb_best <= nr_act:
+            x, it, relres = best_x, best_it, nb_best / nb
+        else:
+            relres = nr_act / nb
+    return x, flag, relres, it, np.array(resvec)
+
+
+# ---------------------------------------------------------------------------
 # JVIE_Solver (solver 'G'): src_vie/src_solver/JVIE_Solver.m:71-156,176-299,513-514
 # ---------------------------------------------------------------------------
 def jvie_setup(Einc, e_r, r, freq, form=2):
@@ -200,9 +480,16 @@ def jvie_setup(Einc, e_r, r, freq, form=2):
     return dict(Mr=Mr, Mc=Mc, Gram=Gram, idxS3=idxS3, Vrhs=Vrhs, shape=(L, M, N))
 
 
-def JVIE_Solver(Einc, e_r, r, freq, fN, tol=1e-3, form=2, precond=0, inner_it=50, outer_it=200, workers=None):
+def JVIE_Solver(Einc, e_r, r, freq, fN, tol=1e-3, form=2, solver="B", precond=0, max_it=1000, inner_it=50,
+                outer_it=200, ritz=5, workers=None):
+    """JVIE_Solver.m:71-122 argument handling, :176-299 operators, :300-499 the
+    solver dispatch ('G' pgmres, 'D' pgmresDR, anything else 'B' bicgstab)."""
     if tol < 1e-15 or tol >= 1:
         tol = 1e-3
+    if solver not in ("G", "D"):
+        solver = "B"
+    if precond not in ("L", "R"):
+        precond = 0
     S = jvie_setup(Einc, e_r, r, freq, form)
     Mr, Mc, Gram, idx = S["Mr"], S["Mc"], S["Gram"], S["idxS3"]
 
@@ -212,7 +499,14 @@ def JVIE_Solver(Einc, e_r, r, freq, fN, tol=1e-3, form=2, precond=0, inner_it=50
     def fP(J):
         return mv_AN(J, fN, 1.0 / Mr, 1.0 / Mr - 1.0, Gram, "notransp", idx, workers)
 
-    if precond == "R":
+    if solver == "B":
+        # JVIE_Solver.m:451-499: either precond letter makes fP bicgstab's M1
+        vsol, flag, relres, it, resvec = bicgstab(fA, S["Vrhs"], tol, max_it, fP if precond else None)
+    elif solver == "D":
+        ritz = min(ritz if ritz and ritz >= 1 else 5, inner_it - 1)
+        L1, R1 = (fP, None) if precond == "L" else ((None, fP) if precond == "R" else (None, None))
+        vsol, flag, relres, it, resvec = pgmresDR(fA, S["Vrhs"], inner_it, tol, outer_it, ritz, L1, None, R1)
+    elif precond == "R":
         vsol, flag, relres, it, resvec = pgmres(fA, S["Vrhs"], inner_it, tol, outer_it, None, None, fP)
     elif precond == "L":
         vsol, flag, relres, it, resvec = pgmres(fA, S["Vrhs"], inner_it, tol, outer_it, fP)

@@ -46,7 +46,7 @@ def test_adjoint_gradient_matches_central_differences(objective):
         sig_t[inside] *= 1 + 0.05 * rng.standard_normal(inside.sum())
         from marie_gb300.autograd import complex_permittivity
 
-        Jt = mg.JVIE_Solver(E, np.asfortranarray(complex_permittivity(eps_t, sig_t, FREQ)), r, FREQ, op, tol=1e-12)[0]
+        Jt = mg.JVIE_Solver(E, np.asfortranarray(complex_permittivity(eps_t, sig_t, FREQ)), r, FREQ, op, tol=1e-12, solver="G")[0]
         Et = np.asfortranarray(mg.E_field_Nop(Jt, op, dx**3, FREQ, E))
     F, ge, gs, flags, iters = F_of(op, E, eps, sig, dx, objective, Et)
     assert flags == (0, 0)
@@ -79,7 +79,7 @@ def test_objective_value_matches_oracle_forward_solve():
     op = mg.Operator.assemble(L, L, L, dx, FREQ, precision="fp64")
     F, *_ = F_of(op, E, eps, sig, dx)
     er = complex_permittivity(eps, sig, FREQ)
-    Je = vo.JVIE_Solver(E, er, r, FREQ, op.to_array(), tol=1e-12)[0]
+    Je = vo.JVIE_Solver(E, er, r, FREQ, op.to_array(), tol=1e-12, solver="G")[0]
     inside = np.abs(er - 1) > 1e-12
     Ei = Je[inside] / (1j * 2 * np.pi * FREQ * vo.EPS0 * (er[inside] - 1)[:, None])
     F_ref = np.sum(0.5 * sig[inside][:, None] * np.abs(Ei) ** 2)

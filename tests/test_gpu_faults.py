@@ -25,7 +25,7 @@ def test_non_convergence_is_a_flag_not_an_error():
 
     r, er, E = sphere()
     op = mg.Operator.assemble(8, 8, 8, 5e-3, FREQ)
-    Je, flag, relres, it, resvec, _ = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-12, inner_it=2, outer_it=1)
+    Je, flag, relres, it, resvec, _ = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-12, inner_it=2, outer_it=1, solver="G")
     assert flag == 1 and relres > 1e-12
     assert it == [2, 1] and len(resvec) == 3
 
@@ -38,8 +38,8 @@ def test_non_finite_input_is_reported_and_library_recovers():
     Ebad = E.copy(order="F")
     Ebad[3, 3, 3, 0] = np.nan
     with pytest.raises(mg.MarieError, match="non-finite"):
-        mg.JVIE_Solver(Ebad, er, r, FREQ, op, tol=1e-8)
-    out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8)
+        mg.JVIE_Solver(Ebad, er, r, FREQ, op, tol=1e-8, solver="G")
+    out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8, solver="G")
     assert out[1] == 0
 
 
@@ -49,9 +49,9 @@ def test_air_only_and_zero_excitation():
     r, er, E = sphere()
     op = mg.Operator.assemble(8, 8, 8, 5e-3, FREQ)
     air = np.ones_like(er)
-    Je, flag, relres, *_ = mg.JVIE_Solver(E, air, r, FREQ, op, tol=1e-8)
+    Je, flag, relres, *_ = mg.JVIE_Solver(E, air, r, FREQ, op, tol=1e-8, solver="G")
     assert flag == 0 and not np.any(Je)
-    Je, flag, relres, *_ = mg.JVIE_Solver(np.zeros_like(E), er, r, FREQ, op, tol=1e-8)
+    Je, flag, relres, *_ = mg.JVIE_Solver(np.zeros_like(E), er, r, FREQ, op, tol=1e-8, solver="G")
     assert flag == 0 and relres == 0 and not np.any(Je)
 
 
@@ -67,9 +67,9 @@ def test_allocation_failure_is_enomem_and_plan_stays_usable(nth):
     lib.marie_inject_alloc_failure(nth)
     try:
         with pytest.raises(mg.MarieError) as ei:
-            mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8)
+            mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8, solver="G")
         assert ei.value.code == -2
     finally:
         lib.marie_inject_alloc_failure(0)
-    out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8)
+    out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8, solver="G")
     assert out[1] == 0

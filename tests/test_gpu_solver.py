@@ -72,9 +72,9 @@ def test_jvie_solver_matches_oracle(form, precond):
     L, dx = 8, 5e-3
     r, er, E = sphere_problem(L, dx, 0.018)
     fN = vo.getOPERATORS(r, FREQ)
-    ref = vo.JVIE_Solver(E, er, r, FREQ, fN, tol=1e-10, form=form, precond=precond, inner_it=20)
+    ref = vo.JVIE_Solver(E, er, r, FREQ, fN, tol=1e-10, form=form, precond=precond, inner_it=20, solver="G")
     op = mg.Operator.from_array(fN)
-    out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-10, form=form, precond=precond, inner_it=20)
+    out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-10, form=form, precond=precond, inner_it=20, solver="G")
     assert out[1] == ref[1] == 0
     assert out[3] == ref[3]
     np.testing.assert_allclose(out[4], ref[4], rtol=1e-6, atol=1e-13)
@@ -98,7 +98,7 @@ def test_batched_excitations_match_single_solves(precision, precond):
                                                       inner_it=15)
     for e in range(3):
         Js, fs, rs, its, _, _ = mg.JVIE_Solver(np.asfortranarray(Eb[..., e]), er, r, FREQ, op, tol=1e-8,
-                                               precond=precond, inner_it=15)
+                                               precond=precond, inner_it=15, solver="G")
         assert flags[e] == fs == 0
         if precision == "fp64":
             assert list(iters[e]) == list(its)
@@ -112,7 +112,7 @@ def test_batched_excitations_match_single_solves(precision, precond):
         fN = op.to_array()
         for e in range(3):
             ref = vo.JVIE_Solver(np.asfortranarray(Eb[..., e]), er, r, FREQ, fN, tol=1e-8, precond=precond,
-                                 inner_it=15)
+                                 inner_it=15, solver="G")
             assert ref[3] == list(iters[e])
             assert np.max(np.abs(Jb[..., e] - ref[0])) < 1e-7 * np.max(np.abs(ref[0]))
 
@@ -133,7 +133,7 @@ def test_uneven_bodies_solved_concurrently():
         Eb = np.asfortranarray(np.stack(Es, axis=4))
         op = mg.Operator.assemble(L, L, L, dx, FREQ, precision="mixed", nrhs_max=2)
         bodies.append((Eb, er, r, op))
-        singles.append([mg.JVIE_Solver(np.asfortranarray(E), er, r, FREQ, op, tol=1e-7)[0] for E in Es])
+        singles.append([mg.JVIE_Solver(np.asfortranarray(E), er, r, FREQ, op, tol=1e-7, solver="G")[0] for E in Es])
     res, t = mg.JVIE_Solver_bodies(bodies, FREQ, tol=1e-7)
     for (Je, flag, relres, it), ref in zip(res, singles):
         assert np.all(flag == 0) and np.all(relres <= 1e-7)
@@ -148,8 +148,8 @@ def test_mixed_precision_solve_matches_fp64():
     r, er, E = sphere_problem(L, dx, 0.035)
     op64 = mg.Operator.assemble(L, L, L, dx, FREQ, precision="fp64")
     opm = mg.Operator.assemble(L, L, L, dx, FREQ, precision="mixed")
-    J64, f64, rr64, it64, _, _ = mg.JVIE_Solver(E, er, r, FREQ, op64, tol=1e-6)
-    Jm, fm, rrm, itm, resm, _ = mg.JVIE_Solver(E, er, r, FREQ, opm, tol=1e-6)
+    J64, f64, rr64, it64, _, _ = mg.JVIE_Solver(E, er, r, FREQ, op64, tol=1e-6, solver="G")
+    Jm, fm, rrm, itm, resm, _ = mg.JVIE_Solver(E, er, r, FREQ, opm, tol=1e-6, solver="G")
     assert f64 == 0 and fm == 0 and rrm <= 1e-6
     # both solutions satisfy the FP64 system to 1e-6: fields agree to ~cond * tol
     assert np.linalg.norm(Jm - J64) / np.linalg.norm(J64) < 2e-5
@@ -160,7 +160,7 @@ def mie_error(L, dx, R, precision="fp64"):
 
     r, er, E = sphere_problem(L, dx, R)
     op = mg.Operator.assemble(L, L, L, dx, FREQ, precision=precision)
-    Je, flag, relres, it, resvec, _ = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-6)
+    Je, flag, relres, it, resvec, _ = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-6, solver="G")
     assert flag == 0
     Et = mg.E_field_Nop(Je, op, dx**3, FREQ, E)
     rad = np.sqrt(np.sum(r * r, axis=3))

@@ -152,7 +152,7 @@ def test_jvie_field_current_identity():
     fN = vo.getOPERATORS(r, FREQ)
     em = vo.EMconstants(FREQ)
     E, _ = vo.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
-    Je, flag, relres, it, resvec = vo.JVIE_Solver(E, er, r, FREQ, fN, tol=1e-10, form=1)
+    Je, flag, relres, it, resvec = vo.JVIE_Solver(E, er, r, FREQ, fN, tol=1e-10, form=1, solver="G")
     assert flag == 0
     Et = vo.E_field_Nop(Je, fN, dx**3, FREQ, E)
     Ej = Je[inside] / (1j * em["omega"] * vo.EPS0 * (er[inside, None] - 1))
@@ -170,3 +170,69 @@ def test_getoperators_small_grid_self_consistency():
     np.testing.assert_allclose(np.fft.fftn(Cc, axes=(0, 1, 2)), F, rtol=1e-12, atol=1e-12 * np.abs(F).max())
     # the diagonal components dominate and are even
     assert np.abs(T[0, 0, 0, 0]) > np.abs(T[0, 0, 0, 1])
+
+
+def hard_dense(n, seed):
+    """Complex system whose spectrum has a few small eigenvalues, so that
+    restarted GMRES stalls and deflation helps."""
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    lam = np.concatenate([[0.01, 0.02, 0.05], np.linspace(1, 4, n - 3)]) * np.exp(0.3j * rng.random(n))
+    A = Q @ np.diag(lam) @ Q.conj().T + 0.01 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    return A, b
+
+
+def test_bicgstab_dense_systems_converge_to_solve():
+    for seed in range(3):
+        rng = np.random.default_rng(seed)
+        n = 60
+        A = np.eye(n) * 3 + 0.4 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+        b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        x, flag, relres, it, resvec = vo.bicgstab(lambda v: A @ v, b, 1e-10, 200)
+        assert flag == 0 and relres <= 1e-10
+        assert 2 * it + 1 == len(resvec)  # one norm per half step plus the initial one
+        np.testing.assert_allclose(x, np.linalg.solve(A, b), rtol=1e-8)
+        # a left preconditioner (Jacobi) as M1 gives the same solution
+        P = np.diag(1.0 / np.diag(A))
+        xp, flagp, *_ = vo.bicgstab(lambda v: A @ v, b, 1e-10, 200, lambda v: P @ v)
+        assert flagp == 0
+        np.testing.assert_allclose(xp, x, rtol=1e-8)
+
+
+def test_bicgstab_flags_and_best_iterate():
+    A, b = hard_dense(80, 1)
+    x, flag, relres, it, resvec = vo.bicgstab(lambda v: A @ v, b, 1e-12, 3)
+    assert flag == 1
+    # the returned iterate is the best one seen, with its true residual
+    assert np.isclose(relres, np.linalg.norm(b - A @ x) / np.linalg.norm(b))
+    assert relres <= resvec[-1] / np.linalg.norm(b) * (1 + 1e-12)
+    # zero right-hand side: x = 0 at once
+    x0, f0, r0, i0, rv0 = vo.bicgstab(lambda v: A @ v, np.zeros(80, complex), 1e-8, 10)
+    assert f0 == 0 and i0 == 0 and not np.any(x0)
+    # breakdown scalar: rho = r~'r = 0 cannot occur, but A = 0 gives r~'v = 0
+    _, f4, *_ = vo.bicgstab(lambda v: 0 * v, b, 1e-8, 10)
+    assert f4 == 4
+
+
+def test_pgmresdr_dense_systems():
+    A, b = hard_dense(120, 2)
+    xs = np.linalg.solve(A, b)
+    # one cycle long enough: pgmresDR is plain GMRES
+    x1, f1, r1, it1, rv1 = vo.pgmresDR(lambda v: A @ v, b, 119, 1e-10, 1, 5)
+    x2, f2, r2, it2, rv2 = vo.pgmres(lambda v: A @ v, b, 119, 1e-10, 1)
+    # (pgmresDR.m counts only the cycles after the first in iter(2))
+    assert f1 == f2 == 0 and it1[0] == it2[0] and it1[1] == it2[1] - 1
+    np.testing.assert_allclose(rv1, rv2, rtol=1e-8)
+    # short restarts: deflation converges in fewer matvecs than GMRES(m)
+    xd, fd, rd, itd, rvd = vo.pgmresDR(lambda v: A @ v, b, 12, 1e-8, 200, 4)
+    xg, fg, rg, itg, rvg = vo.pgmres(lambda v: A @ v, b, 12, 1e-8, 200)
+    assert fd == 0 and rd <= 1e-8
+    np.testing.assert_allclose(xd, xs, rtol=1e-6)
+    assert len(rvd) < len(rvg)
+    # preconditioned forms reach the same solution
+    P = np.diag(1.0 / np.diag(A))
+    for kw in (dict(L1=lambda v: P @ v), dict(R1=lambda v: P @ v)):
+        xp, fp, *_ = vo.pgmresDR(lambda v: A @ v, b, 12, 1e-10, 200, 4, **kw)
+        assert fp == 0
+        np.testing.assert_allclose(xp, xs, rtol=1e-7)
