@@ -76,23 +76,27 @@ k_xyfwd(const double2* __restrict__ J, long long js, const int* __restrict__ inv
       const bool valid = yl < C::RY;
       const int y = q * C::RY + yl;
       V reg[E];
+      // all index loads first, then all value loads: one exposed latency per level
+      int kk[E];
+      const int* invr = inv + (long long)L * (y + (long long)M * plane);
 #pragma unroll
       for (int b = 0; b < E / R0; ++b)
 #pragma unroll
         for (int r = 0; r < R0; ++r) {
           const int p = FX::in_pos(t, b, r);
-          V val = mk<V>(0, 0);
-          if (valid && r < R0 / 2 && p < L) {
-            const int k = inv[(long long)p + (long long)L * (y + (long long)M * plane)];
-            if (k >= 0) {
-              double2 jv = Jr[k];
-              if (pro.conjin) jv.y = -jv.y;
-              if (pro.pre) jv = cmul(pro.pre[k], jv);
-              val = cvt<V>(jv);
-            }
-          }
-          reg[b * R0 + r] = val;
+          kk[b * R0 + r] = (valid && r < R0 / 2 && p < L) ? invr[p] : -1;
         }
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        V val = mk<V>(0, 0);
+        if (kk[i] >= 0) {
+          double2 jv = Jr[kk[i]];
+          if (pro.conjin) jv.y = -jv.y;
+          if (pro.pre) jv = cmul(pro.pre[kk[i]], jv);
+          val = cvt<V>(jv);
+        }
+        reg[i] = val;
+      }
       FX::run_half(reg, xb + s * C::ROWP, SAddr(1, true), t, twx_s);
       if (valid) {
 #pragma unroll
@@ -139,7 +143,7 @@ k_xyfwd(const double2* __restrict__ J, long long js, const int* __restrict__ inv
 }
 
 template <typename T, int NL, int NM, int CS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (XYCfg<T, NL, NM, CS>::FXI::E <= 16 && XYCfg<T, NL, NM, CS>::FYI::E <= 16) ? 3 : 1)
 k_yxinv(const cplx<T>* __restrict__ B, long long bs, const double2* __restrict__ J, long long js,
         const int* __restrict__ inv, Epilogue ep, double2* __restrict__ out, long long os, Dims d,
         const cplx<T>* __restrict__ twx, const cplx<T>* __restrict__ twy) {
@@ -207,27 +211,71 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const double2* __restrict__
       FXI::load(reg, base, rowa, t, NL);
       FXI::run(reg, base, rowa, t, twx_s);
       if (valid) {
+        const int* invr = inv + (long long)L * (y + (long long)M * plane);
+        if constexpr (E <= 16) {
+          // index loads, then the per-DOF loads, then the epilogue arithmetic
+          int kk[E];
 #pragma unroll
-        for (int b = 0; b < E / RL; ++b)
+          for (int b = 0; b < E / RL; ++b)
 #pragma unroll
-          for (int r = 0; r < RL; ++r) {
-            const int x = FXI::out_pos(t, b, r);
-            if (x >= L) continue;
-            const int k = inv[(long long)x + (long long)L * (y + (long long)M * plane)];
-            if (k < 0) continue;
-            const double2 v = cvt<double2>(reg[b * RL + r]);
-            const double2 jv = Jr[k];
-            const double2 A_k = ep.a ? ep.a[k] : ep.a_s;
-            double2 res = cmul(A_k, jv);
-            if (ep.conjout) {
-              res.x -= v.x;
-              res.y += v.y;
-            } else {
-              const double2 B_k = ep.b ? ep.b[k] : ep.b_s;
-              res = csub(res, cmul(B_k, v));
+            for (int r = 0; r < RL; ++r) {
+              const int x = FXI::out_pos(t, b, r);
+              kk[b * RL + r] = x < L ? invr[x] : -1;
             }
-            outr[k] = res;
+          // per-DOF loads in groups of EPI (bounded registers)
+          constexpr int EPI = 2;
+#pragma unroll
+          for (int i0 = 0; i0 < E; i0 += EPI) {
+            double2 jv[EPI], ak[EPI], bk[EPI];
+#pragma unroll
+            for (int j = 0; j < EPI; ++j) {
+              const int k = kk[i0 + j];
+              if (k < 0) continue;
+              jv[j] = Jr[k];
+              ak[j] = ep.a ? ep.a[k] : ep.a_s;
+              bk[j] = ep.b ? ep.b[k] : ep.b_s;
+            }
+#pragma unroll
+            for (int j = 0; j < EPI; ++j) {
+              const int k = kk[i0 + j];
+              if (k < 0) continue;
+              // the diagonal Gram*Mr*J term in FP64; the circulant term in the
+              // transform's precision
+              double2 res = cmul(ak[j], jv[j]);
+              if (ep.conjout) {
+                const double2 v = cvt<double2>(reg[i0 + j]);
+                res.x -= v.x;
+                res.y += v.y;
+              } else {
+                res = csub(res, cvt<double2>(cmul(cvt<V>(bk[j]), reg[i0 + j])));
+              }
+              outr[k] = res;
+            }
           }
+        } else {
+          // wide register sets (E = 20, 24): one DOF at a time
+#pragma unroll
+          for (int b = 0; b < E / RL; ++b)
+#pragma unroll
+            for (int r = 0; r < RL; ++r) {
+              const int x = FXI::out_pos(t, b, r);
+              if (x >= L) continue;
+              const int k = invr[x];
+              if (k < 0) continue;
+              const double2 jv = Jr[k];
+              const double2 A_k = ep.a ? ep.a[k] : ep.a_s;
+              double2 res = cmul(A_k, jv);
+              if (ep.conjout) {
+                const double2 v = cvt<double2>(reg[b * RL + r]);
+                res.x -= v.x;
+                res.y += v.y;
+              } else {
+                const double2 B_k = ep.b ? ep.b[k] : ep.b_s;
+                res = csub(res, cvt<double2>(cmul(cvt<V>(B_k), reg[b * RL + r])));
+              }
+              outr[k] = res;
+            }
+        }
       }
     }
   }
