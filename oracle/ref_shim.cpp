@@ -7,6 +7,7 @@
 // translation units define clashing non-static symbols (GL_1D, Kernel, ...).
 // The argument order follows the MEX gateways:
 //   cubature_nop_mex.cpp:29-78   (Np, w, u, v, r_m, r_n, R_faces[3][4][6], ko, dx)
+//   cubature_kop_mex.cpp          (Np, w, u, v, r_m, r_n, R_faces[3][4][6], ko)
 //   directfn_ws_st_const_mex.cpp (r1, r2, r3, ko, Np_1D)
 //   directfn_ws_ea_const_mex.cpp:50 passes (r1, r2, r3, r4, r2, r1, ko, Np_1D)
 //   directfn_ws_va_const_mex.cpp:51 passes (r1, r2, r3, r4, r5, r1, ko, Np_1D)
@@ -34,6 +35,26 @@ extern "C" void ref_cubature_nop(int Np, const double* w, const double* u, const
       out[2 * (6 * i + j)] = I[i][j].real();
       out[2 * (6 * i + j) + 1] = I[i][j].imag();
     }
+}
+#endif
+
+#if defined(SHIM_CUBATURE_KOP)
+void cubature_kop(const int Np, const double w[], const double u[], const double v[], const double r_m[3],
+                  const double r_n[3], const double R_faces[3][4][6], const double ko, complex<double> IK_mn[3]);
+// out: 3 complex as (re, im) pairs
+extern "C" void ref_cubature_kop(int Np, const double* w, const double* u, const double* v,
+                                 const double* r_m, const double* r_n,
+                                 const double* R_faces_colmajor, double ko, double* out) {
+  double RR[3][4][6];
+  for (int k = 0; k < 6; k++)
+    for (int j = 0; j < 4; j++)
+      for (int i = 0; i < 3; i++) RR[i][j][k] = R_faces_colmajor[i + 3 * j + 12 * k];
+  complex<double> I[3];
+  cubature_kop(Np, w, u, v, r_m, r_n, RR, ko, I);
+  for (int i = 0; i < 3; i++) {
+    out[2 * i] = I[i].real();
+    out[2 * i + 1] = I[i].imag();
+  }
 }
 #endif
 

@@ -771,19 +771,167 @@ def circulant_nop(G):
     return C
 
 
+# ---------------------------------------------------------------------------
+# K operator: assembly_kop.m:7-120, cubature_kop.cpp:8-120,
+# cubature_kop_near_sym.m:1-105, nearby_correct_kop.m:1-134,
+# circulant_kop.m:1-41, gperiodic_coeff_kop.m:1-36
+# ---------------------------------------------------------------------------
+# cubature_kop.cpp:30-32: the 12 integrated (obs, src) face pairs and their signs
+KOP_OBS = [0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5]
+KOP_SRC = [0, 1, 0, 1, 2, 3, 2, 3, 4, 5, 4, 5]
+KOP_SIGN = [1.0, -1.0, -1.0, 1.0, 1.0, -1.0, -1.0, 1.0, 1.0, -1.0, -1.0, 1.0]
+
+
+def _kop_pair(Np, w, u, v, r_m, R_faces, ko, io, isrc):
+    """sum over point pairs of w_p w_q G(R) (r_p - r_q), G = (1 - e^{-jkR}(1 + jkR)) / R^3,
+    for observation offsets r_m (B x 3); returns (B, 3)."""
+    p1, p2, p4 = R_faces[:, 0, io], R_faces[:, 1, io], R_faces[:, 3, io]
+    q1, q2, q4 = R_faces[:, 0, isrc], R_faces[:, 1, isrc], R_faces[:, 3, isrc]
+    rp = p1[None, :] + np.outer(u, p2 - p1) + np.outer(v, p4 - p1)
+    rq = q1[None, :] + np.outer(u, q2 - q1) + np.outer(v, q4 - q1)
+    d = (rp[None, :, None, :] + r_m[:, None, None, :]) - rq[None, None, :, :]  # B x Np x Np x 3
+    R = np.sqrt(np.sum(d * d, axis=-1))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        G = (1.0 - np.exp(-1j * ko * R) * (1.0 + 1j * ko * R)) / R**3
+    W = np.outer(w, w)
+    return np.einsum("bpq,bpqc->bc", W[None] * G, d)
+
+
+def cubature_kop_batch(Np, w, u, v, r_m, R_faces, ko):
+    """cubature_kop.cpp:8-120 (r_n = 0): IK_mn (B x 3), without the dx^4 factor."""
+    r_m = np.atleast_2d(r_m)
+    out = np.zeros((r_m.shape[0], 3), dtype=complex)
+    for io, isrc, sg in zip(KOP_OBS, KOP_SRC, KOP_SIGN):
+        out += sg * _kop_pair(Np, w, u, v, r_m, R_faces, ko, io, isrc)
+    return out
+
+
+def cubature_kop_near_sym(Np, w, u, v, r_m, m, R_faces, ko):
+    """cubature_kop_near_sym.m:17-105 for one offset: the 21 unique face pairs
+    with the 20-point rule, the 15 mirrored copies, nearby_correct_kop (the
+    coincident pairs dropped) and the face-normal combination."""
+    I = np.zeros((6, 6, 3), dtype=complex)
+    rm = np.asarray(r_m, float)[None]
+    for io, isrc in zip(INDEX_OBS, INDEX_SRC):
+        I[io, isrc] = _kop_pair(Np, w, u, v, rm, R_faces, ko, io, isrc)[0]
+    for (a, b), (c, d_) in MIRROR:
+        I[a, b] = I[c, d_]
+    I = nearby_correct_kop(m, I)
+    J = np.zeros((6, 6), dtype=complex)
+    for i in range(6):
+        J[i] = (1.0 if i % 2 else -1.0) * I[i, :, i // 2]
+    return np.array([np.sum(J[:, 2 * c + 1] - J[:, 2 * c]) for c in range(3)])
+
+
+def nearby_correct_kop(m, I_non):
+    """nearby_correct_kop.m:5-134: only the coincident (ST) face pairs are
+    changed (to zero); every other pair keeps its 20-point value."""
+    I = I_non.copy()
+    for i in range(6):
+        for j in range(6):
+            if near_class(m, i, j) == 1:
+                I[i, j] = 0.0
+    return I
+
+
+def assembly_kop(L, M, N, ko, dx):
+    """assembly_kop.m:7-120 -> IK_mn (L, M, N, 3)."""
+    R_faces = cube_faces(dx, dx, dx)
+    K = np.zeros((L, M, N, 3), dtype=complex)
+    d = np.array([dx, dx, dx])
+    Np, w, u, v = gauss_2d(4)
+    for mz in range(N):
+        for my in range(M):
+            mx = np.arange(L)
+            r_m = np.stack([mx * dx, np.full(L, my * dx), np.full(L, mz * dx)], axis=1)
+            K[:, my, mz] = cubature_kop_batch(Np, w, u, v, r_m, R_faces, ko)
+    Np, w, u, v = gauss_2d(10)
+    for mx in range(min(5, L)):
+        for my in range(min(5, M)):
+            for mz in range(min(5, N)):
+                K[mx, my, mz] = cubature_kop_batch(Np, w, u, v, np.array([mx, my, mz]) * d, R_faces, ko)[0]
+    Np, w, u, v = gauss_2d(20)
+    for mx in range(min(2, L)):
+        for my in range(min(2, M)):
+            for mz in range(min(2, N)):
+                K[mx, my, mz] = cubature_kop_near_sym(Np, w, u, v, np.array([mx, my, mz]) * d, (mx, my, mz),
+                                                      R_faces, ko)
+    return dx**4 / (1j * ko) ** 2 / (4 * np.pi) * K
+
+
+# gperiodic_coeff_kop.m:4-34: component i of K is odd along axis i
+_GPK = {"L": [-1, 1, 1], "M": [1, -1, 1], "N": [1, 1, -1], "LM": [-1, -1, 1], "LN": [-1, 1, -1],
+        "MN": [1, -1, -1], "LMN": [-1, -1, -1]}
+
+
+def circulant_kop(G):
+    """circulant_kop.m:17-41."""
+    L, M, N, _ = G.shape
+    C = np.zeros((2 * L, 2 * M, 2 * N, 3), dtype=complex)
+    C[:L, :M, :N] = G
+    for ii in range(3):
+        C[L + 1:, :M, :N, ii] = G[L - 1:0:-1, :, :, ii] * _GPK["L"][ii]
+        C[:L, M + 1:, :N, ii] = G[:, M - 1:0:-1, :, ii] * _GPK["M"][ii]
+        C[:L, :M, N + 1:, ii] = G[:, :, N - 1:0:-1, ii] * _GPK["N"][ii]
+        C[L + 1:, M + 1:, :N, ii] = G[L - 1:0:-1, M - 1:0:-1, :, ii] * _GPK["LM"][ii]
+        C[L + 1:, :M, N + 1:, ii] = G[L - 1:0:-1, :, N - 1:0:-1, ii] * _GPK["LN"][ii]
+        C[:L, M + 1:, N + 1:, ii] = G[:, M - 1:0:-1, N - 1:0:-1, ii] * _GPK["MN"][ii]
+        C[L + 1:, M + 1:, N + 1:, ii] = G[L - 1:0:-1, M - 1:0:-1, N - 1:0:-1, ii] * _GPK["LMN"][ii]
+    return C
+
+
+def mv_K(JIn0, fK, r_shape, idx, workers=None):
+    """src_vie/src_mvp/mv_K.m:30-93: crop(IFFT(fK x FFT(J))) on the entries idx
+    (the curl-type product out = [K3 J2 - K2 J3, K1 J3 - K3 J1, K2 J1 - K1 J2])."""
+    LfK, MfK, NfK, _ = fK.shape
+    L, M, N = r_shape[:3]
+    s = (LfK, MfK, NfK)
+    flat = np.zeros(L * M * N * 3, dtype=complex)
+    flat[np.asarray(idx) - 1] = JIn0
+    JIn = flat.reshape((L, M, N, 3), order="F")
+    f1 = _fftn(JIn[:, :, :, 0], s, workers)
+    f2 = _fftn(JIn[:, :, :, 1], s, workers)
+    f3 = _fftn(JIn[:, :, :, 2], s, workers)
+    o1 = fK[..., 2] * f2 - fK[..., 1] * f3
+    o2 = fK[..., 0] * f3 - fK[..., 2] * f1
+    o3 = fK[..., 1] * f1 - fK[..., 0] * f2
+    JOut = np.zeros((L, M, N, 3), dtype=complex)
+    for c, o in enumerate((o1, o2, o3)):
+        JOut[:, :, :, c] = _ifftn(o, workers)[:L, :M, :N]
+    return JOut.reshape(-1, order="F")[np.asarray(idx) - 1]
+
+
+def H_field_Kop(J, fK, Gram, Hinc=None, workers=None):
+    """src_vie/src_fields/src_op/H_field_Kop.m:46-77: Hinc + mv_K(J) / Gram."""
+    if Hinc is None:
+        Hinc = np.zeros_like(J)
+    if not np.any(J):
+        return Hinc
+    L, M, N, _ = J.shape
+    idx = np.arange(1, 3 * L * M * N + 1)
+    H = mv_K(J.reshape(-1, order="F"), fK, J.shape, idx, workers).reshape((L, M, N, 3), order="F")
+    return Hinc + H / Gram
+
+
 def fft_operator(A, workers=None):
     """fft_operator.m:6-8."""
     return scipy.fft.fftn(A, axes=(0, 1, 2), workers=workers)
 
 
 def getOPERATORS(r, f, op="N", typ="FFTofC", sing=None):
-    """getOPERATORS.m:36-90 for op 'N'.  sing = the five singular integrals
-    (defaults to the converged quadrature of singular_integrals)."""
-    if op != "N":
-        raise NotImplementedError("only the N operator")
+    """getOPERATORS.m:36-127 for op 'N' and 'K'.  sing = the five singular
+    integrals of N (defaults to the converged quadrature of singular_integrals)."""
     dx = r[1, 0, 0, 0] - r[0, 0, 0, 0]
     ko = 2 * np.pi / 299792458 * f
     L, M, N, _ = r.shape
+    if op == "K":
+        T = assembly_kop(L, M, N, ko, dx)
+        if typ == "T":
+            return T
+        C = circulant_kop(T)
+        return C if typ == "C" else fft_operator(C)
+    if op != "N":
+        raise ValueError("op must be 'N' or 'K'")
     if sing is None:
         sing = singular_integrals(ko, dx)
     T = assembly_nop(L, M, N, ko, dx, sing)

@@ -61,6 +61,42 @@ def parse_nearby(ref: Path):
     return out
 
 
+def parse_nearby_kop(ref: Path):
+    """The ST entries of the C tables of nearby_correct_kop.m (the only pairs
+    that routine changes), as 0/1 matrices per offset."""
+    src = (ref / "src_vie/src_operators/cubatures/nearby_correct_kop.m").read_text(errors="replace")
+    src = "\n".join(l.split("%")[0] for l in src.split("\n"))
+    out = {}
+    for mx, my, mz, body in re.findall(r"m == \[(\d),(\d),(\d)\];(.*?)(?=elseif|\nend)", src, re.S):
+        Cm = re.search(r"C\s*=\s*\[(.*?)\];", body, re.S).group(1)
+        Cr = [r.split() for r in Cm.strip().split("\n")]
+        out[f"{int(mx) - 1},{int(my) - 1},{int(mz) - 1}"] = [[1 if Cr[i][j] == "ST" else 0 for j in range(6)]
+                                                             for i in range(6)]
+    return out
+
+
+def cubature_kop_cases():
+    sys.path.insert(0, str(ROOT))
+    from oracle import vie_oracle as vo
+
+    lib = ctypes.CDLL(str(ROOT / "oracle/_ref/libref_cubature_kop.so"))
+    cases = []
+    for dx in (5e-3, 2e-3):
+        ko = 2 * np.pi * FREQ / C0
+        Rf = vo.cube_faces(dx, dx, dx)
+        Rcol = np.asfortranarray(Rf).reshape(-1, order="F")
+        for order in (4, 10):
+            Np, w, u, v = vo.gauss_2d(order)
+            for m in ((1, 0, 0), (0, 2, 1), (3, 1, 2), (5, 0, 0), (7, 6, 5), (2, 2, 2)):
+                r_m = np.array(m, dtype=float) * dx
+                out = np.zeros(6)
+                lib.ref_cubature_kop(ctypes.c_int(Np), _ptr(w), _ptr(u), _ptr(v), _ptr(r_m), _ptr(np.zeros(3)),
+                                     _ptr(Rcol), ctypes.c_double(ko), _ptr(out))
+                cases.append({"dx": dx, "ko": ko, "order": order, "m": list(m),
+                              "re": out[0::2].tolist(), "im": out[1::2].tolist()})
+    return cases
+
+
 def build_ref(ref: Path):
     subprocess.run(["make", "-C", str(ROOT / "oracle"), f"REF={ref}"], check=True, capture_output=True)
 
@@ -143,6 +179,8 @@ def main(ref: Path):
         "gauss_1d": parse_gauss(ref),
         "nearby": parse_nearby(ref),
         "cubature_nop": cubature_cases(),
+        "nearby_kop_st": parse_nearby_kop(ref),
+        "cubature_kop": cubature_kop_cases(),
         "directfn": direct,
     }
     OUT.write_text(json.dumps(data, indent=1))

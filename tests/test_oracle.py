@@ -236,3 +236,58 @@ def test_pgmresdr_dense_systems():
         xp, fp, *_ = vo.pgmresDR(lambda v: A @ v, b, 12, 1e-10, 200, 4, **kw)
         assert fp == 0
         np.testing.assert_allclose(xp, xs, rtol=1e-7)
+
+
+def test_cubature_kop_matches_reference_cpp(golden):
+    for case in golden["cubature_kop"]:
+        dx, ko = case["dx"], case["ko"]
+        Np, w, u, v = vo.gauss_2d(case["order"])
+        Rf = vo.cube_faces(dx, dx, dx)
+        I = vo.cubature_kop_batch(Np, w, u, v, np.array(case["m"], float)[None] * dx, Rf, ko)[0]
+        ref = np.array(case["re"]) + 1j * np.array(case["im"])
+        # touching faces evaluate 0/0 at coincident Gauss points in both codes
+        fin = np.isfinite(ref)
+        assert np.array_equal(fin, np.isfinite(I))
+        if fin.any():
+            np.testing.assert_allclose(I[fin], ref[fin], rtol=1e-12, atol=1e-12 * np.abs(ref[fin]).max())
+
+
+def test_nearby_correct_kop_drops_exactly_the_reference_st_pairs(golden):
+    for key, st in golden["nearby_kop_st"].items():
+        m = tuple(int(c) for c in key.split(","))
+        mine = [[1 if vo.near_class(m, i, j) == 1 else 0 for j in range(6)] for i in range(6)]
+        assert mine == st, key
+
+
+def test_k_operator_structure():
+    """Toeplitz K: component c odd in axis c (zero on that axis' zero plane);
+    the circulant has the gperiodic_coeff_kop parities; mv_K is the cross
+    product fK x J (so K applied to J and K applied to J + a J' differ linearly)."""
+    r = vo.grid(6, 5, 4, 4e-3)
+    T = vo.getOPERATORS(r, FREQ, "K", "T")
+    scale = np.abs(T).max()
+    assert np.abs(T[0, :, :, 0]).max() < 1e-12 * scale
+    assert np.abs(T[:, 0, :, 1]).max() < 1e-12 * scale
+    assert np.abs(T[:, :, 0, 2]).max() < 1e-12 * scale
+    C = vo.circulant_kop(T)
+    L, M, N = 6, 5, 4
+    for c in range(3):
+        s = np.ones(3)
+        s[c] = -1
+        np.testing.assert_allclose(C[2 * L - 2, 1, 1, c], s[0] * C[2, 1, 1, c])
+        np.testing.assert_allclose(C[1, 2 * M - 1, 1, c], s[1] * C[1, 1, 1, c])
+        np.testing.assert_allclose(C[1, 1, 2 * N - 3, c], s[2] * C[1, 1, 3, c])
+    fK = vo.fft_operator(C)
+    rng = np.random.default_rng(0)
+    idx = np.arange(1, 3 * L * M * N + 1)
+    J1 = rng.standard_normal(idx.size) + 1j * rng.standard_normal(idx.size)
+    J2 = rng.standard_normal(idx.size) + 1j * rng.standard_normal(idx.size)
+    a = 0.3 - 1.1j
+    lhs = vo.mv_K(J1 + a * J2, fK, (L, M, N), idx)
+    rhs = vo.mv_K(J1, fK, (L, M, N), idx) + a * vo.mv_K(J2, fK, (L, M, N), idx)
+    np.testing.assert_allclose(lhs, rhs, atol=1e-12 * np.abs(rhs).max())
+    # a current along x at one voxel gives no x component of the output
+    Jx = np.zeros(idx.size, complex)
+    Jx[1 + L * 2 + L * M * 1] = 1.0
+    out = vo.mv_K(Jx, fK, (L, M, N), idx).reshape((L, M, N, 3), order="F")
+    assert np.abs(out[..., 0]).max() < 1e-12 * np.abs(out).max()
