@@ -123,12 +123,22 @@ __global__ void __launch_bounds__(BT) kb_dots(const double2* __restrict__ Vb, lo
           acc[q].y = fma(v.x, wv.y, fma(-v.y, wv.x, acc[q].y));
         }
     }
+    // one block reduction for the 8 columns: warp sums, then warp partials
+    // summed in warp order by one thread per column (fixed order)
+    __shared__ double2 red[BT / 32][8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      if (q >= nc) break;
-      const double2 r = bsum2(acc[q]);
-      if (threadIdx.x == 0) part[((long long)s * 128 + c0 + q) * gridDim.x + blockIdx.x] = r;
+      const double2 r = wsum2(acc[q]);
+      if (lane == 0) red[wid][q] = r;
     }
+    __syncthreads();
+    if (threadIdx.x < nc) {
+      double2 r = red[0][threadIdx.x];
+      for (int w = 1; w < BT / 32; ++w) r = cadd(r, red[w][threadIdx.x]);
+      part[((long long)s * 128 + c0 + threadIdx.x) * gridDim.x + blockIdx.x] = r;
+    }
+    __syncthreads();  // red is reused by the next sweep
   }
 }
 
