@@ -275,7 +275,7 @@ def run_gpu(args, world, rank, local):
                       "speedup_mixed_vs_fp64": round(t64 / (ms_per_step / 1e3), 3),
                       "field_rel_err_mixed_vs_fp64": field_err, "mixed_other_solvers": variants},
             "matvec_ms": {"fp32": mv["fp32_ms"], "fp64": mv["fp64_ms"], "fp32_passes_ms": mv["fp32_passes"],
-                          "fp64_passes_ms": mv["fp64_passes"]},
+                          "fp64_passes_ms": mv["fp64_passes"], "fp32_cufft_comparison": mv["fp32_cufft_ms"]},
             "assembly_s": round(t_asm, 3),
             "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": round(dom["gbs"], 1), "peak": hbm,
                          "unit": "GB/s", "frac": round(dom["gbs"] / hbm, 4),
@@ -340,6 +340,16 @@ def matvec_times(mg, op, op64, er, lib):
         e1.synchronize()
         res[name + "_ms"] = round(e0.elapsed_time(e1) / reps, 4)
         res[name + "_passes"] = passes
+    # the same FP32 matvec through cuFFT (padded arrays, full operator), for comparison
+    ms = C.c_float()
+    cf = []
+    for _ in range(3 + 10):
+        s = lib.marie_mv_AN_cufft(op.plan, C.c_void_p(J.data_ptr()), C.c_void_p(Mr.data_ptr()),
+                                  C.c_void_p(Mc.data_ptr()), 8e-9, C.c_void_p(idx_d.data_ptr()), n,
+                                  C.c_void_p(out.data_ptr()), C.byref(ms))
+        assert s == 0, lib.marie_last_error()
+        cf.append(ms.value)
+    res["fp32_cufft_ms"] = round(float(np.median(cf[3:])), 4)
     # algorithmic bytes (complex64 spectra), per pass and per matvec
     S = 8
     Lp, Mp = 2 * L, 2 * M

@@ -63,7 +63,8 @@ int marie_plan_destroy(marie_plan* plan);
 void* marie_plan_stream(marie_plan* plan);
 
 /* Replaces getOPERATORS(r, f, op, type, singular)
- * (src_vie/src_operators/getOPERATORS.m:1-127) for op = 'N'.
+ * (src_vie/src_operators/getOPERATORS.m:1-127) for op = 'N' (6 components)
+ * and op = 'K' (3 components [Kx, Ky, Kz], assembly_kop.m; singular unused).
  *   r:       L x M x N x 3 voxel centres (uniform spacing; dx = r[1]-r[0])
  *   type:    'F' FFT of the circulant (2L x 2M x 2N x 6, the default 'FFTofC'),
  *            'C' circulant (2L x 2M x 2N x 6), 'T' Toeplitz (L x M x N x 6)
@@ -85,6 +86,10 @@ int marie_set_operator(marie_plan* plan, const double* fN, int64_t Lf, int64_t M
 /* Assemble the operator on the device for this plan's grid (no host copy). */
 int marie_plan_assemble(marie_plan* plan, double dx, double freq, char singular,
                         const double* singular_values);
+/* The K operator of getOPERATORS(r, f, 'K') for mv_K / H_field_Kop, uploaded
+ * (2L x 2M x 2N x 3 complex, as gpuArray(fK)) or assembled on the device. */
+int marie_set_operator_k(marie_plan* plan, const double* fK, int64_t Lf, int64_t Mf, int64_t Nf);
+int marie_plan_assemble_k(marie_plan* plan, double dx, double freq);
 /* Copy the plan's FP64 operator out (2L x 2M x 2N x 6 complex, host or device). */
 int marie_get_plan_operator(marie_plan* plan, double* fN_out);
 
@@ -117,6 +122,12 @@ int marie_mv_AN_static(marie_plan* plan, const double* JIn0, const double* Mr,
  * JOut = crop(N J) - Gram*J on the entries idx. */
 int marie_mv_L(marie_plan* plan, const double* JIn0, double Gram, const int64_t* idx,
                int64_t n_idx, double* JOut, int64_t nrhs, int precision);
+
+/* Replaces mv_K(JIn0, fK, r, idx, GPU_flag) (src_vie/src_mvp/mv_K.m:1-93) with
+ * the plan's K operator: JOut = crop(IFFT(fK x FFT(J))) on the entries idx,
+ * the cross product [K3 J2 - K2 J3, K1 J3 - K3 J1, K2 J1 - K1 J2]. */
+int marie_mv_K(marie_plan* plan, const double* JIn0, const int64_t* idx, int64_t n_idx,
+               double* JOut, int64_t nrhs, int precision);
 
 /* Replaces pgmres(A, b, restart, tol, maxit, L1, L2, R1, R2, x0)
  * (src_numeric/src_iterative/pgmres.m:70-181, pgmres_iter.m:22-150): restarted
@@ -208,6 +219,29 @@ int marie_jvie_solve_batch(marie_plan* plan, const double* Einc, int64_t nexc, c
                            int outer_it, double* Je, int* flag, double* relres, int* iter,
                            double* solvert);
 
+/* Replaces H_field_Kop(J, fK, Gram, Hinc, GPU_flag) (src_vie/src_fields/src_op/
+ * H_field_Kop.m:46-77): Htot = Hinc + mv_K(J) / Gram with the plan's K
+ * operator.  J, Hinc (may be NULL), Htot: L x M x N x 3 complex. */
+int marie_h_field_kop(marie_plan* plan, const double* J, double Gram, const double* Hinc,
+                      double* Htot, int precision);
+
+/* Replaces Scat_Solver(Einc, Hinc, freq, r, epsilon_r, sigma_e, rho, tol, fN, fK,
+ * form, solver, precond, max_it, inner_it, outer_it, ritz, gpu_flag)
+ * (src_vie/src_solver/Scat_Solver.m:1-241) on the plan: e_r = eps_r -
+ * j sigma/(eps0 omega), the JVIE_Solver current Jout, SAR Sout = |J|^2 /
+ * (2 sigma rho) (0 where |2 sigma rho| <= 1e-10), the total field Eout
+ * (E_field_Nop), Bout = mu0 H_field_Kop(Jout, fK, Gram, Hinc), Gsar = sum Sout
+ * Gram and Pabs = 0.5 Re sum Eout . conj(Jout) Gram.  The plan's N and K
+ * operators are assembled first when it holds none (Scat_Solver.m:155-160).
+ * eps_r, sigma_e, rho: L x M x N real; Einc, Hinc (may be NULL), Jout, Eout,
+ * Bout: L x M x N x 3 complex; Sout: L x M x N real; NULL outputs are skipped
+ * (Jout is required). */
+int marie_scat_solver(marie_plan* plan, const double* Einc, const double* Hinc, double dx,
+                      double freq, const double* eps_r, const double* sigma_e, const double* rho,
+                      double tol, int form, char solver, char precond, int max_it, int inner_it,
+                      int outer_it, int ritz, double* Jout, double* Sout, double* Eout, double* Bout,
+                      double* Gsar, double* Pabs);
+
 /* Replaces E_field_Nop(J, fN, Gram, freq, Einc) (src_vie/src_fields/src_op/
  * E_field_Nop.m:59-84): Etot = Einc + (N J - Gram J)/(Gram*j*omega*eps0).
  * J, Einc (may be NULL), Etot: L x M x N x 3 complex. */
@@ -222,6 +256,14 @@ int marie_plane_wave(const double* r, int64_t L, int64_t M, int64_t N, const dou
                      const double* Eo, double* E);
 int marie_dipole_field(const double* r, int64_t L, int64_t M, int64_t N, double ko,
                        const double* Jd, const double* pos, int64_t ndip, double* E);
+
+/* Comparison build (no counterpart in the reference): the FP32 'notransp'
+ * mv_AN through cuFFT (zero-padded arrays, batched 3-D transforms, full
+ * operator), the sequence of mv_AN.m:101-131 on a gpuArray.  *ms returns the
+ * device time of the matvec proper (padding to epilogue).  Keeps its cuFFT plan
+ * and buffers with the plan after the first call. */
+int marie_mv_AN_cufft(marie_plan* plan, const double* JIn0, const double* Mr, const double* Mc,
+                      double Gram, const int64_t* idx, int64_t n_idx, double* JOut, float* ms);
 
 /* Instrumentation (no counterpart in the reference, which times with tic/toc):
  * number of kernels this library has launched since load, and per-pass device

@@ -5,9 +5,12 @@ in include/marie_vie.h); this package is the reference-facing host API.
 """
 from ._lib import MARIE_FP32, MARIE_FP64, MARIE_MIXED, MarieError, load  # noqa: F401
 from .vie import (EMconstants, E_field_Nop, JVIE_Solver, JVIE_Solver_batch, JVIE_Solver_bodies, Operator,  # noqa: F401,E501
-                  PlaneWave_Excitation, Dipole_Excitation, bicgstab, getOPERATORS, mv_AN, mv_L, pgmres, pgmresDR,
-                  singular_integrals)
+                  Scat_Solver,
+                  PlaneWave_Excitation, Dipole_Excitation, H_field_Kop, bicgstab, getOPERATORS, mv_AN, mv_K, mv_L,
+                  pgmres, pgmresDR, singular_integrals)
 
 __all__ = ["EMconstants", "E_field_Nop", "JVIE_Solver", "JVIE_Solver_batch", "Operator", "PlaneWave_Excitation",
-           "Dipole_Excitation", "bicgstab", "getOPERATORS", "mv_AN", "mv_L", "pgmres", "pgmresDR", "singular_integrals",
+           "Scat_Solver",
+           "Dipole_Excitation", "H_field_Kop", "bicgstab", "getOPERATORS", "mv_AN", "mv_K", "mv_L", "pgmres", "pgmresDR",
+           "singular_integrals",
            "MarieError", "load"]

@@ -46,8 +46,13 @@ SIGNATURES = {
     "marie_set_operator": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, C.c_int64]),
     "marie_plan_assemble": (C.c_int, [_vp, C.c_double, C.c_double, C.c_char, _vp]),
     "marie_get_plan_operator": (C.c_int, [_vp, _vp]),
+    "marie_set_operator_k": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, C.c_int64]),
+    "marie_plan_assemble_k": (C.c_int, [_vp, C.c_double, C.c_double]),
+    "marie_mv_K": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, C.c_int64, C.c_int]),
+    "marie_h_field_kop": (C.c_int, [_vp, _vp, C.c_double, _vp, _vp, C.c_int]),
     "marie_mv_AN": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, C.c_int, _vp, C.c_int64, _vp, C.c_int64, C.c_int]),
     "marie_mv_AN_static": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, C.c_int, _vp, C.c_int64, _vp, C.c_int]),
+    "marie_mv_AN_cufft": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, _vp, C.c_int64, _vp, C.POINTER(C.c_float)]),
     "marie_mv_L": (C.c_int, [_vp, _vp, C.c_double, _vp, C.c_int64, _vp, C.c_int64, C.c_int]),
     "marie_pgmres": (C.c_int, [_vp, OP_FN, _vp, _vp, C.c_int64, C.c_int, C.c_double, C.c_int,
                                OP_FN, _vp, OP_FN, _vp, OP_FN, _vp, OP_FN, _vp,
@@ -60,6 +65,9 @@ SIGNATURES = {
     "marie_jvie_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_char, C.c_char,
                                    C.c_int, C.c_int, C.c_int, C.c_int, _vp, _ip, _dp, _dp, _dp, C.c_int64, _i64p,
                                    _dp]),
+    "marie_scat_solver": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, _vp, _vp, _vp, C.c_double, C.c_int,
+                                    C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp,
+                                    _dp, _dp]),
     "marie_jvie_solve_bodies": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, C.c_char,
                                           C.c_double, C.c_int, C.c_int, _vp, _ip, _dp, _ip, _dp]),
     "marie_jvie_adjoint_grad": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_int, _vp, C.c_double, C.c_int,

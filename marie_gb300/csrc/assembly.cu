@@ -113,7 +113,7 @@ struct CubArgs {
   double face_o[6][3], face_a[6][3], face_b[6][3];
   double P[6][6][6];  // vector_projection.m: P(i,j,k)
   double2 sing[5];    // ST, EAc, EAo, VAc, VAo
-  double ko, dx, scale;  // scale = dx^4 / (4 pi)
+  double ko, dx, scale;  // K: the factor dx^4 / (j k0)^2 / (4 pi) of assembly_kop.m
   int L, M, N;
 };
 
@@ -548,8 +548,8 @@ static int assemble_toeplitz(int L, int M, int N, double dx, double ko, const do
   return MARIE_OK;
 }
 
-// Forward 3-D FFT in place of the 6 components of a 2L x 2M x 2N circulant.
-static int fft_operator(double2* C, int Lp, int Mp, int Np, cudaStream_t st) {
+// Forward 3-D FFT in place of the nq components of a 2L x 2M x 2N circulant.
+static int fft_operator(double2* C, int Lp, int Mp, int Np, cudaStream_t st, int nq = 6) {
   std::vector<double2*> tw(3, nullptr);
   const int lens[3] = {Lp, Mp, Np};
   std::vector<DBuf> twb(3);
@@ -564,15 +564,276 @@ static int fft_operator(double2* C, int Lp, int Mp, int Np, cudaStream_t st) {
     tw[a] = twb[a].as<double2>();
   }
   const long long P = (long long)Lp * Mp * Np;
-  MARIE_CUDA_TRY(rows_full(Lp, C, 6 * P / Lp, tw[0], st));
+  MARIE_CUDA_TRY(rows_full(Lp, C, nq * P / Lp, tw[0], st));
   using ML = MatvecLaunch<double>;
   // y: columns of S consecutive x, stride Lp, w = (z, q)
-  MARIE_CUDA_TRY(ML::cols(false, Mp, C, (long long)Lp * Mp, 0, Mp, C, (long long)Lp * Mp, 0, Mp, Lp, 6 * Np,
+  MARIE_CUDA_TRY(ML::cols(false, Mp, C, (long long)Lp * Mp, 0, Mp, C, (long long)Lp * Mp, 0, Mp, Lp, nq * Np,
                           tw[1], 1, st));
   // z: columns over the contiguous (x, y) plane, stride Lp*Mp, w = q
-  MARIE_CUDA_TRY(ML::cols(false, Np, C, P, 0, Np, C, P, 0, Np, Lp * Mp, 6, tw[2], 1, st));
+  MARIE_CUDA_TRY(ML::cols(false, Np, C, P, 0, Np, C, P, 0, Np, Lp * Mp, nq, tw[2], 1, st));
   MARIE_CUDA_TRY(cudaStreamSynchronize(st));
   return MARIE_OK;
+}
+
+// --------------------------------------------------------------------------
+// K operator: getOPERATORS(r, f, 'K') (getOPERATORS.m:101-120)
+//   Toeplitz IK_mn(mx,my,mz,1..3) = dx^4 / (j k0)^2 / (4 pi) * I(m) with
+//   (assembly_kop.m:7-120)
+//     far    : every offset, 4-point rule, the 12 signed face pairs of
+//              cubature_kop.cpp:30-32 of sum w_p w_q G(R) (r_p - r_q),
+//              G = (1 - exp(-j k0 R)(1 + j k0 R)) / R^3
+//     medium : offsets < 5 per axis, the same with the 10-point rule
+//     near   : offsets < 2 per axis, 20-point rule on all 36 face pairs (21
+//              integrated, 15 copies as for N), the coincident pairs dropped
+//              (nearby_correct_kop.m) and the face-normal combination of
+//              cubature_kop_near_sym.m:91-105
+//   circulant with component c odd along axis c (circulant_kop.m,
+//   gperiodic_coeff_kop.m), then the FFT of the 3 components.
+// --------------------------------------------------------------------------
+__constant__ int c_kop_obs[12] = {0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5};
+__constant__ int c_kop_src[12] = {0, 1, 0, 1, 2, 3, 2, 3, 4, 5, 4, 5};
+__constant__ double c_kop_sign[12] = {1, -1, -1, 1, 1, -1, -1, 1, 1, -1, -1, 1};
+
+// sum over point pairs of w_p w_q G(R) (r_p - r_q) for one face pair
+__device__ void kop_pair_sum(const CubArgs& A, const double* __restrict__ w, const double* __restrict__ u,
+                             const double* __restrict__ v, int Np, int io, int is, const double rm[3], int lane,
+                             int nl, double2 out[3]) {
+  out[0] = out[1] = out[2] = mk<double2>(0, 0);
+  const double* po = A.face_o[io];
+  const double* pa = A.face_a[io];
+  const double* pb = A.face_b[io];
+  const double* qo = A.face_o[is];
+  const double* qa = A.face_a[is];
+  const double* qb = A.face_b[is];
+  const long long tot = (long long)Np * Np;
+  for (long long t = lane; t < tot; t += nl) {
+    const int ip = (int)(t / Np), iq = (int)(t - (long long)ip * Np);
+    const double up = u[ip], vp = v[ip], uq = u[iq], vq = v[iq];
+    double d[3];
+    for (int c = 0; c < 3; ++c)
+      d[c] = (po[c] + pa[c] * up + pb[c] * vp + rm[c]) - (qo[c] + qa[c] * uq + qb[c] * vq);
+    const double R = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double kR = A.ko * R;
+    double sn, cs;
+    sincos(kR, &sn, &cs);
+    // 1 - exp(-j kR) (1 + j kR) = (1 - cs - kR sn) - j (kR cs - sn)
+    const double R3 = R * R * R;
+    const double wt = w[ip] * w[iq] / R3;
+    const double gr = wt * (1.0 - cs - kR * sn), gi = -wt * (kR * cs - sn);
+    for (int c = 0; c < 3; ++c) {
+      out[c].x += gr * d[c];
+      out[c].y += gi * d[c];
+    }
+  }
+}
+
+// far field: one warp per offset outside the medium region; writes I (3 comps)
+__global__ void k_kop_far(CubArgs A, const double* __restrict__ gw, const double* __restrict__ gu,
+                          const double* __restrict__ gv, int Np, int n_medium, double2* __restrict__ K) {
+  __shared__ double w[16], u[16], v[16];
+  if (threadIdx.x < Np) {
+    w[threadIdx.x] = gw[threadIdx.x];
+    u[threadIdx.x] = gu[threadIdx.x];
+    v[threadIdx.x] = gv[threadIdx.x];
+  }
+  __syncthreads();
+  const long long V = (long long)A.L * A.M * A.N;
+  const int lane = threadIdx.x & 31;
+  const long long wpb = blockDim.x >> 5;
+  for (long long off = blockIdx.x * wpb + (threadIdx.x >> 5); off < V; off += (long long)gridDim.x * wpb) {
+    const int mx = (int)(off % A.L);
+    const int my = (int)((off / A.L) % A.M);
+    const int mz = (int)(off / ((long long)A.L * A.M));
+    if (mx < n_medium && my < n_medium && mz < n_medium) continue;
+    const double rm[3] = {mx * A.dx, my * A.dx, mz * A.dx};
+    // signed lane sums over the 12 pairs, one warp reduction per component
+    double2 acc[3] = {mk<double2>(0, 0), mk<double2>(0, 0), mk<double2>(0, 0)};
+    for (int p = 0; p < 12; ++p) {
+      double2 o[3];
+      kop_pair_sum(A, w, u, v, Np, c_kop_obs[p], c_kop_src[p], rm, lane, 32, o);
+      for (int c = 0; c < 3; ++c) acc[c] = cadd(acc[c], cscale(o[c], c_kop_sign[p]));
+    }
+    for (int c = 0; c < 3; ++c) acc[c] = warp_sum2(acc[c]);
+    if (lane == 0)
+      for (int c = 0; c < 3; ++c) K[c * V + off] = cscale(acc[c], A.scale);
+  }
+}
+
+// medium (near = false: the 12 signed pairs) or near (the 21 pairs of the
+// symmetric set): one block per (offset, pair); out[o][pair][3]
+__global__ void k_kop_region(CubArgs A, const double* __restrict__ gw, const double* __restrict__ gu,
+                             const double* __restrict__ gv, int Np, int nr, bool near, double2* __restrict__ out) {
+  extern __shared__ double sh[];
+  double* w = sh;
+  double* u = sh + Np;
+  double* v = sh + 2 * Np;
+  for (int i = threadIdx.x; i < Np; i += blockDim.x) {
+    w[i] = gw[i];
+    u[i] = gu[i];
+    v[i] = gv[i];
+  }
+  __syncthreads();
+  const int pair = blockIdx.y;
+  const int o = blockIdx.x;
+  const int mx = o % nr, my = (o / nr) % nr, mz = o / (nr * nr);
+  const double rm[3] = {mx * A.dx, my * A.dx, mz * A.dx};
+  const int io = near ? c_pair_obs[pair] : c_kop_obs[pair];
+  const int is = near ? c_pair_src[pair] : c_kop_src[pair];
+  double2 acc[3];
+  kop_pair_sum(A, w, u, v, Np, io, is, rm, threadIdx.x, blockDim.x, acc);
+  __shared__ double2 ws[3][32];
+  for (int c = 0; c < 3; ++c) {
+    const double2 r = warp_sum2(acc[c]);
+    if ((threadIdx.x & 31) == 0) ws[c][threadIdx.x >> 5] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double2 t = mk<double2>(0, 0);
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t = cadd(t, ws[threadIdx.x][i]);
+    out[((long long)o * (near ? 21 : 12) + pair) * 3 + threadIdx.x] = t;
+  }
+}
+
+__global__ void k_kop_finish(CubArgs A, const double2* __restrict__ I, int nr, bool near, double2* __restrict__ K) {
+  const long long V = (long long)A.L * A.M * A.N;
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= nr * nr * nr) return;
+  const int mx = o % nr, my = (o / nr) % nr, mz = o / (nr * nr);
+  if (mx >= A.L || my >= A.M || mz >= A.N) return;
+  const long long off = mx + (long long)A.L * (my + (long long)A.M * mz);
+  double2 r[3] = {mk<double2>(0, 0), mk<double2>(0, 0), mk<double2>(0, 0)};
+  if (!near) {
+    for (int p = 0; p < 12; ++p)
+      for (int c = 0; c < 3; ++c) r[c] = cadd(r[c], cscale(I[((long long)o * 12 + p) * 3 + c], c_kop_sign[p]));
+  } else {
+    // I(6,6,3): the 21 integrated pairs, the 15 copies, coincident pairs dropped
+    double2 F[6][6][3];
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j)
+        for (int c = 0; c < 3; ++c) F[i][j][c] = mk<double2>(0, 0);
+    for (int p = 0; p < 21; ++p)
+      for (int c = 0; c < 3; ++c) F[c_pair_obs[p]][c_pair_src[p]][c] = I[((long long)o * 21 + p) * 3 + c];
+    for (int q = 0; q < 15; ++q)
+      for (int c = 0; c < 3; ++c) F[c_copy_dst[q][0]][c_copy_dst[q][1]][c] = F[c_copy_src[q][0]][c_copy_src[q][1]][c];
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j)
+        if (near_class(mx, my, mz, i, j) == 1)
+          for (int c = 0; c < 3; ++c) F[i][j][c] = mk<double2>(0, 0);
+    // J(i,:) = -/+ I(i,:,axis(i)); IK_c = sum_i J(i, 2c+1) - J(i, 2c)
+    for (int i = 0; i < 6; ++i) {
+      const double sg = (i % 2) ? 1.0 : -1.0;
+      for (int c = 0; c < 3; ++c) r[c] = cadd(r[c], cscale(csub(F[i][2 * c + 1][i / 2], F[i][2 * c][i / 2]), sg));
+    }
+  }
+  for (int c = 0; c < 3; ++c) K[c * V + off] = cscale(r[c], A.scale);
+}
+
+// circulant_kop.m:17-41: component c odd along axis c; index L stays zero
+__global__ void k_circulant_k(const double2* __restrict__ G, int L, int M, int N, double2* __restrict__ C) {
+  const long long Lp = 2LL * L, Mp = 2LL * M, Np = 2LL * N;
+  const long long P = Lp * Mp * Np;
+  const long long V = (long long)L * M * N;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 3 * P; t += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(t / P);
+    long long r = t - q * P;
+    const int ix = (int)(r % Lp);
+    r /= Lp;
+    const int iy = (int)(r % Mp);
+    const int iz = (int)(r / Mp);
+    double sgn = 1.0;
+    int sx = ix, sy = iy, sz = iz;
+    bool zero = false;
+    if (ix == L) zero = true; else if (ix > L) { sx = (int)(Lp - ix); if (q == 0) sgn = -sgn; }
+    if (iy == M) zero = true; else if (iy > M) { sy = (int)(Mp - iy); if (q == 1) sgn = -sgn; }
+    if (iz == N) zero = true; else if (iz > N) { sz = (int)(Np - iz); if (q == 2) sgn = -sgn; }
+    double2 val = mk<double2>(0, 0);
+    if (!zero) {
+      val = G[q * V + sx + (long long)L * (sy + (long long)M * sz)];
+      val = mk<double2>(sgn * val.x, sgn * val.y);
+    }
+    C[t] = val;
+  }
+}
+
+// Toeplitz K (L x M x N x 3) on the device.
+static int assemble_toeplitz_k(int L, int M, int N, double dx, double ko, double2* K, cudaStream_t st) {
+  CubArgs A{};
+  const FaceGeom fg = make_faces(dx);
+  for (int f = 0; f < 6; ++f)
+    for (int c = 0; c < 3; ++c) {
+      A.face_o[f][c] = fg.o[f][c];
+      A.face_a[f][c] = fg.a[f][c];
+      A.face_b[f][c] = fg.b[f][c];
+    }
+  A.ko = ko;
+  A.dx = dx;
+  A.scale = -dx * dx * dx * dx / (4.0 * M_PI * ko * ko);  // dx^4 / (j k0)^2 / (4 pi)
+  A.L = L; A.M = M; A.N = N;
+  const int n_medium = 5;
+  struct Rule { DBuf w, u, v; int Np; };
+  Rule rules[3];
+  const int orders[3] = {4, 10, 20};
+  for (int r = 0; r < 3; ++r) {
+    std::vector<double> w, u, v;
+    gauss_2d(orders[r], w, u, v);
+    rules[r].Np = (int)w.size();
+    MARIE_TRY(rules[r].w.alloc(w.size() * sizeof(double), st));
+    MARIE_TRY(rules[r].u.alloc(w.size() * sizeof(double), st));
+    MARIE_TRY(rules[r].v.alloc(w.size() * sizeof(double), st));
+    MARIE_CUDA_TRY(cudaMemcpyAsync(rules[r].w.p, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    MARIE_CUDA_TRY(cudaMemcpyAsync(rules[r].u.p, u.data(), u.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    MARIE_CUDA_TRY(cudaMemcpyAsync(rules[r].v.p, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  const long long V = (long long)L * M * N;
+  {
+    const int warps = 8;
+    long long blocks = (V + warps - 1) / warps;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    k_kop_far<<<(unsigned)blocks, 32 * warps, 0, st>>>(A, rules[0].w.as<double>(), rules[0].u.as<double>(),
+                                                       rules[0].v.as<double>(), rules[0].Np, n_medium, K);
+    count_launch();
+    MARIE_CUDA_TRY(cudaGetLastError());
+  }
+  // medium (10-point rule, 12 pairs) then near (20-point rule, 21 pairs); the
+  // MATLAB loops run 1:5 and 1:2 per axis, offsets beyond the grid are dropped
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool near = pass == 1;
+    const int nr = near ? 2 : n_medium;
+    const int npairs = near ? 21 : 12;
+    Rule& R = rules[pass + 1];
+    const int nO = nr * nr * nr;
+    DBuf I;
+    MARIE_TRY(I.alloc((size_t)nO * npairs * 3 * sizeof(double2), st));
+    dim3 grid(nO, npairs);
+    k_kop_region<<<grid, 256, 3 * R.Np * sizeof(double), st>>>(A, R.w.as<double>(), R.u.as<double>(),
+                                                              R.v.as<double>(), R.Np, nr, near, I.as<double2>());
+    count_launch();
+    MARIE_CUDA_TRY(cudaGetLastError());
+    k_kop_finish<<<(nO + 127) / 128, 128, 0, st>>>(A, I.as<double2>(), nr, near, K);
+    count_launch();
+    MARIE_CUDA_TRY(cudaGetLastError());
+    MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  return MARIE_OK;
+}
+
+int assemble_k_device(int L, int M, int N, double dx, double freq, char type, double2* out, cudaStream_t st) {
+  const double ko = 2.0 * M_PI / 299792458.0 * freq;  // getOPERATORS.m:48
+  const long long V = (long long)L * M * N;
+  if (type == 'T') return assemble_toeplitz_k(L, M, N, dx, ko, out, st);
+  DBuf G;
+  MARIE_TRY(G.alloc(3 * V * sizeof(double2), st));
+  MARIE_TRY(assemble_toeplitz_k(L, M, N, dx, ko, G.as<double2>(), st));
+  const long long P = 8 * V;
+  k_circulant_k<<<(unsigned)std::min<long long>((3 * P + 255) / 256, 152 * 32), 256, 0, st>>>(G.as<double2>(), L, M,
+                                                                                              N, out);
+  count_launch();
+  MARIE_CUDA_TRY(cudaGetLastError());
+  if (type == 'C') {
+    MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+    return MARIE_OK;
+  }
+  return fft_operator(out, 2 * L, 2 * M, 2 * N, st, 3);
 }
 
 static int get_sing(char singular, const double* user, double ko, double dx, double2 s[5], cudaStream_t st) {
@@ -627,7 +888,7 @@ int marie_singular_integrals(double ko, double dx, double* out10) {
 int marie_get_operators(const double* r, int64_t L, int64_t M, int64_t N, double f, char op, char type,
                         char singular, const double* singular_values, double* op_out) {
   if (!r || !op_out) return set_error(MARIE_EINVAL, "NULL argument");
-  if (op != 'N') return set_error(MARIE_EUNSUPPORTED, "only the N operator is built");
+  if (op != 'N' && op != 'K') return set_error(MARIE_EINVAL, "op must be 'N' or 'K'");
   if (type != 'F' && type != 'C' && type != 'T') return set_error(MARIE_EINVAL, "type must be 'F', 'C' or 'T'");
   if (L < 2) return set_error(MARIE_EINVAL, "L must be >= 2 to read dx from r");
   if (type != 'T' && (!fft_length_supported((int)(2 * L)) || !fft_length_supported((int)(2 * M)) ||
@@ -639,11 +900,16 @@ int marie_get_operators(const double* r, int64_t L, int64_t M, int64_t N, double
   if (!(dx > 0)) return set_error(MARIE_EINVAL, "r must have increasing x coordinates");
   cudaStream_t st = 0;
   const long long V = L * M * N;
-  const size_t bytes = (type == 'T' ? 6 * V : 48 * V) * sizeof(double2);
+  const long long nq = op == 'N' ? 6 : 3;
+  const size_t bytes = (type == 'T' ? nq * V : 8 * nq * V) * sizeof(double2);
   DBuf tmp;
   void* dev;
   MARIE_TRY(stage_out(op_out, bytes, st, tmp, &dev));
-  MARIE_TRY(assemble_operator_device((int)L, (int)M, (int)N, dx, f, singular, singular_values, type, (double2*)dev, st));
+  if (op == 'K')
+    MARIE_TRY(assemble_k_device((int)L, (int)M, (int)N, dx, f, type, (double2*)dev, st));
+  else
+    MARIE_TRY(assemble_operator_device((int)L, (int)M, (int)N, dx, f, singular, singular_values, type,
+                                       (double2*)dev, st));
   MARIE_TRY(finish_out(op_out, dev, bytes, st));
   MARIE_CUDA_TRY(cudaStreamSynchronize(st));
   return MARIE_OK;
@@ -657,6 +923,15 @@ int marie_plan_assemble(marie_plan* p, double dx, double freq, char singular, co
   MARIE_TRY(assemble_operator_device(p->d.L, p->d.M, p->d.N, dx, freq, singular, singular_values, 'F',
                                      F.as<double2>(), p->stream));
   return install_operator(p, F.as<double2>());
+}
+
+int marie_plan_assemble_k(marie_plan* p, double dx, double freq) {
+  if (!p) return set_error(MARIE_EINVAL, "NULL plan");
+  if (!(dx > 0) || !(freq > 0)) return set_error(MARIE_EINVAL, "dx and freq must be positive");
+  DBuf F;
+  MARIE_TRY(F.alloc((size_t)24 * p->d.V * sizeof(double2), p->stream));
+  MARIE_TRY(assemble_k_device(p->d.L, p->d.M, p->d.N, dx, freq, 'F', F.as<double2>(), p->stream));
+  return install_operator(p, F.as<double2>(), 1);
 }
 
 }  // extern "C"

@@ -220,7 +220,8 @@ int build_coefficients(marie_plan* p, const int64_t* idx_dev, long long n, const
 template <typename T>
 static int run_matvec_t(marie_plan* p, const double2* J, long long js, double2* out, long long os, long long n,
                         int nrhs, const int* inv, const Prologue& pro, const Epilogue& ep, const cplx<T>* fN,
-                        cplx<T>* const* tw, const int* stop, int step) {
+                        cplx<T>* const* tw, const int* stop, int step, int kind) {
+  const int oct = kind == 0 ? p->oct : p->octK;
   using ML = MatvecLaunch<T>;
   const int prec = sizeof(T) == 4 ? MARIE_FP32 : MARIE_FP64;
   const long long chunk_max = p->nrhs_max > 0 ? p->nrhs_max : 1;
@@ -244,7 +245,7 @@ static int run_matvec_t(marie_plan* p, const double2* J, long long js, double2* 
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[1], p->stream));
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
       }
-      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, p->oct, d, tw[2], nr, p->stream));
+      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, oct, d, tw[2], nr, p->stream, kind));
       if (prof) {
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[4], p->stream));
@@ -257,7 +258,7 @@ static int run_matvec_t(marie_plan* p, const double2* J, long long js, double2* 
       MARIE_CUDA_TRY(ML::cols(false, d.Mp, A, (long long)d.Lp * d.M, sA, d.M, B, (long long)d.Lp * d.Mp, sB, d.Mp,
                               d.Lp, 3 * d.N, tw[1], nr, p->stream, d.stop, step));
       if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
-      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, p->oct, d, tw[2], nr, p->stream));
+      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, oct, d, tw[2], nr, p->stream, kind));
       if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
       MARIE_CUDA_TRY(ML::cols(true, d.Mp, B, (long long)d.Lp * d.Mp, sB, d.Mp, A, (long long)d.Lp * d.M, sA, d.M,
                               d.Lp, 3 * d.N, tw[1], nr, p->stream, d.stop, step));
@@ -280,14 +281,20 @@ static int run_matvec_t(marie_plan* p, const double2* J, long long js, double2* 
 }
 
 int run_matvec(marie_plan* p, int prec, const double2* J, long long js, double2* out, long long os, long long n,
-               int nrhs, const int* inv, const Prologue& pro, const Epilogue& ep, const int* stop, int step) {
-  if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator: call marie_set_operator or marie_plan_assemble");
+               int nrhs, const int* inv, const Prologue& pro, const Epilogue& ep, const int* stop, int step,
+               int kind) {
+  if (kind == 0 && !p->has_op)
+    return set_error(MARIE_ENOOP, "plan has no operator: call marie_set_operator or marie_plan_assemble");
+  if (kind == 1 && !p->has_opK)
+    return set_error(MARIE_ENOOP, "plan has no K operator: call marie_set_operator_k or marie_plan_assemble_k");
+  const float2* f32 = kind == 0 ? p->fN32 : p->fK32;
+  const double2* f64 = kind == 0 ? p->fN64 : p->fK64;
   if (prec == MARIE_FP32) {
-    if (!p->fN32) return set_error(MARIE_EINVAL, "plan was not created with FP32 arithmetic");
-    return run_matvec_t<float>(p, J, js, out, os, n, nrhs, inv, pro, ep, p->fN32, p->tw32, stop, step);
+    if (!f32) return set_error(MARIE_EINVAL, "plan was not created with FP32 arithmetic");
+    return run_matvec_t<float>(p, J, js, out, os, n, nrhs, inv, pro, ep, f32, p->tw32, stop, step, kind);
   }
-  if (!p->fN64) return set_error(MARIE_EINVAL, "plan was not created with FP64 arithmetic");
-  return run_matvec_t<double>(p, J, js, out, os, n, nrhs, inv, pro, ep, p->fN64, p->tw64, stop, step);
+  if (!f64) return set_error(MARIE_EINVAL, "plan was not created with FP64 arithmetic");
+  return run_matvec_t<double>(p, J, js, out, os, n, nrhs, inv, pro, ep, f64, p->tw64, stop, step, kind);
 }
 
 int run_matvec(marie_plan* p, int prec, const double2* J, double2* out, long long n, int nrhs, const int* inv,
@@ -317,24 +324,28 @@ __global__ void k_scale_convert(const double2* in, long long n, double s, double
 }
 
 // parity of component q along axis a (0 x, 1 y, 2 z): true = odd
-__host__ __device__ inline bool comp_odd(int q, int a) {
-  return a == 0 ? (q == 1 || q == 2) : (a == 1 ? (q == 1 || q == 4) : (q == 2 || q == 4));
+// component q of operator kind (0: N, 6 components; 1: K, 3) odd along axis a
+__host__ __device__ inline bool comp_odd(int kind, int q, int a) {
+  return kind == 0 ? OpKind<0>::odd(q, a) : OpKind<1>::odd(q, a);
 }
+__host__ __device__ inline int comp_count(int kind) { return kind == 0 ? 6 : 3; }
 
 // max |fN(k) - s fN(mirror k)| and max |fN(k)| over the full operator (as the
 // bit patterns of non-negative doubles, which order like the values).
-__global__ void k_symmetry_check(const double2* __restrict__ f, int L, int M, int N,
+__global__ void k_symmetry_check(const double2* __restrict__ f, int L, int M, int N, int kind,
                                  unsigned long long* __restrict__ out) {
+  const int NQ = comp_count(kind);
   const long long Lp = 2LL * L, Mp = 2LL * M, Np = 2LL * N, P = Lp * Mp * Np;
   double dev = 0, mx = 0;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 6 * P; t += (long long)gridDim.x * blockDim.x) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < NQ * P; t += (long long)gridDim.x * blockDim.x) {
     const int q = (int)(t / P);
     long long r = t - q * P;
     const long long ix = r % Lp;
     r /= Lp;
     const long long iy = r % Mp, iz = r / Mp;
     const long long jx = ix > L ? Lp - ix : ix, jy = iy > M ? Mp - iy : iy, jz = iz > N ? Np - iz : iz;
-    const bool neg = ((ix > L) && comp_odd(q, 0)) ^ ((iy > M) && comp_odd(q, 1)) ^ ((iz > N) && comp_odd(q, 2));
+    const bool neg = ((ix > L) && comp_odd(kind, q, 0)) ^ ((iy > M) && comp_odd(kind, q, 1)) ^
+                     ((iz > N) && comp_odd(kind, q, 2));
     const double2 a = f[t];
     double2 b = f[q * P + jx + Lp * (jy + Mp * jz)];
     if (neg) b = mk<double2>(-b.x, -b.y);
@@ -351,12 +362,12 @@ __global__ void k_symmetry_check(const double2* __restrict__ f, int L, int M, in
   }
 }
 
-// octant (L+1) x (M+1) x (N+1) x 6 of the full operator, scaled, in FP64 and/or FP32
-__global__ void k_extract_octant(const double2* __restrict__ f, int L, int M, int N, double s, double2* o64,
+// octant (L+1) x (M+1) x (N+1) x NQ of the full operator, scaled, in FP64 and/or FP32
+__global__ void k_extract_octant(const double2* __restrict__ f, int L, int M, int N, int NQ, double s, double2* o64,
                                  float2* o32) {
   const long long Lp = 2LL * L, Mp = 2LL * M, Np = 2LL * N, P = Lp * Mp * Np;
   const long long Lo = L + 1, Mo = M + 1, No = N + 1, O = Lo * Mo * No;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 6 * O; t += (long long)gridDim.x * blockDim.x) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < NQ * O; t += (long long)gridDim.x * blockDim.x) {
     const int q = (int)(t / O);
     long long r = t - q * O;
     const long long ox = r % Lo;
@@ -369,36 +380,42 @@ __global__ void k_extract_octant(const double2* __restrict__ f, int L, int M, in
 }
 
 // full operator from the octant (inverse of k_extract_octant), scaled by s
-__global__ void k_expand_octant(const double2* __restrict__ o, int L, int M, int N, double s, double2* __restrict__ f) {
+__global__ void k_expand_octant(const double2* __restrict__ o, int L, int M, int N, int kind, double s,
+                                double2* __restrict__ f) {
   const long long Lp = 2LL * L, Mp = 2LL * M, Np = 2LL * N, P = Lp * Mp * Np;
   const long long Lo = L + 1, Mo = M + 1, No = N + 1, O = Lo * Mo * No;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 6 * P; t += (long long)gridDim.x * blockDim.x) {
+  const int NQ = comp_count(kind);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < NQ * P; t += (long long)gridDim.x * blockDim.x) {
     const int q = (int)(t / P);
     long long r = t - q * P;
     const long long ix = r % Lp;
     r /= Lp;
     const long long iy = r % Mp, iz = r / Mp;
     const long long jx = ix > L ? Lp - ix : ix, jy = iy > M ? Mp - iy : iy, jz = iz > N ? Np - iz : iz;
-    const bool neg = ((ix > L) && comp_odd(q, 0)) ^ ((iy > M) && comp_odd(q, 1)) ^ ((iz > N) && comp_odd(q, 2));
+    const bool neg = ((ix > L) && comp_odd(kind, q, 0)) ^ ((iy > M) && comp_odd(kind, q, 1)) ^
+                     ((iz > N) && comp_odd(kind, q, 2));
     double2 v = o[q * O + jx + Lo * (jy + Mo * jz)];
     const double sg = neg ? -s : s;
     f[t] = mk<double2>(v.x * sg, v.y * sg);
   }
 }
 
-// Installs fN (full layout, device) into the plan: the octant when fN has the
-// circulant's parity symmetry to 1e-12 of its maximum (every operator built
-// by getOPERATORS does), the full array otherwise.  Scaled by 1/(8LMN).
-int install_operator(marie_plan* p, const double2* fN_dev) {
+// Installs an operator (full layout, device) into the plan: the octant when it
+// has the circulant's parity symmetry to 1e-12 of its maximum (every operator
+// built by getOPERATORS does), the full array otherwise.  Scaled by 1/(8LMN).
+// kind 0: N (6 components, fN64/fN32), 1: K (3 components, fK64/fK32).
+int install_operator(marie_plan* p, const double2* fN_dev, int kind) {
   const Dims& d = p->d;
   const long long P = (long long)d.Lp * d.Mp * d.Np;
   const long long O = (long long)(d.L + 1) * (d.M + 1) * (d.N + 1);
+  const int NQ = comp_count(kind);
   const bool need64 = p->precision != MARIE_FP32;
   const bool need32 = p->precision != MARIE_FP64;
   DBuf flags;
   MARIE_TRY(flags.alloc(2 * sizeof(unsigned long long), p->stream));
   MARIE_CUDA_TRY(cudaMemsetAsync(flags.p, 0, 2 * sizeof(unsigned long long), p->stream));
-  k_symmetry_check<<<grid_for(6 * P), 256, 0, p->stream>>>(fN_dev, d.L, d.M, d.N, flags.as<unsigned long long>());
+  k_symmetry_check<<<grid_for(NQ * P), 256, 0, p->stream>>>(fN_dev, d.L, d.M, d.N, kind,
+                                                            flags.as<unsigned long long>());
   count_launch();
   unsigned long long h[2];
   MARIE_CUDA_TRY(cudaMemcpyAsync(h, flags.p, sizeof(h), cudaMemcpyDeviceToHost, p->stream));
@@ -407,25 +424,37 @@ int install_operator(marie_plan* p, const double2* fN_dev) {
   memcpy(&dev, &h[0], sizeof(double));
   memcpy(&mx, &h[1], sizeof(double));
   const int oct = (dev <= 1e-12 * mx) ? 1 : 0;
-  const long long n = oct ? 6 * O : 6 * P;
-  cudaFree(p->fN64);
-  cudaFree(p->fN32);
-  p->fN64 = nullptr;
-  p->fN32 = nullptr;
-  if (need64) MARIE_CUDA_TRY(cudaMalloc(&p->fN64, n * sizeof(double2)));
-  if (need32) MARIE_CUDA_TRY(cudaMalloc(&p->fN32, n * sizeof(float2)));
+  const long long n = oct ? NQ * O : NQ * P;
+  if (kind == 0) release_cufft_state(p);  // its full copy of fN is stale now
+  double2*& f64 = kind == 0 ? p->fN64 : p->fK64;
+  float2*& f32 = kind == 0 ? p->fN32 : p->fK32;
+  cudaFree(f64);
+  cudaFree(f32);
+  f64 = nullptr;
+  f32 = nullptr;
+  if (kind == 0)
+    p->has_op = false;
+  else
+    p->has_opK = false;
+  if (need64) MARIE_CUDA_TRY(cudaMalloc(&f64, n * sizeof(double2)));
+  if (need32) MARIE_CUDA_TRY(cudaMalloc(&f32, n * sizeof(float2)));
   if (oct) {
-    k_extract_octant<<<grid_for(n), 256, 0, p->stream>>>(fN_dev, d.L, d.M, d.N, 1.0 / (double)P,
-                                                         need64 ? p->fN64 : nullptr, need32 ? p->fN32 : nullptr);
+    k_extract_octant<<<grid_for(n), 256, 0, p->stream>>>(fN_dev, d.L, d.M, d.N, NQ, 1.0 / (double)P,
+                                                         need64 ? f64 : nullptr, need32 ? f32 : nullptr);
   } else {
-    k_scale_convert<<<grid_for(n), 256, 0, p->stream>>>(fN_dev, n, 1.0 / (double)P, need64 ? p->fN64 : nullptr,
-                                                         need32 ? p->fN32 : nullptr);
+    k_scale_convert<<<grid_for(n), 256, 0, p->stream>>>(fN_dev, n, 1.0 / (double)P, need64 ? f64 : nullptr,
+                                                         need32 ? f32 : nullptr);
   }
   count_launch();
   MARIE_CUDA_TRY(cudaGetLastError());
   MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
-  p->oct = oct;
-  p->has_op = true;
+  if (kind == 0) {
+    p->oct = oct;
+    p->has_op = true;
+  } else {
+    p->octK = oct;
+    p->has_opK = true;
+  }
   return MARIE_OK;
 }
 
@@ -488,11 +517,14 @@ int marie_plan_create(int64_t L, int64_t M, int64_t N, int precision, int64_t nr
 int marie_plan_destroy(marie_plan* p) {
   if (!p) return MARIE_OK;
   if (p->stream) cudaStreamSynchronize(p->stream);
+  release_cufft_state(p);
   if (p->wsA) cudaFreeAsync(p->wsA, p->stream);
   if (p->wsB) cudaFreeAsync(p->wsB, p->stream);
   if (p->stream) cudaStreamSynchronize(p->stream);
   cudaFree(p->fN64);
   cudaFree(p->fN32);
+  cudaFree(p->fK64);
+  cudaFree(p->fK32);
   for (int a = 0; a < 3; ++a) {
     cudaFree(p->tw64[a]);
     cudaFree(p->tw32[a]);
@@ -537,6 +569,18 @@ int marie_set_operator(marie_plan* p, const double* fN, int64_t Lf, int64_t Mf, 
   return install_operator(p, (const double2*)dev);
 }
 
+int marie_set_operator_k(marie_plan* p, const double* fK, int64_t Lf, int64_t Mf, int64_t Nf) {
+  if (!p || !fK) return set_error(MARIE_EINVAL, "NULL plan or operator");
+  if (Lf != p->d.Lp || Mf != p->d.Mp || Nf != p->d.Np)
+    return set_error(MARIE_EINVAL, "operator is %lldx%lldx%lld, plan expects %dx%dx%d", (long long)Lf,
+                     (long long)Mf, (long long)Nf, p->d.Lp, p->d.Mp, p->d.Np);
+  const size_t bytes = (size_t)3 * Lf * Mf * Nf * sizeof(double2);
+  DBuf tmp;
+  const void* dev = nullptr;
+  MARIE_TRY(stage_in(fK, bytes, p->stream, tmp, &dev));
+  return install_operator(p, (const double2*)dev, 1);
+}
+
 int marie_get_plan_operator(marie_plan* p, double* fN_out) {
   if (!p || !fN_out) return set_error(MARIE_EINVAL, "NULL plan or output");
   if (!p->has_op || !p->fN64) return set_error(MARIE_ENOOP, "plan holds no FP64 operator");
@@ -546,7 +590,7 @@ int marie_get_plan_operator(marie_plan* p, double* fN_out) {
   void* dev = nullptr;
   MARIE_TRY(stage_out(fN_out, bytes, p->stream, tmp, &dev));
   if (p->oct)
-    k_expand_octant<<<grid_for(6 * P), 256, 0, p->stream>>>(p->fN64, p->d.L, p->d.M, p->d.N, (double)P,
+    k_expand_octant<<<grid_for(6 * P), 256, 0, p->stream>>>(p->fN64, p->d.L, p->d.M, p->d.N, 0, (double)P,
                                                             (double2*)dev);
   else
     k_scale_convert<<<grid_for(6 * P), 256, 0, p->stream>>>(p->fN64, 6 * P, (double)P, (double2*)dev, nullptr);
@@ -626,6 +670,35 @@ int marie_mv_L(marie_plan* p, const double* JIn0, double Gram, const int64_t* id
   ep.b_s = mk<double2>(-1.0, 0.0);
   if (n > 0)
     MARIE_TRY(run_matvec(p, precision, (const double2*)J_d, (double2*)out_d, n, (int)nrhs, inv.as<int>(), pro, ep));
+  MARIE_TRY(finish_out(JOut, out_d, n * nrhs * sizeof(double2), p->stream));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return MARIE_OK;
+}
+
+int marie_mv_K(marie_plan* p, const double* JIn0, const int64_t* idx, int64_t n_idx, double* JOut, int64_t nrhs,
+               int precision) {
+  if (!p || !JIn0 || !JOut || (!idx && n_idx > 0)) return set_error(MARIE_EINVAL, "NULL argument");
+  if (nrhs < 1) return set_error(MARIE_EINVAL, "nrhs must be >= 1");
+  if (precision != MARIE_FP64 && precision != MARIE_FP32)
+    return set_error(MARIE_EINVAL, "precision must be MARIE_FP64 or MARIE_FP32");
+  if (!p->has_opK) return set_error(MARIE_ENOOP, "plan has no K operator");
+  const long long V = p->d.V, n = n_idx;
+  DBuf tJ, tidx, tout, inv;
+  const void *J_d, *idx_d;
+  void* out_d;
+  MARIE_TRY(stage_in(JIn0, n * nrhs * sizeof(double2), p->stream, tJ, &J_d));
+  MARIE_TRY(stage_in(idx, n * sizeof(int64_t), p->stream, tidx, &idx_d));
+  MARIE_TRY(stage_out(JOut, n * nrhs * sizeof(double2), p->stream, tout, &out_d));
+  MARIE_TRY(inv.alloc(3 * V * sizeof(int), p->stream));
+  MARIE_TRY(build_inverse_index(p, (const int64_t*)idx_d, n, inv.as<int>()));
+  // out = crop(IFFT(fK x FFT(J))): no diagonal term
+  Prologue pro{nullptr, 0};
+  Epilogue ep{};
+  ep.a_s = mk<double2>(0.0, 0.0);
+  ep.b_s = mk<double2>(-1.0, 0.0);
+  if (n > 0)
+    MARIE_TRY(run_matvec(p, precision, (const double2*)J_d, n, (double2*)out_d, n, n, (int)nrhs, inv.as<int>(), pro,
+                         ep, nullptr, 0, 1));
   MARIE_TRY(finish_out(JOut, out_d, n * nrhs * sizeof(double2), p->stream));
   MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
   return MARIE_OK;

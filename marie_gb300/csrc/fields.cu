@@ -135,6 +135,39 @@ int marie_e_field_nop(marie_plan* p, const double* J, double Gram, double freq, 
   return MARIE_OK;
 }
 
+int marie_h_field_kop(marie_plan* p, const double* J, double Gram, const double* Hinc, double* Htot,
+                      int precision) {
+  if (!p || !J || !Htot) return set_error(MARIE_EINVAL, "NULL argument");
+  if (precision != MARIE_FP64 && precision != MARIE_FP32) return set_error(MARIE_EINVAL, "bad precision");
+  if (!p->has_opK) return set_error(MARIE_ENOOP, "plan has no K operator");
+  cudaStream_t st = p->stream;
+  const long long n = 3 * p->d.V;
+  DBuf tJ, tH, tO, inv;
+  const void *J_d, *H_d = nullptr;
+  void* O_d;
+  MARIE_TRY(stage_in(J, n * sizeof(double2), st, tJ, &J_d));
+  if (Hinc) MARIE_TRY(stage_in(Hinc, n * sizeof(double2), st, tH, &H_d));
+  MARIE_TRY(stage_out(Htot, n * sizeof(double2), st, tO, &O_d));
+  MARIE_TRY(inv.alloc(n * sizeof(int), st));
+  k_identity_index<<<grid_n(n), 256, 0, st>>>(inv.as<int>(), n);
+  count_launch();
+  // out = mv_K(J) / Gram (H_field_Kop.m:74-76)
+  Prologue pro{nullptr, 0};
+  Epilogue ep{};
+  ep.a_s = mk<double2>(0.0, 0.0);
+  ep.b_s = mk<double2>(-1.0 / Gram, 0.0);
+  MARIE_TRY(run_matvec(p, precision, (const double2*)J_d, n, (double2*)O_d, n, n, 1, inv.as<int>(), pro, ep,
+                       nullptr, 0, 1));
+  if (Hinc) {
+    k_add_field<<<grid_n(n), 256, 0, st>>>((const double2*)H_d, (double2*)O_d, n);
+    count_launch();
+  }
+  MARIE_CUDA_TRY(cudaGetLastError());
+  MARIE_TRY(finish_out(Htot, O_d, n * sizeof(double2), st));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+  return MARIE_OK;
+}
+
 int marie_plane_wave(const double* r, int64_t L, int64_t M, int64_t N, const double* k, const double* Eo,
                      double* E) {
   if (!r || !k || !Eo || !E || L < 2 || M < 2 || N < 2) return set_error(MARIE_EINVAL, "bad argument");

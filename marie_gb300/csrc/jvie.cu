@@ -571,11 +571,137 @@ static void clamp_solver(SolverArgs& sa, int inner_it) {
   if (sa.ritz > inner_it - 1) sa.ritz = inner_it - 1;
 }
 
+// Scat_Solver post-processing (Scat_Solver.m:177-229) in one pass over the
+// voxels: SAR S = sum_c |J_c|^2 / (2 sigma rho) where |2 sigma rho| > 1e-10
+// (zero elsewhere), and per-block partial sums of S and of Re(E . conj(J)).
+__global__ void k_sar_power(const double2* __restrict__ J, const double2* __restrict__ E,
+                            const double* __restrict__ sigma, const double* __restrict__ rho, long long V,
+                            double* __restrict__ S, double* __restrict__ part) {
+  double ssum = 0, psum = 0;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+    double jj = 0, ej = 0;
+    for (int c = 0; c < 3; ++c) {
+      const double2 j = J[c * V + v], e = E[c * V + v];
+      jj = fma(j.x, j.x, fma(j.y, j.y, jj));
+      ej = fma(e.x, j.x, fma(e.y, j.y, ej));  // Re(e conj(j))
+    }
+    const double denom = 2.0 * sigma[v] * rho[v];
+    const double sv = fabs(denom) > 1e-10 ? jj / denom : 0.0;
+    S[v] = sv;
+    ssum += sv;
+    psum += ej;
+  }
+  __shared__ double ws[2][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    ssum += __shfl_xor_sync(0xffffffffu, ssum, o);
+    psum += __shfl_xor_sync(0xffffffffu, psum, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    ws[0][wid] = ssum;
+    ws[1][wid] = psum;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[threadIdx.x][w];
+    part[threadIdx.x * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// e_r = eps_r - j sigma / (eps0 omega) (Scat_Solver.m:144)
+__global__ void k_complex_permittivity(const double* __restrict__ eps_r, const double* __restrict__ sigma,
+                                       double eps0_omega, long long V, double2* __restrict__ er) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+    er[v] = mk<double2>(eps_r[v], -sigma[v] / eps0_omega);
+}
+
+__global__ void k_scale_field(double2* __restrict__ x, double s, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x[i] = mk<double2>(x[i].x * s, x[i].y * s);
+}
+
 }  // namespace marie
 
 using namespace marie;
 
 extern "C" {
+
+int marie_scat_solver(marie_plan* p, const double* Einc, const double* Hinc, double dx, double freq,
+                      const double* eps_r, const double* sigma_e, const double* rho, double tol, int form,
+                      char solver, char precond, int max_it, int inner_it, int outer_it, int ritz, double* Jout,
+                      double* Sout, double* Eout, double* Bout, double* Gsar, double* Pabs) {
+  if (!p || !Einc || !eps_r || !sigma_e || !rho || !Jout) return set_error(MARIE_EINVAL, "NULL argument");
+  if (!(dx > 0) || !(freq > 0)) return set_error(MARIE_EINVAL, "dx and freq must be positive");
+  cudaStream_t st = p->stream;
+  const long long V = p->d.V;
+  const double Gram = dx * dx * dx;
+  // Scat_Solver.m:155-160: the operators when the plan has none
+  if (!p->has_op) MARIE_TRY(marie_plan_assemble(p, dx, freq, 'D', nullptr));
+  if ((Bout || Hinc) && !p->has_opK) MARIE_TRY(marie_plan_assemble_k(p, dx, freq));
+  DBuf tE, tH, teps, tsig, trho, tJ, tS, tEo, tB, er, part;
+  const void *E_d, *H_d = nullptr, *eps_d, *sig_d, *rho_d;
+  void *J_d, *S_d = nullptr, *Eo_d = nullptr, *B_d = nullptr;
+  MARIE_TRY(stage_in(Einc, 3 * V * sizeof(double2), st, tE, &E_d));
+  if (Hinc) MARIE_TRY(stage_in(Hinc, 3 * V * sizeof(double2), st, tH, &H_d));
+  MARIE_TRY(stage_in(eps_r, V * sizeof(double), st, teps, &eps_d));
+  MARIE_TRY(stage_in(sigma_e, V * sizeof(double), st, tsig, &sig_d));
+  MARIE_TRY(stage_in(rho, V * sizeof(double), st, trho, &rho_d));
+  MARIE_TRY(stage_out(Jout, 3 * V * sizeof(double2), st, tJ, &J_d));
+  // SAR and the powers need E even when the caller does not ask for it
+  MARIE_TRY(stage_out(Eout ? Eout : nullptr, 3 * V * sizeof(double2), st, tEo, &Eo_d));
+  if (Sout) MARIE_TRY(stage_out(Sout, V * sizeof(double), st, tS, &S_d));
+  if (Bout) MARIE_TRY(stage_out(Bout, 3 * V * sizeof(double2), st, tB, &B_d));
+  DBuf S_tmp;
+  if (!S_d) {
+    MARIE_TRY(S_tmp.alloc(V * sizeof(double), st));
+    S_d = S_tmp.p;
+  }
+  MARIE_TRY(er.alloc(V * sizeof(double2), st));
+  const double omega = 2.0 * M_PI * freq;
+  k_complex_permittivity<<<grid_n(V), 256, 0, st>>>((const double*)eps_d, (const double*)sig_d, eps0() * omega, V,
+                                                    er.as<double2>());
+  count_launch();
+  MARIE_CUDA_TRY(cudaGetLastError());
+  // the current (Scat_Solver.m:164)
+  double iter[2], relres;
+  int flag;
+  MARIE_TRY(marie_jvie_solve(p, (const double*)E_d, (const double*)er.p, dx, freq, tol, form, solver, precond,
+                             max_it, inner_it, outer_it, ritz, (double*)J_d, &flag, &relres, iter, nullptr, 0,
+                             nullptr, nullptr));
+  // total E (:181) and B = mu0 H (:186-187)
+  const int prec = p->fN64 ? MARIE_FP64 : MARIE_FP32;
+  MARIE_TRY(marie_e_field_nop(p, (const double*)J_d, Gram, freq, (const double*)E_d, (double*)Eo_d, prec));
+  if (Bout) {
+    const int precK = p->fK64 ? MARIE_FP64 : MARIE_FP32;
+    MARIE_TRY(marie_h_field_kop(p, (const double*)J_d, Gram, (const double*)H_d, (double*)B_d, precK));
+    k_scale_field<<<grid_n(3 * V), 256, 0, st>>>((double2*)B_d, 4.0 * M_PI * 1e-7, 3 * V);
+    count_launch();
+  }
+  // SAR (:170-178), Pabs and Gsar (:190-194)
+  const int G = 152 * 2;
+  MARIE_TRY(part.alloc(2 * G * sizeof(double), st));
+  k_sar_power<<<G, 256, 0, st>>>((const double2*)J_d, (const double2*)Eo_d, (const double*)sig_d,
+                                 (const double*)rho_d, V, (double*)S_d, part.as<double>());
+  count_launch();
+  MARIE_CUDA_TRY(cudaGetLastError());
+  std::vector<double> hp(2 * G);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hp.data(), part.p, 2 * G * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MARIE_TRY(finish_out(Jout, J_d, 3 * V * sizeof(double2), st));
+  if (Eout) MARIE_TRY(finish_out(Eout, Eo_d, 3 * V * sizeof(double2), st));
+  if (Sout) MARIE_TRY(finish_out(Sout, S_d, V * sizeof(double), st));
+  if (Bout) MARIE_TRY(finish_out(Bout, B_d, 3 * V * sizeof(double2), st));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+  double ssum = 0, psum = 0;
+  for (int b = 0; b < G; ++b) {
+    ssum += hp[b];
+    psum += hp[G + b];
+  }
+  if (Gsar) *Gsar = ssum * Gram;
+  if (Pabs) *Pabs = 0.5 * psum * Gram;
+  return MARIE_OK;
+}
+
 
 int marie_jvie_solve(marie_plan* p, const double* Einc, const double* e_r, double dx, double freq, double tol,
                      int form, char solver, char precond, int max_it, int inner_it, int outer_it, int ritz,

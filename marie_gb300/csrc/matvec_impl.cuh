@@ -46,16 +46,23 @@ template <typename T> struct MatvecImpl {
                                                                   n_out, Lp, tw, stop, step);
     return cudaGetLastError();
   }
-  template <int NZ>
-  static cudaError_t zmul_n(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                            cudaStream_t st) {
-    constexpr int S = ZS<T, NZ>::S;
-    const size_t smem = (size_t)ZS<T, NZ>::bytes(S);  // S columns, 3 component buffers
-    cudaError_t e = opt_in_smem(k_zmul<T, NZ>, smem);
+  template <int NZ, int KIND>
+  static cudaError_t zmul_nk(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
+                             cudaStream_t st) {
+    using ZC = ZS<T, NZ, KIND>;
+    constexpr int S = ZC::S;
+    const size_t smem = (size_t)ZC::bytes(S);  // S columns, 3 component buffers, operator tile
+    cudaError_t e = opt_in_smem(k_zmul<T, NZ, KIND>, smem);
     if (e != cudaSuccess) return e;
     dim3 grid((d.Lp + S - 1) / S, d.Mp, nrhs);
-    k_zmul<T, NZ><<<grid, ZS<T, NZ>::THREADS, smem, st>>>(B, bs, fN, oct, d, tw);
+    k_zmul<T, NZ, KIND><<<grid, ZC::THREADS, smem, st>>>(B, bs, fN, oct, d, tw);
     return cudaGetLastError();
+  }
+  template <int NZ>
+  static cudaError_t zmul_n(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
+                            cudaStream_t st, int kind) {
+    return kind == 0 ? zmul_nk<NZ, 0>(B, bs, fN, oct, d, tw, nrhs, st)
+                     : zmul_nk<NZ, 1>(B, bs, fN, oct, d, tw, nrhs, st);
   }
 
   static cudaError_t xfwd(const double2* J, long long js, const int* inv, Prologue pro, V* A, long long as,
@@ -97,9 +104,9 @@ template <typename T> struct MatvecImpl {
     return cudaErrorInvalidValue;
   }
   static cudaError_t zmul(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                          cudaStream_t st) {
+                          cudaStream_t st, int kind) {
     switch (d.Np) {
-#define MARIE_CASE(n_) case n_: return zmul_n<n_>(B, bs, fN, oct, d, tw, nrhs, st);
+#define MARIE_CASE(n_) case n_: return zmul_n<n_>(B, bs, fN, oct, d, tw, nrhs, st, kind);
       MARIE_FFT_LENGTHS(MARIE_CASE)
 #undef MARIE_CASE
     }
@@ -211,8 +218,8 @@ cudaError_t MatvecLaunch<T>::cols(bool inv, int NC, const V* in, long long in_w,
 }
 template <typename T>
 cudaError_t MatvecLaunch<T>::zmul(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                                  cudaStream_t st) {
-  return MatvecImpl<T>::zmul(B, bs, fN, oct, d, tw, nrhs, st);
+                                  cudaStream_t st, int kind) {
+  return MatvecImpl<T>::zmul(B, bs, fN, oct, d, tw, nrhs, st, kind);
 }
 
 }  // namespace marie

@@ -239,7 +239,24 @@ k_cols(const cplx<T>* __restrict__ in, long long in_w, long long in_rhs, int n_i
 // fNo[q][oz][oy][ox], (L+1) x (M+1) x (N+1) per component.  oct = 0: full
 // fN[q][kz][ky][kx].
 // ---------------------------------------------------------------------------
-template <typename T, int NZ> struct ZS {
+// The two circulant operators of the path: N, the symmetric 3x3 tensor of
+// mv_AN / mv_L (6 components [xx xy xz yy yz zz], kind 0), and K, the
+// curl-type kernel of mv_K (3 components [Kx Ky Kz], kind 1).  odd(q, a): the
+// circulant component q is odd along axis a (gperiodic_coeff_nop.m,
+// gperiodic_coeff_kop.m), so its transform changes sign under reflection.
+template <int KIND> struct OpKind;
+template <> struct OpKind<0> {
+  static constexpr int NQ = 6;
+  __host__ __device__ static constexpr bool odd(int q, int a) {
+    return a == 0 ? (q == 1 || q == 2) : (a == 1 ? (q == 1 || q == 4) : (q == 2 || q == 4));
+  }
+};
+template <> struct OpKind<1> {
+  static constexpr int NQ = 3;
+  __host__ __device__ static constexpr bool odd(int q, int a) { return q == a; }
+};
+
+template <typename T, int NZ, int KIND = 0> struct ZS {
   static constexpr int TT = FFT<cplx<T>, NZ, false>::T;   // threads per transform
   static constexpr int S0 = sizeof(T) == 4 ? 8 : 4;        // columns per CTA
   static constexpr int S = (3 * S0 * TT <= 1024) ? S0 : ((3 * (S0 / 2) * TT <= 1024) ? S0 / 2 : S0 / 4);
@@ -248,8 +265,8 @@ template <typename T, int NZ> struct ZS {
   static constexpr bool HALF = S * (int)sizeof(cplx<T>) == 64;
   static constexpr int ES = HALF ? S : S + 1;
   static constexpr int BUF = NZ * ES + (HALF ? (NZ / 16 + 1) * S : 0);  // one component's exchange buffer
-  // octant operator tile of the CTA's columns: 6 components x (N+1) planes x S
-  static constexpr int TILE = 6 * (NZ / 2 + 1) * S;
+  // octant operator tile of the CTA's columns: NQ components x (N+1) planes x S
+  static constexpr int TILE = OpKind<KIND>::NQ * (NZ / 2 + 1) * S;
   static constexpr long long bytes(int) { return (long long)(NZ + 3 * BUF + TILE) * sizeof(cplx<T>); }
   __device__ static SAddr addr() { return SAddr(ES, false, HALF ? S : 0); }
 };
@@ -267,10 +284,8 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
-// odd components along x, y, z: xy (1), xz (2) | xy (1), yz (4) | xz (2), yz (4)
-__host__ __device__ constexpr bool odd_x(int q) { return q == 1 || q == 2; }
-__host__ __device__ constexpr bool odd_y(int q) { return q == 1 || q == 4; }
-__host__ __device__ constexpr bool odd_z(int q) { return q == 2 || q == 4; }
+// N components odd along z: xz (2), yz (4)
+__host__ __device__ constexpr bool odd_z(int q) { return OpKind<0>::odd(q, 2); }
 
 // Components of row c of the symmetric tensor [xx xy xz; xy yy yz; xz yz zz].
 template <int C> struct ZRow {
@@ -321,22 +336,64 @@ __device__ __forceinline__ void zrow(V* reg, int t, int s, bool active, int oct,
     }
 }
 
+// Row C of the K product out = K x J at this thread's output positions:
+// out_x = Kz J_y - Ky J_z, out_y = Kx J_z - Kz J_x, out_z = Ky J_x - Kx J_y
+// (mv_K.m:57-74).  Kz is odd along z, so the z reflection flips it.
+template <int C> struct KRow {
+  static constexpr int qa = C == 0 ? 2 : (C == 1 ? 0 : 1), ia = C == 0 ? 1 : (C == 1 ? 2 : 0);
+  static constexpr int qb = C == 0 ? 1 : (C == 1 ? 2 : 0), ib = C == 0 ? 2 : (C == 1 ? 0 : 1);
+};
+
+template <int C, typename FF, typename V, int NZ, int S>
+__device__ __forceinline__ void zrow_k(V* reg, int t, int s, bool active, int oct, const V* tile, const V* fp,
+                                       long long fq, long long fplane, const V* const* bc, SAddr ad) {
+  using RW = KRow<C>;
+  constexpr int NH = NZ / 2, NO = NH + 1, RL = FF::RL;
+#pragma unroll
+  for (int b = 0; b < FF::E / RL; ++b)
+#pragma unroll
+    for (int r = 0; r < RL; ++r) {
+      const int kz = FF::out_pos(t, b, r);
+      V y = mk<V>(0, 0);
+      if (active) {
+        V na, nb;
+        if (oct) {
+          const bool fz = kz > NH;
+          const int oz = fz ? NZ - kz : kz;
+          na = tile[(RW::qa * NO + oz) * S + s];
+          nb = tile[(RW::qb * NO + oz) * S + s];
+          if constexpr (RW::qa == 2) na = neg_if(na, fz);
+          if constexpr (RW::qb == 2) nb = neg_if(nb, fz);
+        } else {
+          const long long o = (long long)kz * fplane;
+          na = fp[RW::qa * fq + o];
+          nb = fp[RW::qb * fq + o];
+        }
+        const int e = ad(kz);
+        y = csub(cmul(na, bc[RW::ia][e]), cmul(nb, bc[RW::ib][e]));
+      }
+      reg[b * RL + r] = y;
+    }
+}
+
 // Thread group c (of three) transforms component c of the S columns.  After
 // the forward transforms the three spectra meet in shared memory; group c
 // forms row c of the symmetric product and runs its inverse transform from
 // the registers (the inverse radix order starts where the forward ended).
-template <typename T, int NZ>
-__global__ void __launch_bounds__(ZS<T, NZ>::THREADS)
+template <typename T, int NZ, int KIND>
+__global__ void __launch_bounds__(ZS<T, NZ, KIND>::THREADS)
 k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN, int oct, Dims d,
        const cplx<T>* __restrict__ tw) {
   if (rhs_skipped(d, blockIdx.z)) return;
   using V = cplx<T>;
   using FF = FFT<V, NZ, false>;
   using FI = FFT<V, NZ, true>;
-  constexpr int S = ZS<T, NZ>::S;
-  constexpr int BUF = ZS<T, NZ>::BUF;
+  using ZC = ZS<T, NZ, KIND>;
+  using OK = OpKind<KIND>;
+  constexpr int S = ZC::S;
+  constexpr int BUF = ZC::BUF;
   constexpr int NH = NZ / 2, NO = NH + 1;  // N non-zero planes; N+1 octant planes
-  const SAddr ad = ZS<T, NZ>::addr();
+  const SAddr ad = ZC::addr();
   constexpr int E = FF::E, R0 = FF::R0, RLI = FI::RL;
   static_assert(FI::R0 == FF::RL, "inverse must start where the forward transform ended");
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -359,7 +416,7 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   const long long frow = oct ? (long long)(d.L + 1) : d.Lp;
   // Tile rows (q, oz) of S columns: this thread copies column s of rows
   // row0, row0 + STEP, ... (THREADS is a multiple of S).
-  constexpr int ROWS = 6 * NO, STEP = ZS<T, NZ>::THREADS / S;
+  constexpr int ROWS = OK::NQ * NO, STEP = ZC::THREADS / S;
   const int row0 = threadIdx.x / S;
   if (oct && active) {
     // the operator tile streams into shared memory while the forward
@@ -399,8 +456,8 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
     const bool fx = kx0 + s > d.L;
     unsigned flip = 0;
 #pragma unroll
-    for (int q = 0; q < 6; ++q)
-      if ((fx && odd_x(q)) != (fy && odd_y(q))) flip |= 1u << q;
+    for (int q = 0; q < OK::NQ; ++q)
+      if ((fx && OK::odd(q, 0)) != (fy && OK::odd(q, 1))) flip |= 1u << q;
     if (flip) {
       int q = row0 / NO, oz = row0 - q * NO;
       for (int row = row0; row < ROWS; row += STEP) {
@@ -423,12 +480,22 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   const V* b1 = buf + BUF + s;
   const V* b2 = buf + 2 * BUF + s;
   // c is uniform over whole warps (groups of S * T threads) for the long transforms
-  if (c == 0)
-    zrow<0, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, b0, b1, b2, ad);
-  else if (c == 1)
-    zrow<1, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, b0, b1, b2, ad);
-  else
-    zrow<2, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, b0, b1, b2, ad);
+  if constexpr (KIND == 0) {
+    if (c == 0)
+      zrow<0, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, b0, b1, b2, ad);
+    else if (c == 1)
+      zrow<1, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, b0, b1, b2, ad);
+    else
+      zrow<2, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, b0, b1, b2, ad);
+  } else {
+    const V* bc[3] = {b0, b1, b2};
+    if (c == 0)
+      zrow_k<0, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, bc, ad);
+    else if (c == 1)
+      zrow_k<1, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, bc, ad);
+    else
+      zrow_k<2, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, bc, ad);
+  }
   FI::run(reg, my, ad, t, tw_s);
 #pragma unroll
   for (int b = 0; b < E / RLI; ++b)

@@ -21,6 +21,12 @@ struct marie_plan {
   bool fuse = true;  // fused x+y / y+x passes when the grid has them
   int oct = 0;  // 1: fN64/fN32 hold the (L+1)(M+1)(N+1) octant, 0: the full array
 
+  // K operator (mv_K, H_field_Kop), same scaling and layouts with 3 components.
+  double2* fK64 = nullptr;
+  float2* fK32 = nullptr;
+  bool has_opK = false;
+  int octK = 0;
+
   // Twiddle tables exp(-2*pi*i*k/n) for the three padded axis lengths.
   double2* tw64[3] = {nullptr, nullptr, nullptr};
   float2* tw32[3] = {nullptr, nullptr, nullptr};
@@ -80,15 +86,20 @@ int run_matvec(marie_plan* p, int prec, const double2* J, double2* out, long lon
 // Same with column strides js / os and the batched-solve skip mask: column r
 // is left untouched when stop[r] < step.
 int run_matvec(marie_plan* p, int prec, const double2* J, long long js, double2* out, long long os, long long n,
-               int nrhs, const int* inv, const Prologue& pro, const Epilogue& ep, const int* stop, int step);
+               int nrhs, const int* inv, const Prologue& pro, const Epilogue& ep, const int* stop, int step,
+               int kind = 0);
 
 // Scale fN by 1/(8LMN) into the plan's FP64/FP32 copies (fN_dev: full layout).
-int install_operator(marie_plan* p, const double2* fN_dev);
+// kind 0: the N operator (6 components), 1: the K operator (3 components).
+int install_operator(marie_plan* p, const double2* fN_dev, int kind = 0);
 
 // Per-DOF coefficient arrays for mv_AN: (a, b) or (pre, a) for the adjoint.
 // mode 0: a = Gram*Mr, b = Mc      mode 1: pre = Mc, a = Gram*conj(Mr)
 int build_coefficients(marie_plan* p, const int64_t* idx_dev, long long n, const double2* Mr,
                        const double2* Mc, double Gram, int mode, double2* a, double2* b);
+
+// Drops the cuFFT comparison state of a plan (cufft_compare.cu), if any.
+void release_cufft_state(const marie_plan* p);
 
 // Deterministic reductions and vector kernels (krylov.cu).
 int dev_norm2(marie_plan* p, const double2* x, long long n, double* out_host);

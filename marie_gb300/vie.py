@@ -7,6 +7,8 @@ argument order, defaults and return tuples:
     mv_AN(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, GPU_flag)
                                                  src_vie/src_mvp/mv_AN.m:1
     mv_L(JIn0, fN, r, Gram, idx, GPU_flag)       src_vie/src_mvp/mv_L.m:1
+    mv_K(JIn0, fK, r, idx, GPU_flag)             src_vie/src_mvp/mv_K.m:1
+    H_field_Kop(J, fK, Gram, Hinc, GPU_flag)     src_vie/src_fields/src_op/H_field_Kop.m:1
     pgmres(A, b, restart, tol, maxit, L1, L2, R1, R2, x0)
                                                  src_numeric/src_iterative/pgmres.m:70
     pgmresDR(A, b, restart, tol, maxit, ritz, L1, L2, R1, R2, x0)
@@ -15,6 +17,9 @@ argument order, defaults and return tuples:
     JVIE_Solver(Einc, e_r, r, freq, fN, tol, form, solver, precond, max_it,
                 inner_it, outer_it, ritz, gpu_flag, logfile)
                                                  src_vie/src_solver/JVIE_Solver.m:1
+    Scat_Solver(Einc, Hinc, freq, r, epsilon_r, sigma_e, rho, tol, fN, fK, form,
+                solver, precond, max_it, inner_it, outer_it, ritz, gpu_flag, logfile)
+                                                 src_vie/src_solver/Scat_Solver.m:1
     E_field_Nop(J, fN, Gram, freq, Einc, GPU_flag)
                                                  src_vie/src_fields/src_op/E_field_Nop.m:1
     PlaneWave_Excitation(r, k, omega_mu, Eo)     src_vie/src_fields/src_excitations/PlaneWave_Excitation.m:1
@@ -142,6 +147,28 @@ class Operator:
         op.dx, op.freq = dx, freq
         return op
 
+    @classmethod
+    def from_array_k(cls, fK, precision="fp64", nrhs_max=1):
+        """A plan holding only the K operator (2L x 2M x 2N x 3, getOPERATORS(r, f, 'K'))."""
+        Lf, Mf, Nf, q = fK.shape
+        if q != 3 or Lf % 2 or Mf % 2 or Nf % 2:
+            raise ValueError("fK must be 2L x 2M x 2N x 3")
+        op = cls(Lf // 2, Mf // 2, Nf // 2, precision, nrhs_max)
+        op.set_k(fK)
+        return op
+
+    def set_k(self, fK):
+        """Upload the K operator into this plan (beside fN)."""
+        ptr, keep = _in(fK)
+        check(self.lib.marie_set_operator_k(self.plan, ptr, 2 * self.L, 2 * self.M, 2 * self.N))
+        del keep
+        return self
+
+    def assemble_k(self, dx, freq):
+        """getOPERATORS(r, f, 'K') computed straight into this plan."""
+        check(self.lib.marie_plan_assemble_k(self.plan, float(dx), float(freq)))
+        return self
+
     def to_array(self):
         """The FP64 operator as a 2L x 2M x 2N x 6 numpy array."""
         ptr, arr = _out((2 * self.L, 2 * self.M, 2 * self.N, 6), False)
@@ -180,21 +207,23 @@ def _operator_for(fN, precision):
 # getOPERATORS
 # ---------------------------------------------------------------------------
 def getOPERATORS(r, f, op="N", type="FFTofC", singular="DIRECTFN", singular_values=None):
-    """getOPERATORS.m:1-127 for op 'N'.  type 'FFTofC' (default), 'C' or 'T'.
+    """getOPERATORS.m:1-127 for op 'N' (6 components) and 'K' (3 components).
+    type 'FFTofC' (default), 'C' or 'T'.
 
     singular='DIRECTFN' evaluates the weakly singular self/edge/vertex integrals
-    with a converged device quadrature; singular_values = [ST, EAc, EAo, VAc,
-    VAo] overrides them (e.g. with the reference's own DIRECTFN values)."""
+    of N with a converged device quadrature; singular_values = [ST, EAc, EAo,
+    VAc, VAo] overrides them (e.g. with the reference's own DIRECTFN values)."""
     lib = _lib.load()
-    if op != "N":
-        raise NotImplementedError("only the N operator is on this path")
+    if op not in ("N", "K"):
+        raise ValueError("op must be 'N' or 'K'")
     L, M, N = r.shape[:3]
+    q = 6 if op == "N" else 3
     t = {"FFTofC": b"F", "C": b"C", "T": b"T"}[type]
-    shape = (L, M, N, 6) if t == b"T" else (2 * L, 2 * M, 2 * N, 6)
+    shape = (L, M, N, q) if t == b"T" else (2 * L, 2 * M, 2 * N, q)
     rp, rk = _in(r, np.float64)
     op_ptr, out = _out(shape, _is_cuda(r))
     sv, keep = _singular_arg(singular, singular_values)
-    check(lib.marie_get_operators(rp, L, M, N, float(f), b"N", t, sv[0], sv[1], op_ptr))
+    check(lib.marie_get_operators(rp, L, M, N, float(f), op.encode(), t, sv[0], sv[1], op_ptr))
     return out
 
 
@@ -246,6 +275,47 @@ def mv_L(JIn0, fN, r, Gram, idx, GPU_flag=1, precision="fp64"):
         ip, ik = _in(idx, np.int64)
         op_, out = _out(JIn0.shape, cuda)
         check(opr.lib.marie_mv_L(opr.plan, jp, float(Gram), ip, n, op_, nrhs, prec))
+        return out
+    finally:
+        if tmp:
+            opr.close()
+
+
+def _k_operator_for(fK, precision):
+    if isinstance(fK, Operator):
+        return fK, False
+    return Operator.from_array_k(fK, precision=precision), True
+
+
+def mv_K(JIn0, fK, r, idx, GPU_flag=1, precision="fp64"):
+    """mv_K.m: crop(IFFT(fK x FFT(J))) on the entries idx.  fK is an Operator
+    holding K (Operator.assemble_k / set_k) or a 2L x 2M x 2N x 3 array."""
+    prec = _PREC[precision]
+    opr, tmp = _k_operator_for(fK, "mixed" if prec == MARIE_FP32 else "fp64")
+    try:
+        cuda = _is_cuda(JIn0)
+        n = JIn0.shape[0]
+        nrhs = 1 if JIn0.ndim == 1 else JIn0.shape[1]
+        jp, jk = _in(JIn0)
+        ip, ik = _in(idx, np.int64)
+        op_, out = _out(JIn0.shape, cuda)
+        check(opr.lib.marie_mv_K(opr.plan, jp, ip, n, op_, nrhs, prec))
+        return out
+    finally:
+        if tmp:
+            opr.close()
+
+
+def H_field_Kop(J, fK, Gram, Hinc=None, GPU_flag=1, precision="fp64"):
+    """H_field_Kop.m:46-77: Htot = Hinc + mv_K(J) / Gram."""
+    opr, tmp = _k_operator_for(fK, "fp64")
+    try:
+        if Hinc is not None and not np.any(np.asarray(J.cpu() if _is_cuda(J) else J)):
+            return Hinc
+        jp, jk = _in(J)
+        hp, hk = _in(Hinc) if Hinc is not None else (None, None)
+        op_, out = _out(tuple(J.shape), _is_cuda(J))
+        check(opr.lib.marie_h_field_kop(opr.plan, jp, float(Gram), hp, op_, _PREC[precision]))
         return out
     finally:
         if tmp:
@@ -455,6 +525,51 @@ def JVIE_Solver(Einc, e_r, r, freq, fN, tol=None, form=None, solver=None, precon
     finally:
         if tmp:
             opr.close()
+
+
+def Scat_Solver(Einc, Hinc, freq, r, epsilon_r, sigma_e, rho, tol=None, fN=None, fK=None, form=None, solver=None,
+                precond=None, max_it=None, inner_it=None, outer_it=None, ritz=None, gpu_flag=1, logfile=None,
+                precision="fp64"):
+    """Scat_Solver.m on the device: the J-VIE current, SAR, total E, B = mu0 H,
+    global SAR and absorbed power.  fN / fK: an Operator holding them (N and
+    K on one plan), or None to assemble both.  Returns (Jout, Sout, Eout, Bout,
+    Gsar, Pabs, op) where op is the Operator that holds fN and fK."""
+    tol = 1e-3 if tol is None else tol
+    form = 2 if form is None else form
+    solver = solver if solver in ("G", "D") else "B"
+    pc = {None: b"\0", 0: b"\0", "L": b"L", "R": b"R"}.get(precond, b"\0")
+    max_it = 1000 if max_it is None else max_it
+    inner_it = 50 if inner_it is None or inner_it < 1 else inner_it
+    outer_it = 200 if outer_it is None or outer_it < 1 else outer_it
+    ritz = 5 if ritz is None or ritz < 1 else ritz
+    L, M, N = epsilon_r.shape
+    dx = float(r[1, 0, 0, 0] - r[0, 0, 0, 0]) if not _is_cuda(r) else float((r[1, 0, 0, 0] - r[0, 0, 0, 0]).item())
+    if isinstance(fN, Operator):
+        opr = fN
+        if isinstance(fK, np.ndarray):
+            opr.set_k(fK)
+    else:
+        opr = Operator(L, M, N, precision)
+        if fN is not None:
+            ptr, keep = _in(fN)
+            check(opr.lib.marie_set_operator(opr.plan, ptr, 2 * L, 2 * M, 2 * N))
+        if fK is not None:
+            opr.set_k(fK)
+    cuda = _is_cuda(Einc)
+    ep, ek = _in(Einc)
+    hp, hk = _in(Hinc) if Hinc is not None else (None, None)
+    epsp, epsk = _in(epsilon_r, np.float64)
+    sp_, sk = _in(sigma_e, np.float64)
+    rp_, rk = _in(rho, np.float64)
+    jp, Jout = _out((L, M, N, 3), cuda)
+    spo, Sout = _out((L, M, N), cuda, np.float64)
+    eo, Eout = _out((L, M, N, 3), cuda)
+    bo, Bout = _out((L, M, N, 3), cuda)
+    gsar, pabs = C.c_double(), C.c_double()
+    check(opr.lib.marie_scat_solver(opr.plan, ep, hp, dx, float(freq), epsp, sp_, rp_, float(tol), int(form),
+                                    solver.encode(), pc, int(max_it), int(inner_it), int(outer_it), int(ritz), jp, spo,
+                                    eo, bo, C.byref(gsar), C.byref(pabs)))
+    return Jout, Sout, Eout, Bout, gsar.value, pabs.value, opr
 
 
 def JVIE_Solver_batch(Einc, e_r, r, freq, fN, tol=None, form=None, precond=None, inner_it=None, outer_it=None):

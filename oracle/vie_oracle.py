@@ -518,6 +518,30 @@ def JVIE_Solver(Einc, e_r, r, freq, fN, tol=1e-3, form=2, solver="B", precond=0,
     return Je.reshape((L, M, N, 3), order="F"), flag, relres, it, resvec
 
 
+def Scat_Solver(Einc, Hinc, freq, r, epsilon_r, sigma_e, rho, tol=1e-3, fN=None, fK=None, form=2, solver="B",
+                precond=0, max_it=1000, inner_it=50, outer_it=200, ritz=5):
+    """src_vie/src_solver/Scat_Solver.m:143-194: current, SAR, total E,
+    B = mu0 H, global SAR and absorbed power."""
+    em = EMconstants(freq)
+    e_r = epsilon_r - 1j * sigma_e / (em["eo"] * em["omega"])
+    dx = r[1, 0, 0, 0] - r[0, 0, 0, 0]
+    Gram = dx**3
+    if fN is None:
+        fN = getOPERATORS(r, freq, "N")
+    if fK is None:
+        fK = getOPERATORS(r, freq, "K")
+    Jout = JVIE_Solver(Einc, e_r, r, freq, fN, tol, form, solver, precond, max_it, inner_it, outer_it, ritz)[0]
+    denom = 2 * sigma_e * rho
+    S = np.sum(np.abs(Jout) ** 2, axis=3)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        Sout = np.where(np.abs(denom) > 1e-10, S / denom, 0.0)
+    Eout = E_field_Nop(Jout, fN, Gram, freq, Einc)
+    Bout = 4 * np.pi * 1e-7 * H_field_Kop(Jout, fK, Gram, Hinc)
+    Pabs = 0.5 * np.real(np.sum(Eout * np.conj(Jout))) * Gram
+    Gsar = np.sum(Sout) * Gram
+    return Jout, Sout, Eout, Bout, Gsar, Pabs
+
+
 # ---------------------------------------------------------------------------
 # excitations
 # ---------------------------------------------------------------------------

@@ -171,3 +171,30 @@ def test_fused_and_five_pass_paths_agree(monkeypatch):
     a = mg.mv_AN(J, op_f, Mr, Mc, 1e-7, "notransp", idx)
     b = mg.mv_AN(J, op_u, Mr, Mc, 1e-7, "notransp", idx)
     assert relerr(a, b) < 1e-13
+
+
+def test_cufft_comparison_matvec_matches_oracle(cuda):
+    """The cuFFT build of the FP32 mv_AN (timed beside the hand-written one in
+    bench.py) computes the same product."""
+    import ctypes as C
+
+    import torch
+
+    import marie_gb300 as mg
+    from marie_gb300 import _lib
+
+    lib = _lib.load()
+    for shape in ((12, 20, 24), (32, 32, 4)):
+        fN, Mr, Mc, idx, J = problem(*shape, seed=5, physical=True)
+        ref = vo.mv_AN(J, fN, Mr, Mc, 0.37, "notransp", idx)
+        op = mg.Operator.from_array(fN, precision="mixed")
+        out = np.zeros_like(ref)
+        ms = C.c_float()
+        vp = lambda a: C.c_void_p(a.ctypes.data)
+        Jc, Mrf, Mcf, ix = (np.ascontiguousarray(J), np.asfortranarray(Mr), np.asfortranarray(Mc),
+                            np.ascontiguousarray(idx.astype(np.int64)))
+        _lib.check(lib.marie_mv_AN_cufft(op.plan, vp(Jc), vp(Mrf), vp(Mcf), 0.37, vp(ix), ix.size, vp(out),
+                                         C.byref(ms)))
+        assert relerr(out, ref) < 1e-5
+        assert ms.value > 0
+        op.close()
