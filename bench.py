@@ -180,6 +180,9 @@ def run_gpu(args, world, rank, local):
     op = mg.Operator.assemble(L, M, N, DX, FREQ, precision="mixed")
     torch.cuda.synchronize()
     t_asm = time.perf_counter() - t_asm0
+    # schedule autotuner (outside the timed region): fused / five-pass x-y
+    # passes, z-pass radix schedule and columns per CTA
+    tuned, tune_cands = op.autotune()
 
     def colmajor(a):
         t = torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose(*range(a.ndim - 1, -1, -1))))
@@ -277,6 +280,9 @@ def run_gpu(args, world, rank, local):
             "matvec_ms": {"fp32": mv["fp32_ms"], "fp64": mv["fp64_ms"], "fp32_passes_ms": mv["fp32_passes"],
                           "fp64_passes_ms": mv["fp64_passes"], "fp32_cufft_comparison": mv["fp32_cufft_ms"]},
             "assembly_s": round(t_asm, 3),
+            "autotune": {"chosen": {"fused_xy": tuned[0], "z_variant": tuned[1]},
+                         "candidates_ms": [{"fused_xy": f, "z_variant": z, "ms": round(ms, 4)}
+                                           for f, z, ms in tune_cands]},
             "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": round(dom["gbs"], 1), "peak": hbm,
                          "unit": "GB/s", "frac": round(dom["gbs"] / hbm, 4),
                          "traffic": zmul_traffic() if dom["name"] == "z_multiply" else None,

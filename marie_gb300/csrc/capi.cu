@@ -187,6 +187,14 @@ static inline int grid_for(long long n, int threads = 256) {
   return (int)g;
 }
 
+// autotuner input: J = a smooth pattern, the identity DOF map over the grid
+__global__ void k_tune_fill(double2* __restrict__ J, int* __restrict__ inv, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    J[i] = mk<double2>(1.0 + 1e-3 * (double)(i % 97), -1e-3 * (double)(i % 89));
+    inv[i] = (int)i;
+  }
+}
+
 int build_inverse_index(marie_plan* p, const int64_t* idx_dev, long long n, int* inv) {
   const long long n3V = 3 * p->d.V;
   if (n < 0 || n > n3V) return set_error(MARIE_EINVAL, "n_idx = %lld outside [0, 3*L*M*N = %lld]", n, n3V);
@@ -245,7 +253,7 @@ static int run_matvec_t(marie_plan* p, const double2* J, long long js, double2* 
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[1], p->stream));
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
       }
-      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, oct, d, tw[2], nr, p->stream, kind));
+      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, oct, d, tw[2], nr, p->stream, kind, kind == 0 ? p->zvar : 0));
       if (prof) {
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[4], p->stream));
@@ -258,7 +266,7 @@ static int run_matvec_t(marie_plan* p, const double2* J, long long js, double2* 
       MARIE_CUDA_TRY(ML::cols(false, d.Mp, A, (long long)d.Lp * d.M, sA, d.M, B, (long long)d.Lp * d.Mp, sB, d.Mp,
                               d.Lp, 3 * d.N, tw[1], nr, p->stream, d.stop, step));
       if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
-      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, oct, d, tw[2], nr, p->stream, kind));
+      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, oct, d, tw[2], nr, p->stream, kind, kind == 0 ? p->zvar : 0));
       if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
       MARIE_CUDA_TRY(ML::cols(true, d.Mp, B, (long long)d.Lp * d.Mp, sB, d.Mp, A, (long long)d.Lp * d.M, sA, d.M,
                               d.Lp, 3 * d.N, tw[1], nr, p->stream, d.stop, step));
@@ -538,6 +546,86 @@ int marie_plan_destroy(marie_plan* p) {
 }
 
 void* marie_plan_stream(marie_plan* p) { return p ? (void*)p->stream : nullptr; }
+
+// Autotuner: times the FP32 matvec of this plan's grid for every candidate
+// schedule (fused x+y passes or the five-pass form; the z pass with the wide
+// or narrow radix schedule and with 8 or 4 columns per CTA), keeps the
+// fastest on the plan and reports every candidate's time.
+int marie_plan_autotune(marie_plan* p, int* fuse_out, int* zvar_out, double* ms_out, int64_t cap, int64_t* count) {
+  if (!p) return set_error(MARIE_EINVAL, "NULL plan");
+  if (count) *count = 0;
+  if (!p->has_op || !p->fN32) return MARIE_OK;  // nothing to tune without the FP32 operator
+  cudaStream_t st = p->stream;
+  const long long n = 3 * p->d.V;
+  DBuf J, out, inv;
+  MARIE_TRY(J.alloc(n * sizeof(double2), st));
+  MARIE_TRY(out.alloc(n * sizeof(double2), st));
+  MARIE_TRY(inv.alloc(n * sizeof(int), st));
+  k_tune_fill<<<grid_for(n), 256, 0, st>>>(J.as<double2>(), inv.as<int>(), n);
+  count_launch();
+  MARIE_CUDA_TRY(cudaGetLastError());
+  Prologue pro{nullptr, 0};
+  Epilogue ep{};
+  ep.a_s = mk<double2>(1.0, 0.0);
+  ep.b_s = mk<double2>(1.0, 0.0);
+  const bool can_fuse = MatvecLaunch<float>::fused(p->d);
+  const bool wide = p->d.Np == 16 || p->d.Np == 128 || p->d.Np == 256;
+  struct Cand { int fuse, zvar; double ms; };
+  std::vector<Cand> cands;
+  for (int f = can_fuse ? 1 : 0; f >= 0; --f)
+    for (int z = 0; z < 3; ++z)
+      if (z != 1 || wide) cands.push_back({f, z, 0.0});
+  const bool fuse0 = p->fuse;
+  const int zvar0 = p->zvar;
+  cudaEvent_t e0, e1;
+  MARIE_CUDA_TRY(cudaEventCreate(&e0));
+  MARIE_CUDA_TRY(cudaEventCreate(&e1));
+  int status = MARIE_OK;
+  for (auto& c : cands) {
+    p->fuse = c.fuse != 0;
+    p->zvar = c.zvar;
+    const int reps = 5;
+    for (int r = 0; r < 2 + reps && status == MARIE_OK; ++r) {
+      if (r == 2) cudaEventRecord(e0, st);
+      status = run_matvec(p, MARIE_FP32, J.as<double2>(), out.as<double2>(), n, 1, inv.as<int>(), pro, ep);
+    }
+    if (status != MARIE_OK) break;
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    c.ms = ms / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (status != MARIE_OK) {
+    p->fuse = fuse0;
+    p->zvar = zvar0;
+    return status;
+  }
+  const Cand* best = &cands[0];
+  for (const auto& c : cands)
+    if (c.ms < best->ms) best = &c;
+  p->fuse = best->fuse != 0;
+  p->zvar = best->zvar;
+  if (fuse_out) *fuse_out = best->fuse;
+  if (zvar_out) *zvar_out = best->zvar;
+  for (size_t i = 0; i < cands.size() && (int64_t)i < cap && ms_out; ++i) {
+    ms_out[3 * i] = cands[i].fuse;
+    ms_out[3 * i + 1] = cands[i].zvar;
+    ms_out[3 * i + 2] = cands[i].ms;
+  }
+  if (count) *count = (int64_t)cands.size();
+  return MARIE_OK;
+}
+
+int marie_plan_set_schedule(marie_plan* p, int fuse, int zvar) {
+  if (!p) return set_error(MARIE_EINVAL, "NULL plan");
+  if (zvar < 0 || zvar > 2) return set_error(MARIE_EINVAL, "zvar must be 0, 1 or 2");
+  p->fuse = fuse != 0;
+  p->zvar = zvar;
+  return MARIE_OK;
+}
 
 int64_t marie_launch_count(void) { return g_launches.load(); }
 

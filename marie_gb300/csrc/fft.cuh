@@ -329,10 +329,13 @@ template <typename V, int N> struct Sched<V, N, true> {
 // Transform of length N on values of type V (float2 / double2).  The forward
 // transform uses the schedule's radix list; the inverse uses it reversed, so
 // reg after FFT<V,N,false>::run is directly the input of FFT<V,N,true>::run.
-template <typename V, int N, bool INV> struct FFT {
-  using RF = typename Sched<V, N>::R;
+// W selects the radix schedule: the wide one (radix 16, FP32 lengths 16, 128,
+// 256) or the narrow one (radix <= 8); the default is the wide one where it
+// exists.  The matvec autotuner times both for the z pass.
+template <typename V, int N, bool INV, bool W = (sizeof(V) == 8) && HasWide<N>::value> struct FFT {
+  using RF = typename Sched<V, N, W>::R;
   using RL_ = typename std::conditional<INV, typename RRev<RF>::type, RF>::type;
-  static constexpr int E = Sched<V, N>::E;
+  static constexpr int E = Sched<V, N, W>::E;
   static constexpr int T = N / E;
   static constexpr int R0 = RFirst<RL_>::value;
   using LP = LastPass<N, E, 1, RL_>;

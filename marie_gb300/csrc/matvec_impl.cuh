@@ -46,23 +46,28 @@ template <typename T> struct MatvecImpl {
                                                                   n_out, Lp, tw, stop, step);
     return cudaGetLastError();
   }
-  template <int NZ, int KIND>
+  template <int NZ, int KIND, int VAR>
   static cudaError_t zmul_nk(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
                              cudaStream_t st) {
-    using ZC = ZS<T, NZ, KIND>;
+    using ZC = ZS<T, NZ, KIND, VAR>;
     constexpr int S = ZC::S;
     const size_t smem = (size_t)ZC::bytes(S);  // S columns, 3 component buffers, operator tile
-    cudaError_t e = opt_in_smem(k_zmul<T, NZ, KIND>, smem);
+    cudaError_t e = opt_in_smem(k_zmul<T, NZ, KIND, VAR>, smem);
     if (e != cudaSuccess) return e;
     dim3 grid((d.Lp + S - 1) / S, d.Mp, nrhs);
-    k_zmul<T, NZ, KIND><<<grid, ZC::THREADS, smem, st>>>(B, bs, fN, oct, d, tw);
+    k_zmul<T, NZ, KIND, VAR><<<grid, ZC::THREADS, smem, st>>>(B, bs, fN, oct, d, tw);
     return cudaGetLastError();
   }
   template <int NZ>
   static cudaError_t zmul_n(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                            cudaStream_t st, int kind) {
-    return kind == 0 ? zmul_nk<NZ, 0>(B, bs, fN, oct, d, tw, nrhs, st)
-                     : zmul_nk<NZ, 1>(B, bs, fN, oct, d, tw, nrhs, st);
+                            cudaStream_t st, int kind, int var) {
+    if (kind == 1) return zmul_nk<NZ, 1, 0>(B, bs, fN, oct, d, tw, nrhs, st);
+    if constexpr (sizeof(T) == 4) {
+      if constexpr (HasWide<NZ>::value)
+        if (var == 1) return zmul_nk<NZ, 0, 1>(B, bs, fN, oct, d, tw, nrhs, st);
+      if (var == 2) return zmul_nk<NZ, 0, 2>(B, bs, fN, oct, d, tw, nrhs, st);
+    }
+    return zmul_nk<NZ, 0, 0>(B, bs, fN, oct, d, tw, nrhs, st);
   }
 
   static cudaError_t xfwd(const double2* J, long long js, const int* inv, Prologue pro, V* A, long long as,
@@ -104,9 +109,9 @@ template <typename T> struct MatvecImpl {
     return cudaErrorInvalidValue;
   }
   static cudaError_t zmul(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                          cudaStream_t st, int kind) {
+                          cudaStream_t st, int kind, int var) {
     switch (d.Np) {
-#define MARIE_CASE(n_) case n_: return zmul_n<n_>(B, bs, fN, oct, d, tw, nrhs, st, kind);
+#define MARIE_CASE(n_) case n_: return zmul_n<n_>(B, bs, fN, oct, d, tw, nrhs, st, kind, var);
       MARIE_FFT_LENGTHS(MARIE_CASE)
 #undef MARIE_CASE
     }
@@ -218,8 +223,8 @@ cudaError_t MatvecLaunch<T>::cols(bool inv, int NC, const V* in, long long in_w,
 }
 template <typename T>
 cudaError_t MatvecLaunch<T>::zmul(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                                  cudaStream_t st, int kind) {
-  return MatvecImpl<T>::zmul(B, bs, fN, oct, d, tw, nrhs, st, kind);
+                                  cudaStream_t st, int kind, int var) {
+  return MatvecImpl<T>::zmul(B, bs, fN, oct, d, tw, nrhs, st, kind, var);
 }
 
 }  // namespace marie

@@ -256,9 +256,18 @@ template <> struct OpKind<1> {
   __host__ __device__ static constexpr bool odd(int q, int a) { return q == a; }
 };
 
-template <typename T, int NZ, int KIND = 0> struct ZS {
-  static constexpr int TT = FFT<cplx<T>, NZ, false>::T;   // threads per transform
-  static constexpr int S0 = sizeof(T) == 4 ? 8 : 4;        // columns per CTA
+// z-pass variants the autotuner chooses from (FP32, N operator): 0 the
+// default (wide radix schedule where one exists, 8 columns per CTA), 1 the
+// narrow radix schedule, 2 half the columns per CTA.
+template <typename T, int NZ, int VAR> struct ZVar {
+  static constexpr bool W = VAR == 1 ? false : (sizeof(cplx<T>) == 8 && HasWide<NZ>::value);
+  static constexpr int S0 = (sizeof(T) == 4 ? 8 : 4) / (VAR == 2 ? 2 : 1);
+};
+
+template <typename T, int NZ, int KIND = 0, int VAR = 0> struct ZS {
+  static constexpr bool W = ZVar<T, NZ, VAR>::W;             // radix schedule
+  static constexpr int TT = FFT<cplx<T>, NZ, false, W>::T;   // threads per transform
+  static constexpr int S0 = ZVar<T, NZ, VAR>::S0;            // columns per CTA
   static constexpr int S = (3 * S0 * TT <= 1024) ? S0 : ((3 * (S0 / 2) * TT <= 1024) ? S0 / 2 : S0 / 4);
   static constexpr int THREADS = 3 * S * TT;               // one thread group per component
   // rows of 64 B use the half-line swizzle, others one pad element per row
@@ -380,15 +389,15 @@ __device__ __forceinline__ void zrow_k(V* reg, int t, int s, bool active, int oc
 // the forward transforms the three spectra meet in shared memory; group c
 // forms row c of the symmetric product and runs its inverse transform from
 // the registers (the inverse radix order starts where the forward ended).
-template <typename T, int NZ, int KIND>
-__global__ void __launch_bounds__(ZS<T, NZ, KIND>::THREADS)
+template <typename T, int NZ, int KIND, int VAR>
+__global__ void __launch_bounds__(ZS<T, NZ, KIND, VAR>::THREADS)
 k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN, int oct, Dims d,
        const cplx<T>* __restrict__ tw) {
   if (rhs_skipped(d, blockIdx.z)) return;
   using V = cplx<T>;
-  using FF = FFT<V, NZ, false>;
-  using FI = FFT<V, NZ, true>;
-  using ZC = ZS<T, NZ, KIND>;
+  using ZC = ZS<T, NZ, KIND, VAR>;
+  using FF = FFT<V, NZ, false, ZC::W>;
+  using FI = FFT<V, NZ, true, ZC::W>;
   using OK = OpKind<KIND>;
   constexpr int S = ZC::S;
   constexpr int BUF = ZC::BUF;

@@ -35,9 +35,10 @@ template <typename T> struct MatvecLaunch {
   static cudaError_t cols(bool inv, int NC, const V* in, long long in_w, long long in_rhs, int n_in, V* out,
                           long long out_w, long long out_rhs, int n_out, int Lp, int nw, const V* tw, int nrhs,
                           cudaStream_t st, const int* stop = nullptr, int step = 0);
-  // kind 0: the symmetric N operator (6 components), 1: the K operator (3)
+  // kind 0: the symmetric N operator (6 components), 1: the K operator (3);
+  // var: the z-pass variant chosen by the autotuner (FP32, N operator)
   static cudaError_t zmul(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                          cudaStream_t st, int kind = 0);
+                          cudaStream_t st, int kind = 0, int var = 0);
   // fused x+y passes (thread-block clusters); fused() says whether this grid has them
   static bool fused(const Dims& d);
   static cudaError_t xyfwd(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,

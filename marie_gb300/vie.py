@@ -169,6 +169,22 @@ class Operator:
         check(self.lib.marie_plan_assemble_k(self.plan, float(dx), float(freq)))
         return self
 
+    def autotune(self):
+        """Time the FP32 matvec schedules of this grid (fused or five-pass x/y
+        passes; z-pass radix schedule and columns per CTA), keep the fastest.
+        Returns (chosen (fuse, zvar), [(fuse, zvar, ms), ...])."""
+        ms = np.zeros(3 * 16)
+        fuse, zvar, cnt = C.c_int(), C.c_int(), C.c_int64()
+        check(self.lib.marie_plan_autotune(self.plan, C.byref(fuse), C.byref(zvar), ms.ctypes.data_as(_lib._dp), 16,
+                                           C.byref(cnt)))
+        cands = [(int(ms[3 * i]), int(ms[3 * i + 1]), float(ms[3 * i + 2])) for i in range(cnt.value)]
+        return (fuse.value, zvar.value), cands
+
+    def set_schedule(self, fuse, zvar):
+        """Pin a matvec schedule (fuse 1/0; z-pass variant 0, 1 or 2)."""
+        check(self.lib.marie_plan_set_schedule(self.plan, int(fuse), int(zvar)))
+        return self
+
     def to_array(self):
         """The FP64 operator as a 2L x 2M x 2N x 6 numpy array."""
         ptr, arr = _out((2 * self.L, 2 * self.M, 2 * self.N, 6), False)

@@ -198,3 +198,22 @@ def test_cufft_comparison_matvec_matches_oracle(cuda):
         assert relerr(out, ref) < 1e-5
         assert ms.value > 0
         op.close()
+
+
+@pytest.mark.parametrize("shape", [(16, 16, 64), (32, 32, 4), (12, 20, 8)])
+def test_autotuner_candidates_all_match_oracle(shape):
+    """Every schedule the autotuner chooses from (fused or five-pass; wide or
+    narrow z radix; 8 or 4 z columns per CTA) gives the FP32 product, and the
+    tuner keeps the fastest of the ones it timed."""
+    import marie_gb300 as mg
+
+    fN, Mr, Mc, idx, J = problem(*shape, seed=13, physical=True)
+    ref = vo.mv_AN(J, fN, Mr, Mc, 0.2, "notransp", idx)
+    op = mg.Operator.from_array(fN, precision="mixed")
+    (fuse, zvar), cands = op.autotune()
+    assert cands and min(c[2] for c in cands) == [c[2] for c in cands if c[:2] == (fuse, zvar)][0]
+    for f, z, _ in cands:
+        op.set_schedule(f, z)
+        out = mg.mv_AN(J, op, Mr, Mc, 0.2, "notransp", idx, precision="fp32")
+        assert relerr(out, ref) < TOL["fp32"], (f, z)
+    op.close()
