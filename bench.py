@@ -280,9 +280,9 @@ def run_gpu(args, world, rank, local):
             "matvec_ms": {"fp32": mv["fp32_ms"], "fp64": mv["fp64_ms"], "fp32_passes_ms": mv["fp32_passes"],
                           "fp64_passes_ms": mv["fp64_passes"], "fp32_cufft_comparison": mv["fp32_cufft_ms"]},
             "assembly_s": round(t_asm, 3),
-            "autotune": {"chosen": {"fused_xy": tuned[0], "z_variant": tuned[1]},
-                         "candidates_ms": [{"fused_xy": f, "z_variant": z, "ms": round(ms, 4)}
-                                           for f, z, ms in tune_cands]},
+            "autotune": {"chosen": {"fused_xy": tuned[0], "xy_variant": tuned[1], "z_variant": tuned[2]},
+                         "candidates_ms": [{"fused_xy": f, "xy_variant": fv, "z_variant": z, "ms": round(ms, 4)}
+                                           for f, fv, z, ms in tune_cands]},
             "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": round(dom["gbs"], 1), "peak": hbm,
                          "unit": "GB/s", "frac": round(dom["gbs"] / hbm, 4),
                          "traffic": zmul_traffic() if dom["name"] == "z_multiply" else None,

@@ -273,17 +273,17 @@ int marie_mv_AN_cufft(marie_plan* plan, const double* JIn0, const double* Mr, co
  * previous call, then resets and switches recording on or off. */
 int64_t marie_launch_count(void);
 /* Schedule autotuner (no counterpart in the reference): times the plan's FP32
- * matvec for every candidate schedule (fused or five-pass x/y passes; z pass
- * with the wide or narrow radix schedule and 8 or 4 columns per CTA), keeps the
- * fastest on the plan and returns it in *fuse / *zvar.  ms receives
- * {fuse, zvar, milliseconds} per candidate (up to cap candidates, *count
- * written).  A plan without an FP32 operator is left as it is (*count = 0). */
-int marie_plan_autotune(marie_plan* plan, int* fuse, int* zvar, double* ms, int64_t cap,
+ * matvec for every candidate schedule (fuse: fused x+y cluster passes or the
+ * five-pass form; fvar: default or narrow radix schedule of the fused x/y
+ * transforms; zvar: z pass with the default schedule, the narrow radix
+ * schedule, or 4 instead of 8 columns per CTA), keeps the fastest on the plan
+ * and returns it in *fuse / *fvar / *zvar.  ms receives {fuse, fvar, zvar,
+ * milliseconds} per candidate (up to cap candidates, *count written).  A plan
+ * without an FP32 operator is left as it is (*count = 0). */
+int marie_plan_autotune(marie_plan* plan, int* fuse, int* fvar, int* zvar, double* ms, int64_t cap,
                         int64_t* count);
-/* Pin a schedule (as marie_plan_autotune would choose it): fuse 1 = fused x+y
- * passes where the grid has them, 0 = five passes; zvar 0 default z pass, 1
- * narrow radix schedule, 2 half the columns per CTA. */
-int marie_plan_set_schedule(marie_plan* plan, int fuse, int zvar);
+/* Pin a schedule as marie_plan_autotune would choose it. */
+int marie_plan_set_schedule(marie_plan* plan, int fuse, int fvar, int zvar);
 /* Host-side fault injection for tests (no reference counterpart): the nth
  * device allocation from now on fails with MARIE_ENOMEM (0 switches it off). */
 void marie_inject_alloc_failure(int64_t nth);

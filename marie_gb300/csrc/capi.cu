@@ -248,7 +248,7 @@ static int run_matvec_t(marie_plan* p, const double2* J, long long js, double2* 
     const bool prof = p->profile;
     if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[0], p->stream));
     if (fused) {
-      MARIE_CUDA_TRY(ML::xyfwd(Jc, js, inv, pro, B, sB, d, tw[0], tw[1], nr, p->stream));
+      MARIE_CUDA_TRY(ML::xyfwd(Jc, js, inv, pro, B, sB, d, tw[0], tw[1], nr, p->stream, p->fvar));
       if (prof) {
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[1], p->stream));
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
@@ -258,7 +258,7 @@ static int run_matvec_t(marie_plan* p, const double2* J, long long js, double2* 
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[4], p->stream));
       }
-      MARIE_CUDA_TRY(ML::yxinv(B, sB, Jc, js, inv, ep, oc, os, d, tw[0], tw[1], nr, p->stream));
+      MARIE_CUDA_TRY(ML::yxinv(B, sB, Jc, js, inv, ep, oc, os, d, tw[0], tw[1], nr, p->stream, p->fvar));
       count_launch(3);
     } else {
       MARIE_CUDA_TRY(ML::xfwd(Jc, js, inv, pro, A, sA, d, tw[0], nr, p->stream));
@@ -548,10 +548,12 @@ int marie_plan_destroy(marie_plan* p) {
 void* marie_plan_stream(marie_plan* p) { return p ? (void*)p->stream : nullptr; }
 
 // Autotuner: times the FP32 matvec of this plan's grid for every candidate
-// schedule (fused x+y passes or the five-pass form; the z pass with the wide
-// or narrow radix schedule and with 8 or 4 columns per CTA), keeps the
-// fastest on the plan and reports every candidate's time.
-int marie_plan_autotune(marie_plan* p, int* fuse_out, int* zvar_out, double* ms_out, int64_t cap, int64_t* count) {
+// schedule (fused x+y passes with the default or the narrow radix schedule, or
+// the five-pass form; the z pass with the wide or narrow radix schedule and
+// with 8 or 4 columns per CTA), keeps the fastest on the plan and reports every
+// candidate's time as {fuse, fvar, zvar, ms}.
+int marie_plan_autotune(marie_plan* p, int* fuse_out, int* fvar_out, int* zvar_out, double* ms_out, int64_t cap,
+                        int64_t* count) {
   if (!p) return set_error(MARIE_EINVAL, "NULL plan");
   if (count) *count = 0;
   if (!p->has_op || !p->fN32) return MARIE_OK;  // nothing to tune without the FP32 operator
@@ -568,21 +570,24 @@ int marie_plan_autotune(marie_plan* p, int* fuse_out, int* zvar_out, double* ms_
   Epilogue ep{};
   ep.a_s = mk<double2>(1.0, 0.0);
   ep.b_s = mk<double2>(1.0, 0.0);
+  auto wide = [](int n) { return n == 16 || n == 128 || n == 256; };
   const bool can_fuse = MatvecLaunch<float>::fused(p->d);
-  const bool wide = p->d.Np == 16 || p->d.Np == 128 || p->d.Np == 256;
-  struct Cand { int fuse, zvar; double ms; };
+  const bool narrow_xy = can_fuse && (wide(p->d.Lp) || wide(p->d.Mp));
+  struct Cand { int fuse, fvar, zvar; double ms; };
   std::vector<Cand> cands;
   for (int f = can_fuse ? 1 : 0; f >= 0; --f)
-    for (int z = 0; z < 3; ++z)
-      if (z != 1 || wide) cands.push_back({f, z, 0.0});
+    for (int fv = 0; fv < ((f && narrow_xy) ? 2 : 1); ++fv)
+      for (int z = 0; z < 3; ++z)
+        if (z != 1 || wide(p->d.Np)) cands.push_back({f, fv, z, 0.0});
   const bool fuse0 = p->fuse;
-  const int zvar0 = p->zvar;
+  const int fvar0 = p->fvar, zvar0 = p->zvar;
   cudaEvent_t e0, e1;
   MARIE_CUDA_TRY(cudaEventCreate(&e0));
   MARIE_CUDA_TRY(cudaEventCreate(&e1));
   int status = MARIE_OK;
   for (auto& c : cands) {
     p->fuse = c.fuse != 0;
+    p->fvar = c.fvar;
     p->zvar = c.zvar;
     const int reps = 5;
     for (int r = 0; r < 2 + reps && status == MARIE_OK; ++r) {
@@ -600,6 +605,7 @@ int marie_plan_autotune(marie_plan* p, int* fuse_out, int* zvar_out, double* ms_
   cudaEventDestroy(e1);
   if (status != MARIE_OK) {
     p->fuse = fuse0;
+    p->fvar = fvar0;
     p->zvar = zvar0;
     return status;
   }
@@ -607,22 +613,27 @@ int marie_plan_autotune(marie_plan* p, int* fuse_out, int* zvar_out, double* ms_
   for (const auto& c : cands)
     if (c.ms < best->ms) best = &c;
   p->fuse = best->fuse != 0;
+  p->fvar = best->fvar;
   p->zvar = best->zvar;
   if (fuse_out) *fuse_out = best->fuse;
+  if (fvar_out) *fvar_out = best->fvar;
   if (zvar_out) *zvar_out = best->zvar;
   for (size_t i = 0; i < cands.size() && (int64_t)i < cap && ms_out; ++i) {
-    ms_out[3 * i] = cands[i].fuse;
-    ms_out[3 * i + 1] = cands[i].zvar;
-    ms_out[3 * i + 2] = cands[i].ms;
+    ms_out[4 * i] = cands[i].fuse;
+    ms_out[4 * i + 1] = cands[i].fvar;
+    ms_out[4 * i + 2] = cands[i].zvar;
+    ms_out[4 * i + 3] = cands[i].ms;
   }
   if (count) *count = (int64_t)cands.size();
   return MARIE_OK;
 }
 
-int marie_plan_set_schedule(marie_plan* p, int fuse, int zvar) {
+int marie_plan_set_schedule(marie_plan* p, int fuse, int fvar, int zvar) {
   if (!p) return set_error(MARIE_EINVAL, "NULL plan");
+  if (fvar < 0 || fvar > 1) return set_error(MARIE_EINVAL, "fvar must be 0 or 1");
   if (zvar < 0 || zvar > 2) return set_error(MARIE_EINVAL, "zvar must be 0, 1 or 2");
   p->fuse = fuse != 0;
+  p->fvar = fvar;
   p->zvar = zvar;
   return MARIE_OK;
 }

@@ -7,10 +7,10 @@ namespace marie {
 using V32 = MatvecLaunch<float>::V;
 template bool MatvecLaunch<float>::fused(const Dims&);
 template cudaError_t MatvecLaunch<float>::xyfwd(const double2*, long long, const int*, Prologue, V32*, long long,
-                                                const Dims&, const V32*, const V32*, int, cudaStream_t);
+                                                const Dims&, const V32*, const V32*, int, cudaStream_t, int);
 template cudaError_t MatvecLaunch<float>::yxinv(const V32*, long long, const double2*, long long, const int*,
                                                 Epilogue, double2*, long long, const Dims&, const V32*, const V32*,
-                                                int, cudaStream_t);
+                                                int, cudaStream_t, int);
 template cudaError_t MatvecLaunch<float>::xfwd(const double2*, long long, const int*, Prologue, V32*, long long,
                                                const Dims&, const V32*, int, cudaStream_t);
 template cudaError_t MatvecLaunch<float>::xinv(const V32*, long long, const double2*, long long, const int*, Epilogue,

@@ -21,12 +21,17 @@ namespace marie {
 
 namespace cg = cooperative_groups;
 
-template <typename T, int NL, int NM, int CS> struct XYCfg {
+// NARROW: the radix-8 schedules for the x and y transforms (twice the threads
+// per transform, half the exchange buffer, one more CTA per SM for xyfwd); an
+// autotuner variant for the lengths that have a wide schedule.
+template <typename T, int NL, int NM, int CS, bool NARROW = false> struct XYCfg {
   using V = cplx<T>;
-  using FX = FFT<V, NL, false>;
-  using FXI = FFT<V, NL, true>;
-  using FY = FFT<V, NM, false>;
-  using FYI = FFT<V, NM, true>;
+  static constexpr bool WX = !NARROW && (sizeof(V) == 8) && HasWide<NL>::value;
+  static constexpr bool WY = !NARROW && (sizeof(V) == 8) && HasWide<NM>::value;
+  using FX = FFT<V, NL, false, WX>;
+  using FXI = FFT<V, NL, true, WX>;
+  using FY = FFT<V, NM, false, WY>;
+  using FYI = FFT<V, NM, true, WY>;
   static constexpr int THREADS = 256;
   static constexpr int L = NL / 2, M = NM / 2;
   static constexpr int RY = M / CS;                 // rows per CTA
@@ -43,13 +48,13 @@ template <typename T, int NL, int NM, int CS> struct XYCfg {
                              FY::T <= THREADS;
 };
 
-template <typename T, int NL, int NM, int CS>
-__global__ void __launch_bounds__(256)
+template <typename T, int NL, int NM, int CS, bool NARROW>
+__global__ void __launch_bounds__(256, NARROW ? 4 : 0)
 k_xyfwd(const double2* __restrict__ J, long long js, const int* __restrict__ inv, Prologue pro,
         cplx<T>* __restrict__ B, long long bs, Dims d, const cplx<T>* __restrict__ twx,
         const cplx<T>* __restrict__ twy) {
   if (rhs_skipped(d, blockIdx.y)) return;  // uniform over the cluster
-  using C = XYCfg<T, NL, NM, CS>;
+  using C = XYCfg<T, NL, NM, CS, NARROW>;
   using V = cplx<T>;
   using FX = typename C::FX;
   using FY = typename C::FY;
@@ -142,13 +147,14 @@ k_xyfwd(const double2* __restrict__ J, long long js, const int* __restrict__ inv
   }
 }
 
-template <typename T, int NL, int NM, int CS>
-__global__ void __launch_bounds__(256, (XYCfg<T, NL, NM, CS>::FXI::E <= 16 && XYCfg<T, NL, NM, CS>::FYI::E <= 16) ? 3 : 1)
+template <typename T, int NL, int NM, int CS, bool NARROW>
+__global__ void __launch_bounds__(256, (XYCfg<T, NL, NM, CS, NARROW>::FXI::E <= 16 &&
+                                        XYCfg<T, NL, NM, CS, NARROW>::FYI::E <= 16) ? 3 : 1)
 k_yxinv(const cplx<T>* __restrict__ B, long long bs, const double2* __restrict__ J, long long js,
         const int* __restrict__ inv, Epilogue ep, double2* __restrict__ out, long long os, Dims d,
         const cplx<T>* __restrict__ twx, const cplx<T>* __restrict__ twy) {
   if (rhs_skipped(d, blockIdx.y)) return;  // uniform over the cluster
-  using C = XYCfg<T, NL, NM, CS>;
+  using C = XYCfg<T, NL, NM, CS, NARROW>;
   using V = cplx<T>;
   using FXI = typename C::FXI;
   using FYI = typename C::FYI;

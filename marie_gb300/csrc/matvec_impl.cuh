@@ -149,13 +149,34 @@ template <typename T> struct FusedImpl {
     cfg.numAttrs = 1;
     return cudaLaunchKernelExC(&cfg, (const void*)kern, args);
   }
+  template <int NL, int NM, int CS, bool NARROW>
+  static cudaError_t xyfwd_nv(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
+                              Dims d, const V* twx, const V* twy, int nrhs, cudaStream_t st) {
+    void* args[] = {(void*)&J, (void*)&js, (void*)&inv, (void*)&pro, (void*)&B, (void*)&bs, (void*)&d,
+                    (void*)&twx, (void*)&twy};
+    return launch(k_xyfwd<T, NL, NM, CS, NARROW>, CS, CS * 3 * d.N, nrhs, XYCfg<T, NL, NM, CS, NARROW>::fwd_smem, st,
+                  args);
+  }
+  template <int NL, int NM, int CS, bool NARROW>
+  static cudaError_t yxinv_nv(const V* B, long long bs, const double2* J, long long js, const int* inv, Epilogue ep,
+                              double2* out, long long os, Dims d, const V* twx, const V* twy, int nrhs,
+                              cudaStream_t st) {
+    void* args[] = {(void*)&B, (void*)&bs, (void*)&J, (void*)&js, (void*)&inv, (void*)&ep, (void*)&out,
+                    (void*)&os, (void*)&d, (void*)&twx, (void*)&twy};
+    return launch(k_yxinv<T, NL, NM, CS, NARROW>, CS, CS * 3 * d.N, nrhs, XYCfg<T, NL, NM, CS, NARROW>::inv_smem, st,
+                  args);
+  }
+  // a narrow variant exists where either transform has a wide schedule
+  template <int NL, int NM> static constexpr bool has_narrow() {
+    return sizeof(T) == 4 && (HasWide<NL>::value || HasWide<NM>::value);
+  }
   template <int NL, int NM, int CS>
   static cudaError_t xyfwd_n(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
-                             Dims d, const V* twx, const V* twy, int nrhs, cudaStream_t st) {
+                             Dims d, const V* twx, const V* twy, int nrhs, cudaStream_t st, int fvar) {
     if constexpr (usable<NL, NM, CS>()) {
-      void* args[] = {(void*)&J, (void*)&js, (void*)&inv, (void*)&pro, (void*)&B, (void*)&bs, (void*)&d,
-                      (void*)&twx, (void*)&twy};
-      return launch(k_xyfwd<T, NL, NM, CS>, CS, CS * 3 * d.N, nrhs, XYCfg<T, NL, NM, CS>::fwd_smem, st, args);
+      if constexpr (has_narrow<NL, NM>())
+        if (fvar == 1) return xyfwd_nv<NL, NM, CS, true>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
+      return xyfwd_nv<NL, NM, CS, false>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
     } else {
       return cudaErrorNotSupported;
     }
@@ -163,11 +184,11 @@ template <typename T> struct FusedImpl {
   template <int NL, int NM, int CS>
   static cudaError_t yxinv_n(const V* B, long long bs, const double2* J, long long js, const int* inv, Epilogue ep,
                              double2* out, long long os, Dims d, const V* twx, const V* twy, int nrhs,
-                             cudaStream_t st) {
+                             cudaStream_t st, int fvar) {
     if constexpr (usable<NL, NM, CS>()) {
-      void* args[] = {(void*)&B, (void*)&bs, (void*)&J, (void*)&js, (void*)&inv, (void*)&ep, (void*)&out,
-                      (void*)&os, (void*)&d, (void*)&twx, (void*)&twy};
-      return launch(k_yxinv<T, NL, NM, CS>, CS, CS * 3 * d.N, nrhs, XYCfg<T, NL, NM, CS>::inv_smem, st, args);
+      if constexpr (has_narrow<NL, NM>())
+        if (fvar == 1) return yxinv_nv<NL, NM, CS, true>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
+      return yxinv_nv<NL, NM, CS, false>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
     } else {
       return cudaErrorNotSupported;
     }
@@ -183,10 +204,10 @@ template <typename T> bool MatvecLaunch<T>::fused(const Dims& d) {
 }
 template <typename T>
 cudaError_t MatvecLaunch<T>::xyfwd(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
-                                   const Dims& d, const V* twx, const V* twy, int nrhs, cudaStream_t st) {
+                                   const Dims& d, const V* twx, const V* twy, int nrhs, cudaStream_t st, int fvar) {
 #define MARIE_CASE(a_, b_, c_)    \
   if (d.Lp == a_ && d.Mp == b_) \
-    return FusedImpl<T>::template xyfwd_n<a_, b_, c_>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
+    return FusedImpl<T>::template xyfwd_n<a_, b_, c_>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st, fvar);
   MARIE_FUSED_PAIRS(MARIE_CASE)
 #undef MARIE_CASE
   return cudaErrorNotSupported;
@@ -194,10 +215,10 @@ cudaError_t MatvecLaunch<T>::xyfwd(const double2* J, long long js, const int* in
 template <typename T>
 cudaError_t MatvecLaunch<T>::yxinv(const V* B, long long bs, const double2* J, long long js, const int* inv,
                                    Epilogue ep, double2* out, long long os, const Dims& d, const V* twx, const V* twy,
-                                   int nrhs, cudaStream_t st) {
+                                   int nrhs, cudaStream_t st, int fvar) {
 #define MARIE_CASE(a_, b_, c_)    \
   if (d.Lp == a_ && d.Mp == b_) \
-    return FusedImpl<T>::template yxinv_n<a_, b_, c_>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
+    return FusedImpl<T>::template yxinv_n<a_, b_, c_>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st, fvar);
   MARIE_FUSED_PAIRS(MARIE_CASE)
 #undef MARIE_CASE
   return cudaErrorNotSupported;

@@ -41,11 +41,12 @@ template <typename T> struct MatvecLaunch {
                           cudaStream_t st, int kind = 0, int var = 0);
   // fused x+y passes (thread-block clusters); fused() says whether this grid has them
   static bool fused(const Dims& d);
+  // fvar: 0 the default x/y radix schedules, 1 the narrow (radix-8) ones
   static cudaError_t xyfwd(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
-                           const Dims& d, const V* twx, const V* twy, int nrhs, cudaStream_t st);
+                           const Dims& d, const V* twx, const V* twy, int nrhs, cudaStream_t st, int fvar = 0);
   static cudaError_t yxinv(const V* B, long long bs, const double2* J, long long js, const int* inv, Epilogue ep,
                            double2* out, long long os, const Dims& d, const V* twx, const V* twy, int nrhs,
-                           cudaStream_t st);
+                           cudaStream_t st, int fvar = 0);
 };
 
 }  // namespace marie

@@ -19,6 +19,7 @@ struct marie_plan {
   float2* fN32 = nullptr;
   bool has_op = false;
   bool fuse = true;  // fused x+y / y+x passes when the grid has them
+  int fvar = 0;      // x/y radix schedule of the fused passes (set by marie_plan_autotune)
   int zvar = 0;      // z-pass variant of the FP32 N matvec (set by marie_plan_autotune)
   int oct = 0;  // 1: fN64/fN32 hold the (L+1)(M+1)(N+1) octant, 0: the full array
 

@@ -171,18 +171,20 @@ class Operator:
 
     def autotune(self):
         """Time the FP32 matvec schedules of this grid (fused or five-pass x/y
-        passes; z-pass radix schedule and columns per CTA), keep the fastest.
-        Returns (chosen (fuse, zvar), [(fuse, zvar, ms), ...])."""
-        ms = np.zeros(3 * 16)
-        fuse, zvar, cnt = C.c_int(), C.c_int(), C.c_int64()
-        check(self.lib.marie_plan_autotune(self.plan, C.byref(fuse), C.byref(zvar), ms.ctypes.data_as(_lib._dp), 16,
-                                           C.byref(cnt)))
-        cands = [(int(ms[3 * i]), int(ms[3 * i + 1]), float(ms[3 * i + 2])) for i in range(cnt.value)]
-        return (fuse.value, zvar.value), cands
+        passes, their radix schedule; z-pass radix schedule and columns per
+        CTA), keep the fastest.  Returns (chosen (fuse, fvar, zvar),
+        [(fuse, fvar, zvar, ms), ...])."""
+        ms = np.zeros(4 * 32)
+        fuse, fvar, zvar, cnt = C.c_int(), C.c_int(), C.c_int(), C.c_int64()
+        check(self.lib.marie_plan_autotune(self.plan, C.byref(fuse), C.byref(fvar), C.byref(zvar),
+                                           ms.ctypes.data_as(_lib._dp), 32, C.byref(cnt)))
+        cands = [(int(ms[4 * i]), int(ms[4 * i + 1]), int(ms[4 * i + 2]), float(ms[4 * i + 3]))
+                 for i in range(cnt.value)]
+        return (fuse.value, fvar.value, zvar.value), cands
 
-    def set_schedule(self, fuse, zvar):
-        """Pin a matvec schedule (fuse 1/0; z-pass variant 0, 1 or 2)."""
-        check(self.lib.marie_plan_set_schedule(self.plan, int(fuse), int(zvar)))
+    def set_schedule(self, fuse, fvar, zvar):
+        """Pin a matvec schedule (fuse 1/0; fused radix variant 0/1; z-pass variant 0, 1 or 2)."""
+        check(self.lib.marie_plan_set_schedule(self.plan, int(fuse), int(fvar), int(zvar)))
         return self
 
     def to_array(self):

@@ -200,7 +200,7 @@ def test_cufft_comparison_matvec_matches_oracle(cuda):
         op.close()
 
 
-@pytest.mark.parametrize("shape", [(16, 16, 64), (32, 32, 4), (12, 20, 8)])
+@pytest.mark.parametrize("shape", [(16, 16, 64), (32, 32, 4), (64, 64, 8), (12, 20, 8)])
 def test_autotuner_candidates_all_match_oracle(shape):
     """Every schedule the autotuner chooses from (fused or five-pass; wide or
     narrow z radix; 8 or 4 z columns per CTA) gives the FP32 product, and the
@@ -210,10 +210,10 @@ def test_autotuner_candidates_all_match_oracle(shape):
     fN, Mr, Mc, idx, J = problem(*shape, seed=13, physical=True)
     ref = vo.mv_AN(J, fN, Mr, Mc, 0.2, "notransp", idx)
     op = mg.Operator.from_array(fN, precision="mixed")
-    (fuse, zvar), cands = op.autotune()
-    assert cands and min(c[2] for c in cands) == [c[2] for c in cands if c[:2] == (fuse, zvar)][0]
-    for f, z, _ in cands:
-        op.set_schedule(f, z)
+    chosen, cands = op.autotune()
+    assert cands and min(c[3] for c in cands) == [c[3] for c in cands if c[:3] == chosen][0]
+    for f, fv, z, _ in cands:
+        op.set_schedule(f, fv, z)
         out = mg.mv_AN(J, op, Mr, Mc, 0.2, "notransp", idx, precision="fp32")
-        assert relerr(out, ref) < TOL["fp32"], (f, z)
+        assert relerr(out, ref) < TOL["fp32"], (f, fv, z)
     op.close()
