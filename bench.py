@@ -180,9 +180,6 @@ def run_gpu(args, world, rank, local):
     op = mg.Operator.assemble(L, M, N, DX, FREQ, precision="mixed")
     torch.cuda.synchronize()
     t_asm = time.perf_counter() - t_asm0
-    # schedule autotuner (outside the timed region): fused / five-pass x-y
-    # passes, z-pass radix schedule and columns per CTA
-    tuned, tune_cands = op.autotune()
 
     def colmajor(a):
         t = torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose(*range(a.ndim - 1, -1, -1))))
@@ -195,11 +192,19 @@ def run_gpu(args, world, rank, local):
         return mg.JVIE_Solver(Ein, e_r, rr, FREQ, opr, tol=TOL, form=2, inner_it=RESTART, outer_it=200, solver="G")
 
     if args.solve_only:
-        # profiling entry: the mixed solves of the timed region and nothing else
+        # profiling entry: the mixed solves of the timed region and nothing else,
+        # with the schedule the autotuner picks for this grid on an idle GPU
+        # (fused x+y passes, default radix schedules; a tuning run under a
+        # profiler would time the candidates serialised and could pick another)
+        op.set_schedule(1, 0, 0)
         for _ in range(args.warmup + args.steps):
             res = solve(op, Ed, erd, r)
         torch.cuda.synchronize()
         return {"solve_only": True, "flag": res[1], "relres": res[2], "iter": res[3]} if rank == 0 else {}
+
+    # schedule autotuner (outside the timed region): fused / five-pass x-y
+    # passes and their radix schedule, z-pass radix schedule and columns per CTA
+    tuned, tune_cands = op.autotune()
 
     # --- timed region: mixed-precision solves, inputs resident in HBM --------
     for _ in range(args.warmup):
