@@ -342,6 +342,18 @@ int gmres_dr(marie_plan* p, const DevOp& A, const DevOp* L1, const DevOp* L2, co
   MARIE_TRY(dev_norm2(p, bpb.as<double2>(), n, &bnorm));
   MARIE_TRY(dev_norm2(p, r, n, &rn0));
   out = GmresResult();
+  if (bnorm == 0) {
+    // zero right-hand side: x = x0 (zero) at once instead of the reference's 0/0
+    if (x0 && x0n > 0)
+      MARIE_CUDA_TRY(cudaMemcpyAsync(x, x0, vb, cudaMemcpyDeviceToDevice, st));
+    else
+      MARIE_CUDA_TRY(cudaMemsetAsync(x, 0, vb, st));
+    MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+    out.flag = 0;
+    out.relres = 0;
+    out.resvec.push_back(0.0);
+    return MARIE_OK;
+  }
   out.resvec.push_back(rn0 / bnorm);
   int outit = 0, pk = 0;
   std::vector<double> rin;

@@ -472,7 +472,7 @@ static int solve_single(marie_plan* p, const JvieState& S, const double2* Bv, do
   }
   const int fl = rn <= tol * bn ? 0 : (sa.solver == 'B' && last_flag > 1 ? last_flag : 1);
   B.flag = G.flag = fl;
-  B.relres = G.relres = rn / bn;
+  B.relres = G.relres = bn > 0 ? rn / bn : 0.0;
   B.iter = biter;
   G.iter[0] = last_p;
   G.iter[1] = inner_total;

@@ -99,6 +99,41 @@ __global__ void kb_cycle_init(const double2* __restrict__ r, long long rs, doubl
     v[i] = mk<double2>(x[i].x * inv, x[i].y * inv);
 }
 
+// One sweep over NC basis columns c0..c0+NC-1: the block's partial sums of
+// conj(V(:,j)) w, reduced in the block (warp sums, then warp partials in warp
+// order by one thread per column: a fixed order).  NC is a template argument
+// so that a short last sweep issues no idle FP64 work.
+template <int NC>
+__device__ __forceinline__ void kb_dot_sweep(const double2* __restrict__ V, const double2* __restrict__ w,
+                                             long long n, long long i0, long long i1, int c0,
+                                             double2* __restrict__ part_s, double2 (*red)[8]) {
+  double2 acc[NC];
+#pragma unroll
+  for (int q = 0; q < NC; ++q) acc[q] = mk<double2>(0, 0);
+  for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    const double2 wv = w[i];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      const double2 v = V[(long long)(c0 + q) * n + i];
+      acc[q].x = fma(v.x, wv.x, fma(v.y, wv.y, acc[q].x));
+      acc[q].y = fma(v.x, wv.y, fma(-v.y, wv.x, acc[q].y));
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NC; ++q) {
+    const double2 r = wsum2(acc[q]);
+    if (lane == 0) red[wid][q] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x < NC) {
+    double2 r = red[0][threadIdx.x];
+    for (int w2 = 1; w2 < BT / 32; ++w2) r = cadd(r, red[w2][threadIdx.x]);
+    part_s[(long long)(c0 + threadIdx.x) * gridDim.x + blockIdx.x] = r;
+  }
+  __syncthreads();  // red is reused by the next sweep
+}
+
 // partial[s][j][b] = sum over block rows of conj(V_s(:,j)) w_s, j < k, w_s = V_s(:,k)
 __global__ void __launch_bounds__(BT) kb_dots(const double2* __restrict__ Vb, long long vs, long long n, int k,
                                               const int* __restrict__ stop, double2* __restrict__ part) {
@@ -106,39 +141,21 @@ __global__ void __launch_bounds__(BT) kb_dots(const double2* __restrict__ Vb, lo
   if (skip(stop, s, k)) return;
   const double2* V = Vb + s * vs;
   const double2* w = V + (long long)k * n;
+  double2* part_s = part + (long long)s * 128 * gridDim.x;
+  __shared__ double2 red[BT / 32][8];
   long long i0, i1;
   rows_of(n, i0, i1);
-  for (int c0 = 0; c0 < k; c0 += 8) {
-    double2 acc[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) acc[q] = mk<double2>(0, 0);
-    const int nc = k - c0 < 8 ? k - c0 : 8;
-    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      const double2 wv = w[i];
-#pragma unroll
-      for (int q = 0; q < 8; ++q)
-        if (q < nc) {
-          const double2 v = V[(long long)(c0 + q) * n + i];
-          acc[q].x = fma(v.x, wv.x, fma(v.y, wv.y, acc[q].x));
-          acc[q].y = fma(v.x, wv.y, fma(-v.y, wv.x, acc[q].y));
-        }
-    }
-    // one block reduction for the 8 columns: warp sums, then warp partials
-    // summed in warp order by one thread per column (fixed order)
-    __shared__ double2 red[BT / 32][8];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const double2 r = wsum2(acc[q]);
-      if (lane == 0) red[wid][q] = r;
-    }
-    __syncthreads();
-    if (threadIdx.x < nc) {
-      double2 r = red[0][threadIdx.x];
-      for (int w = 1; w < BT / 32; ++w) r = cadd(r, red[w][threadIdx.x]);
-      part[((long long)s * 128 + c0 + threadIdx.x) * gridDim.x + blockIdx.x] = r;
-    }
-    __syncthreads();  // red is reused by the next sweep
+  int c0 = 0;
+  for (; c0 + 8 <= k; c0 += 8) kb_dot_sweep<8>(V, w, n, i0, i1, c0, part_s, red);
+  switch (k - c0) {
+    case 1: kb_dot_sweep<1>(V, w, n, i0, i1, c0, part_s, red); break;
+    case 2: kb_dot_sweep<2>(V, w, n, i0, i1, c0, part_s, red); break;
+    case 3: kb_dot_sweep<3>(V, w, n, i0, i1, c0, part_s, red); break;
+    case 4: kb_dot_sweep<4>(V, w, n, i0, i1, c0, part_s, red); break;
+    case 5: kb_dot_sweep<5>(V, w, n, i0, i1, c0, part_s, red); break;
+    case 6: kb_dot_sweep<6>(V, w, n, i0, i1, c0, part_s, red); break;
+    case 7: kb_dot_sweep<7>(V, w, n, i0, i1, c0, part_s, red); break;
+    default: break;
   }
 }
 

@@ -73,3 +73,35 @@ def test_allocation_failure_is_enomem_and_plan_stays_usable(nth):
         lib.marie_inject_alloc_failure(0)
     out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8, solver="G")
     assert out[1] == 0
+
+
+@pytest.mark.parametrize("solver", ["B", "D"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_other_solvers_flags_zero_rhs_and_allocation_failures(solver, precision):
+    """Solvers 'B' (bicgstab) and 'D' (pgmresDR): non-convergence is a flag, a
+    zero excitation gives J = 0, injected allocation failures are MARIE_ENOMEM
+    and the plan solves afterwards."""
+    import marie_gb300 as mg
+
+    r, er, E = sphere()
+    op = mg.Operator.assemble(8, 8, 8, 5e-3, FREQ, precision=precision)
+    kw = dict(max_it=1) if solver == "B" else dict(inner_it=3, outer_it=1)
+    Je, flag, relres, it, resvec, _ = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-12, solver=solver, **kw)
+    if precision == "fp64":
+        # the solver's own iteration limit ends it (the mixed refinement repeats
+        # the limited inner solve and may still converge)
+        assert flag != 0 and relres > 1e-12
+    assert np.isfinite(relres) and (flag == 0) == (relres <= 1e-12)
+    Je, flag, relres, *_ = mg.JVIE_Solver(np.zeros_like(E), er, r, FREQ, op, tol=1e-8, solver=solver)
+    assert flag == 0 and relres == 0 and not np.any(Je)
+    lib = mg.load()
+    for nth in (1, 4, 9):
+        lib.marie_inject_alloc_failure(nth)
+        try:
+            with pytest.raises(mg.MarieError) as ei:
+                mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8, solver=solver)
+            assert ei.value.code == -2
+        finally:
+            lib.marie_inject_alloc_failure(0)
+    out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8, solver=solver)
+    assert out[1] == 0 and out[2] <= 1e-8
