@@ -275,7 +275,7 @@ int64_t marie_launch_count(void);
 /* Schedule autotuner (no counterpart in the reference): times the plan's FP32
  * matvec for every candidate schedule (fuse: fused x+y cluster passes or the
  * five-pass form; fvar: default or narrow radix schedule of the fused x/y
- * transforms; zvar: z pass with the default schedule, the narrow radix
+ * transforms, or clusters of half the size; zvar: z pass with the default schedule, the narrow radix
  * schedule, or 4 instead of 8 columns per CTA), keeps the fastest on the plan
  * and returns it in *fuse / *fvar / *zvar.  ms receives {fuse, fvar, zvar,
  * milliseconds} per candidate (up to cap candidates, *count written).  A plan

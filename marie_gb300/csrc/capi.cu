@@ -573,12 +573,16 @@ int marie_plan_autotune(marie_plan* p, int* fuse_out, int* fvar_out, int* zvar_o
   auto wide = [](int n) { return n == 16 || n == 128 || n == 256; };
   const bool can_fuse = MatvecLaunch<float>::fused(p->d);
   const bool narrow_xy = can_fuse && (wide(p->d.Lp) || wide(p->d.Mp));
+  // half-size clusters exist for the grids fused with clusters of 4 or 8
+  const bool half_cluster = can_fuse && p->d.Lp >= 128;
   struct Cand { int fuse, fvar, zvar; double ms; };
   std::vector<Cand> cands;
   for (int f = can_fuse ? 1 : 0; f >= 0; --f)
-    for (int fv = 0; fv < ((f && narrow_xy) ? 2 : 1); ++fv)
+    for (int fv = 0; fv < (f ? 3 : 1); ++fv) {
+      if ((fv == 1 && !narrow_xy) || (fv == 2 && !half_cluster)) continue;
       for (int z = 0; z < 3; ++z)
         if (z != 1 || wide(p->d.Np)) cands.push_back({f, fv, z, 0.0});
+    }
   const bool fuse0 = p->fuse;
   const int fvar0 = p->fvar, zvar0 = p->zvar;
   cudaEvent_t e0, e1;
@@ -630,7 +634,7 @@ int marie_plan_autotune(marie_plan* p, int* fuse_out, int* fvar_out, int* zvar_o
 
 int marie_plan_set_schedule(marie_plan* p, int fuse, int fvar, int zvar) {
   if (!p) return set_error(MARIE_EINVAL, "NULL plan");
-  if (fvar < 0 || fvar > 1) return set_error(MARIE_EINVAL, "fvar must be 0 or 1");
+  if (fvar < 0 || fvar > 2) return set_error(MARIE_EINVAL, "fvar must be 0, 1 or 2");
   if (zvar < 0 || zvar > 2) return set_error(MARIE_EINVAL, "zvar must be 0, 1 or 2");
   p->fuse = fuse != 0;
   p->fvar = fvar;

@@ -176,6 +176,8 @@ template <typename T> struct FusedImpl {
     if constexpr (usable<NL, NM, CS>()) {
       if constexpr (has_narrow<NL, NM>())
         if (fvar == 1) return xyfwd_nv<NL, NM, CS, true>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
+      if constexpr (CS >= 4 && usable<NL, NM, CS / 2>())
+        if (fvar == 2) return xyfwd_nv<NL, NM, CS / 2, false>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
       return xyfwd_nv<NL, NM, CS, false>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
     } else {
       return cudaErrorNotSupported;
@@ -188,6 +190,9 @@ template <typename T> struct FusedImpl {
     if constexpr (usable<NL, NM, CS>()) {
       if constexpr (has_narrow<NL, NM>())
         if (fvar == 1) return yxinv_nv<NL, NM, CS, true>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
+      if constexpr (CS >= 4 && usable<NL, NM, CS / 2>())
+        if (fvar == 2)
+          return yxinv_nv<NL, NM, CS / 2, false>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
       return yxinv_nv<NL, NM, CS, false>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
     } else {
       return cudaErrorNotSupported;
