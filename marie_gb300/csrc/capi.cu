@@ -48,6 +48,36 @@ int set_error(int code, const char* fmt, ...) {
 // host-side fault injection: the n-th allocation from now fails (0 = off)
 static std::atomic<long long> g_fail_alloc_in{0};
 
+// Library-owned stream-ordered memory pool per device.  Its release threshold
+// keeps freed blocks mapped, so the per-solve buffers (the Krylov basis is
+// ~1 GB at 128^3) are reused from the pool instead of being unmapped at every
+// synchronisation and mapped again by the next solve, as the default pool
+// (threshold 0) does.  The pool is separate from the device's default pool,
+// which other libraries in the process keep using unchanged.
+static std::mutex g_pool_mu;
+static std::map<int, cudaMemPool_t> g_pools;
+
+static cudaMemPool_t device_pool() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  auto it = g_pools.find(dev);
+  if (it != g_pools.end()) return it->second;
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool = nullptr;
+  if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  unsigned long long keep = ~0ULL;
+  cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  g_pools[dev] = pool;
+  return pool;
+}
+
 int DBuf::alloc(size_t bytes, cudaStream_t st) {
   s = st;
   if (bytes == 0) bytes = 16;
@@ -58,7 +88,16 @@ int DBuf::alloc(size_t bytes, cudaStream_t st) {
     p = nullptr;
     return set_error(MARIE_ENOMEM, "device allocation of %zu bytes failed (injected)", bytes);
   }
-  cudaError_t e = cudaMallocAsync(&p, bytes, st);
+  cudaMemPool_t pool = device_pool();
+  cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, bytes, pool, st) : cudaMallocAsync(&p, bytes, st);
+  if (e != cudaSuccess && pool) {
+    // blocks cached in the pool may be the wrong sizes: hand them back to the
+    // device once and retry before reporting the failure
+    cudaGetLastError();
+    cudaStreamSynchronize(st);
+    cudaMemPoolTrimTo(pool, 0);
+    e = cudaMallocFromPoolAsync(&p, bytes, pool, st);
+  }
   if (e != cudaSuccess) {
     p = nullptr;
     cudaGetLastError();
