@@ -284,6 +284,12 @@ int marie_plan_autotune(marie_plan* plan, int* fuse, int* fvar, int* zvar, doubl
                         int64_t* count);
 /* Pin a schedule as marie_plan_autotune would choose it. */
 int marie_plan_set_schedule(marie_plan* plan, int fuse, int fvar, int zvar);
+/* Krylov basis precision of the inner solves of a MARIE_MIXED plan's GMRES
+ * refinement (no counterpart in the reference): MARIE_FP32 (the default; FP32
+ * basis, dots and updates with FP64 reductions, Hessenberg and rotations) or
+ * MARIE_FP64.  The outer residuals and the returned solution are FP64 either
+ * way. */
+int marie_plan_set_inner_precision(marie_plan* plan, int precision);
 /* Host-side fault injection for tests (no reference counterpart): the nth
  * device allocation from now on fails with MARIE_ENOMEM (0 switches it off). */
 void marie_inject_alloc_failure(int64_t nth);

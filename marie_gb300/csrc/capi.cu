@@ -681,6 +681,14 @@ int marie_plan_set_schedule(marie_plan* p, int fuse, int fvar, int zvar) {
   return MARIE_OK;
 }
 
+int marie_plan_set_inner_precision(marie_plan* p, int precision) {
+  if (!p) return set_error(MARIE_EINVAL, "NULL plan");
+  if (precision != MARIE_FP32 && precision != MARIE_FP64)
+    return set_error(MARIE_EINVAL, "inner precision must be MARIE_FP32 or MARIE_FP64");
+  p->inner_prec = precision;
+  return MARIE_OK;
+}
+
 int64_t marie_launch_count(void) { return g_launches.load(); }
 
 void marie_inject_alloc_failure(int64_t nth) { g_fail_alloc_in.store(nth > 0 ? nth : 0); }

@@ -363,7 +363,7 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
       if (!any) break;
       std::vector<GmresResult> ri;
       MARIE_TRY(gmres_batch(p, A32, L1m, R1m, Rr, n, n, S_exc, inner_it, inner_tol, outer_it, D, n, ri, true, &act,
-                            false));
+                            false, p->inner_prec == MARIE_FP32));
       MARIE_CUDA_TRY(cudaMemcpyAsync(flags.p, act.data(), S_exc * sizeof(int), cudaMemcpyHostToDevice, st));
       k_add_b<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(D, X, n, flags.as<int>());
       count_launch();
@@ -652,6 +652,11 @@ int marie_scat_solver(marie_plan* p, const double* Einc, const double* Hinc, dou
   MARIE_TRY(stage_out(Eout ? Eout : nullptr, 3 * V * sizeof(double2), st, tEo, &Eo_d));
   if (Sout) MARIE_TRY(stage_out(Sout, V * sizeof(double), st, tS, &S_d));
   if (Bout) MARIE_TRY(stage_out(Bout, 3 * V * sizeof(double2), st, tB, &B_d));
+  HostPrefault pfJ, pfE, pfS, pfB;
+  pfJ.start(Jout, 3 * V * sizeof(double2));
+  if (Eout) pfE.start(Eout, 3 * V * sizeof(double2));
+  if (Sout) pfS.start(Sout, V * sizeof(double));
+  if (Bout) pfB.start(Bout, 3 * V * sizeof(double2));
   DBuf S_tmp;
   if (!S_d) {
     MARIE_TRY(S_tmp.alloc(V * sizeof(double), st));
@@ -687,6 +692,10 @@ int marie_scat_solver(marie_plan* p, const double* Einc, const double* Hinc, dou
   MARIE_CUDA_TRY(cudaGetLastError());
   std::vector<double> hp(2 * G);
   MARIE_CUDA_TRY(cudaMemcpyAsync(hp.data(), part.p, 2 * G * sizeof(double), cudaMemcpyDeviceToHost, st));
+  pfJ.join();
+  pfE.join();
+  pfS.join();
+  pfB.join();
   MARIE_TRY(finish_out(Jout, J_d, 3 * V * sizeof(double2), st));
   if (Eout) MARIE_TRY(finish_out(Eout, Eo_d, 3 * V * sizeof(double2), st));
   if (Sout) MARIE_TRY(finish_out(Sout, S_d, V * sizeof(double), st));
@@ -725,9 +734,12 @@ int marie_jvie_solve(marie_plan* p, const double* Einc, const double* e_r, doubl
   MARIE_TRY(stage_in(Einc, 3 * V * sizeof(double2), st, tE, &E_d));
   MARIE_TRY(stage_in(e_r, V * sizeof(double2), st, tER, &er_d));
   MARIE_TRY(stage_out(Je, 3 * V * sizeof(double2), st, tJe, &Je_d));
+  HostPrefault pf;
+  pf.start(Je, 3 * V * sizeof(double2));
   SolveOut so;
   MARIE_TRY(jvie_solve_core(p, (const double2*)E_d, 3 * V, 1, (const double2*)er_d, dx, freq, form, precond, tol,
                             inner_it, outer_it, (double2*)Je_d, 3 * V, so, sa));
+  pf.join();
   MARIE_TRY(finish_out(Je, Je_d, 3 * V * sizeof(double2), st));
   MARIE_CUDA_TRY(cudaStreamSynchronize(st));
   const auto t1 = std::chrono::steady_clock::now();
@@ -763,9 +775,12 @@ int marie_jvie_solve_batch(marie_plan* p, const double* Einc, int64_t nexc, cons
   MARIE_TRY(stage_in(Einc, (size_t)nexc * 3 * V * sizeof(double2), st, tE, &E_d));
   MARIE_TRY(stage_in(e_r, V * sizeof(double2), st, tER, &er_d));
   MARIE_TRY(stage_out(Je, (size_t)nexc * 3 * V * sizeof(double2), st, tJe, &Je_d));
+  HostPrefault pf;
+  pf.start(Je, (size_t)nexc * 3 * V * sizeof(double2));
   SolveOut so;
   MARIE_TRY(jvie_solve_core(p, (const double2*)E_d, 3 * V, (int)nexc, (const double2*)er_d, dx, freq, form, precond,
                             tol, inner_it, outer_it, (double2*)Je_d, 3 * V, so));
+  pf.join();
   MARIE_TRY(finish_out(Je, Je_d, (size_t)nexc * 3 * V * sizeof(double2), st));
   MARIE_CUDA_TRY(cudaStreamSynchronize(st));
   const auto t1 = std::chrono::steady_clock::now();

@@ -14,7 +14,17 @@
 // The Hessenberg update, the rotations and the small solve run on the device
 // in FP64 (one warp per system), so a whole restart cycle has no host
 // synchronisation and is replayed as one CUDA graph launch.
+//
+// The Krylov basis is stored and combined in FP64 (VB = double2, the
+// reference's arithmetic) or, for the inner solves of mixed-precision
+// refinement, in FP32 (VB = float2): the dots, the Gram-Schmidt update and
+// the basis combinations then run as FP32 FMAs with FP64 reductions across
+// threads, and read half the bytes.  The matvec always takes and returns FP64
+// vectors: with an FP32 basis the current column is kept in an FP64 copy (xin)
+// and the matvec writes to an FP64 work vector (wt) that the update folds into
+// the basis.  Hessenberg entries, rotations and residual norms stay FP64.
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "plan.h"
@@ -58,6 +68,8 @@ __device__ __forceinline__ void rows_of(long long n, long long& i0, long long& i
   i1 = i0 + chunk < n ? i0 + chunk : n;
 }
 __device__ __forceinline__ bool skip(const int* stop, int s, int step) { return stop[s] < step; }
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 // ||X_s||^2 partials: X_s = X + s*xs
 __global__ void __launch_bounds__(BT) kb_norm_part(const double2* __restrict__ X, long long xs, long long n,
@@ -87,42 +99,49 @@ __global__ void kb_norm_fin(const double* __restrict__ part, int G, const int* _
   if (threadIdx.x == 0) out[s] = sqrt(a);
 }
 
-// cycle start: V_s(:,0) = r_s / beta_s ; g = [beta, 0, ...]
-__global__ void kb_cycle_init(const double2* __restrict__ r, long long rs, double2* __restrict__ Vb, long long vs,
-                              long long n, const double* __restrict__ beta, const int* __restrict__ stop) {
+// cycle start: V_s(:,0) = r_s / beta_s (and its FP64 copy xin_s for an FP32 basis)
+template <typename VB>
+__global__ void kb_cycle_init(const double2* __restrict__ r, long long rs, VB* __restrict__ Vb, long long vs,
+                              long long n, const double* __restrict__ beta, const int* __restrict__ stop,
+                              double2* __restrict__ xin) {
   const int s = blockIdx.y;
   if (stop[s] < 1) return;
   const double inv = 1.0 / beta[s];  // 0 -> Inf/NaN exactly as the reference's r / norm(r)
   const double2* x = r + s * rs;
-  double2* v = Vb + s * vs;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    v[i] = mk<double2>(x[i].x * inv, x[i].y * inv);
+  VB* v = Vb + s * vs;
+  double2* xi = xin ? xin + s * n : nullptr;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const VB q = cvt<VB>(mk<double2>(x[i].x * inv, x[i].y * inv));
+    v[i] = q;
+    if (xi) xi[i] = cvt<double2>(q);
+  }
 }
 
 // One sweep over NC basis columns c0..c0+NC-1: the block's partial sums of
 // conj(V(:,j)) w, reduced in the block (warp sums, then warp partials in warp
 // order by one thread per column: a fixed order).  NC is a template argument
-// so that a short last sweep issues no idle FP64 work.
-template <int NC>
-__device__ __forceinline__ void kb_dot_sweep(const double2* __restrict__ V, const double2* __restrict__ w,
+// so that a short last sweep issues no idle work.  Each thread accumulates in
+// the basis precision; the sums across threads are FP64.
+template <int NC, typename VB>
+__device__ __forceinline__ void kb_dot_sweep(const VB* __restrict__ V, const double2* __restrict__ w,
                                              long long n, long long i0, long long i1, int c0,
                                              double2* __restrict__ part_s, double2 (*red)[8]) {
-  double2 acc[NC];
+  VB acc[NC];
 #pragma unroll
-  for (int q = 0; q < NC; ++q) acc[q] = mk<double2>(0, 0);
+  for (int q = 0; q < NC; ++q) acc[q] = mk<VB>(0, 0);
   for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    const double2 wv = w[i];
+    const VB wv = cvt<VB>(w[i]);
 #pragma unroll
     for (int q = 0; q < NC; ++q) {
-      const double2 v = V[(long long)(c0 + q) * n + i];
-      acc[q].x = fma(v.x, wv.x, fma(v.y, wv.y, acc[q].x));
-      acc[q].y = fma(v.x, wv.y, fma(-v.y, wv.x, acc[q].y));
+      const VB v = V[(long long)(c0 + q) * n + i];
+      acc[q].x = fmaT(v.x, wv.x, fmaT(v.y, wv.y, acc[q].x));
+      acc[q].y = fmaT(v.x, wv.y, fmaT(-v.y, wv.x, acc[q].y));
     }
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q < NC; ++q) {
-    const double2 r = wsum2(acc[q]);
+    const double2 r = wsum2(cvt<double2>(acc[q]));
     if (lane == 0) red[wid][q] = r;
   }
   __syncthreads();
@@ -134,13 +153,16 @@ __device__ __forceinline__ void kb_dot_sweep(const double2* __restrict__ V, cons
   __syncthreads();  // red is reused by the next sweep
 }
 
-// partial[s][j][b] = sum over block rows of conj(V_s(:,j)) w_s, j < k, w_s = V_s(:,k)
-__global__ void __launch_bounds__(BT) kb_dots(const double2* __restrict__ Vb, long long vs, long long n, int k,
+// partial[s][j][b] = sum over block rows of conj(V_s(:,j)) w_s, j < k, with
+// w_s = wb + s*ws the new matvec column (FP64)
+template <typename VB>
+__global__ void __launch_bounds__(BT) kb_dots(const VB* __restrict__ Vb, long long vs, long long n, int k,
+                                              const double2* __restrict__ wb, long long ws,
                                               const int* __restrict__ stop, double2* __restrict__ part) {
   const int s = blockIdx.y;
   if (skip(stop, s, k)) return;
-  const double2* V = Vb + s * vs;
-  const double2* w = V + (long long)k * n;
+  const VB* V = Vb + s * vs;
+  const double2* w = wb + s * ws;
   double2* part_s = part + (long long)s * 128 * gridDim.x;
   __shared__ double2 red[BT / 32][8];
   long long i0, i1;
@@ -170,32 +192,36 @@ __global__ void kb_dots_fin(const double2* __restrict__ part, int G, int k, cons
   if (threadIdx.x == 0) h[(long long)s * hld + j] = a;
 }
 
-// w_s -= V_s(:,0:k) h_s ; partial norms of the new w_s
-__global__ void __launch_bounds__(BT) kb_update(double2* __restrict__ Vb, long long vs, long long n, int k,
-                                                const double2* __restrict__ h, int hld, const int* __restrict__ stop,
-                                                double* __restrict__ part) {
+// V_s(:,k) = w_s - V_s(:,0:k) h_s ; partial norms of the new column.  With an
+// FP64 basis w_s is V_s(:,k) itself (updated in place).
+template <typename VB>
+__global__ void __launch_bounds__(BT) kb_update(VB* Vb, long long vs, long long n, int k, const double2* wb,
+                                                long long ws, const double2* __restrict__ h, int hld,
+                                                const int* __restrict__ stop, double* __restrict__ part) {
+  using R = decltype(VB::x);
   const int s = blockIdx.y;
   if (skip(stop, s, k)) return;
-  __shared__ double2 hs[128];
-  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = h[(long long)s * hld + j];
+  __shared__ VB hs[128];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = cvt<VB>(h[(long long)s * hld + j]);
   __syncthreads();
-  double2* V = Vb + s * vs;
-  double2* w = V + (long long)k * n;
+  VB* V = Vb + s * vs;
+  const double2* w = wb + s * ws;
+  VB* out = V + (long long)k * n;
   long long i0, i1;
   rows_of(n, i0, i1);
-  double a = 0;
+  R a = 0;
   for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    double2 v = w[i];
+    VB v = cvt<VB>(w[i]);
     for (int j = 0; j < k; ++j) {
-      const double2 b = V[(long long)j * n + i];
-      const double2 c = hs[j];
-      v.x = fma(-b.x, c.x, fma(b.y, c.y, v.x));
-      v.y = fma(-b.x, c.y, fma(-b.y, c.x, v.y));
+      const VB b = V[(long long)j * n + i];
+      const VB c = hs[j];
+      v.x = fmaT(-b.x, c.x, fmaT(b.y, c.y, v.x));
+      v.y = fmaT(-b.x, c.y, fmaT(-b.y, c.x, v.y));
     }
-    w[i] = v;
-    a = fma(v.x, v.x, fma(v.y, v.y, a));
+    out[i] = v;
+    a = fmaT(v.x, v.x, fmaT(v.y, v.y, a));
   }
-  const double2 r = bsum2(mk<double2>(a, 0));
+  const double2 r = bsum2(mk<double2>((double)a, 0));
   if (threadIdx.x == 0) part[(long long)s * gridDim.x + blockIdx.x] = r.x;
 }
 
@@ -316,39 +342,49 @@ __global__ void kb_givens(GState G, int m, int k, const double2* __restrict__ h,
   if (lane == 0) G.stop[s] = k;
 }
 
-// V_s(:,k) /= H(k+1,k)  (zero norm leaves a zero column instead of 0/0)
-__global__ void kb_scale(double2* __restrict__ Vb, long long vs, long long n, int k, const double* __restrict__ hn,
-                         const int* __restrict__ stop) {
+// V_s(:,k) /= H(k+1,k)  (zero norm leaves a zero column instead of 0/0), and
+// the FP64 copy xin_s of the column for an FP32 basis
+template <typename VB>
+__global__ void kb_scale(VB* __restrict__ Vb, long long vs, long long n, int k, const double* __restrict__ hn,
+                         const int* __restrict__ stop, double2* __restrict__ xin) {
+  using R = decltype(VB::x);
   const int s = blockIdx.y;
   if (skip(stop, s, k)) return;
   const double h = hn[s];
-  const double inv = h > 0 ? 1.0 / h : 0.0;
-  double2* w = Vb + s * vs + (long long)k * n;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    w[i] = mk<double2>(w[i].x * inv, w[i].y * inv);
+  const R inv = (R)(h > 0 ? 1.0 / h : 0.0);
+  VB* w = Vb + s * vs + (long long)k * n;
+  double2* xi = xin ? xin + s * n : nullptr;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const VB q = mk<VB>(w[i].x * inv, w[i].y * inv);
+    w[i] = q;
+    if (xi) xi[i] = cvt<double2>(q);
+  }
 }
 
-// out_s = V_s(:, 0:c_s) coef_s with c_s = stop[s] + extra (skipped when stop[s] < 1)
-__global__ void kb_combine(const double2* __restrict__ Vb, long long vs, long long n, const double2* __restrict__ coef,
+// out_s = V_s(:, 0:c_s) coef_s with c_s = stop[s] + extra (skipped when
+// stop[s] < 1), summed in the basis precision; accumulate adds out_s (FP64)
+template <typename VB>
+__global__ void kb_combine(const VB* __restrict__ Vb, long long vs, long long n, const double2* __restrict__ coef,
                            int cld, const int* __restrict__ stop, int extra, double2* __restrict__ out, long long os,
                            int accumulate) {
   const int s = blockIdx.y;
   const int k = stop[s];
   if (k < 1) return;
   const int nc = k + extra;
-  __shared__ double2 cf[129];
-  for (int j = threadIdx.x; j < nc; j += blockDim.x) cf[j] = coef[(long long)s * cld + j];
+  __shared__ VB cf[129];
+  for (int j = threadIdx.x; j < nc; j += blockDim.x) cf[j] = cvt<VB>(coef[(long long)s * cld + j]);
   __syncthreads();
-  const double2* V = Vb + s * vs;
+  const VB* V = Vb + s * vs;
   double2* o = out + s * os;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double2 v = accumulate ? o[i] : mk<double2>(0, 0);
+    VB v = mk<VB>(0, 0);
     for (int j = 0; j < nc; ++j) {
-      const double2 b = V[(long long)j * n + i];
-      v.x = fma(b.x, cf[j].x, fma(-b.y, cf[j].y, v.x));
-      v.y = fma(b.x, cf[j].y, fma(b.y, cf[j].x, v.y));
+      const VB b = V[(long long)j * n + i];
+      v.x = fmaT(b.x, cf[j].x, fmaT(-b.y, cf[j].y, v.x));
+      v.y = fmaT(b.x, cf[j].y, fmaT(b.y, cf[j].x, v.y));
     }
-    o[i] = v;
+    const double2 r = cvt<double2>(v);
+    o[i] = accumulate ? cadd(o[i], r) : r;
   }
 }
 
@@ -382,18 +418,24 @@ static inline int gx(long long n) {
 struct BatchWork {
   int S = 0, m = 0;
   long long n = 0;
-  DBuf V, t1, t2, r, part_d, part_n, h, H, R, g, cs, sn, y, res, resv, beta, tol, hn, stop, norms;
+  bool f32 = false;  // FP32 basis (with the FP64 column copy xin and matvec output wt)
+  DBuf V, xin, wt, t1, t2, r, part_d, part_n, h, H, R, g, cs, sn, y, res, resv, beta, tol, hn, stop, norms;
   GState gs{};
   cudaGraphExec_t exec = nullptr;
   long long graph_nodes = 0;
   ~BatchWork() {
     if (exec) cudaGraphExecDestroy(exec);
   }
-  int init(cudaStream_t st, int S_, int m_, long long n_) {
+  int init(cudaStream_t st, int S_, int m_, long long n_, bool f32_) {
     S = S_;
     m = m_;
     n = n_;
-    MARIE_TRY(V.alloc((size_t)S * (m + 1) * n * sizeof(double2), st));
+    f32 = f32_;
+    MARIE_TRY(V.alloc((size_t)S * (m + 1) * n * (f32 ? sizeof(float2) : sizeof(double2)), st));
+    if (f32) {
+      MARIE_TRY(xin.alloc((size_t)S * n * sizeof(double2), st));
+      MARIE_TRY(wt.alloc((size_t)S * n * sizeof(double2), st));
+    }
     MARIE_TRY(t1.alloc((size_t)S * n * sizeof(double2), st));
     MARIE_TRY(t2.alloc((size_t)S * n * sizeof(double2), st));
     MARIE_TRY(part_d.alloc((size_t)S * 128 * BG * sizeof(double2), st));
@@ -434,41 +476,48 @@ static int bnorms(marie_plan* p, BatchWork& W, const double2* X, long long xs, s
 }
 
 // one restart cycle for all systems with stop[s] = m (others stop[s] = 0)
+template <typename VB>
 static int cycle(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, double2* X,
                  long long xs, double2* Rv, long long rs) {
+  constexpr bool F32 = std::is_same<VB, float2>::value;
   cudaStream_t st = p->stream;
   const int S = W.S, m = W.m;
   const long long n = W.n, vs = W.vs();
-  double2* V = W.V.as<double2>();
+  VB* V = W.V.as<VB>();
+  double2* xin = F32 ? W.xin.as<double2>() : nullptr;
   int* stop = W.stop.as<int>();
   kb_norm_part<<<dim3(BG, S), BT, 0, st>>>(Rv, rs, n, stop, 1, W.part_n.as<double>());
   kb_norm_fin<<<S, 32, 0, st>>>(W.part_n.as<double>(), BG, stop, 1, W.beta.as<double>());
-  kb_cycle_init<<<dim3(gx(n), S), 256, 0, st>>>(Rv, rs, V, vs, n, W.beta.as<double>(), stop);
+  kb_cycle_init<VB><<<dim3(gx(n), S), 256, 0, st>>>(Rv, rs, V, vs, n, W.beta.as<double>(), stop, xin);
   count_launch(3);
   for (int k = 1; k <= m; ++k) {
-    const double2* src = V + (long long)(k - 1) * n;
-    long long ss = vs;
+    // the matvec input: the previous column (its FP64 copy for an FP32 basis)
+    const double2* src = F32 ? (const double2*)xin : (const double2*)V + (long long)(k - 1) * n;
+    long long ss = F32 ? n : vs;
     if (R1) {
       MARIE_TRY(R1->apply(src, ss, W.t1.as<double2>(), n, S, stop, k));
       src = W.t1.as<double2>();
       ss = n;
     }
-    double2* dst = V + (long long)k * n;
+    // the matvec output: column k itself (FP64 basis) or the work vector
+    double2* dst = F32 ? W.wt.as<double2>() : (double2*)V + (long long)k * n;
+    const long long ds = F32 ? n : vs;
     if (L1) {
       MARIE_TRY(A.apply(src, ss, W.t2.as<double2>(), n, S, stop, k));
-      MARIE_TRY(L1->apply(W.t2.as<double2>(), n, dst, vs, S, stop, k));
+      MARIE_TRY(L1->apply(W.t2.as<double2>(), n, dst, ds, S, stop, k));
     } else {
-      MARIE_TRY(A.apply(src, ss, dst, vs, S, stop, k));
+      MARIE_TRY(A.apply(src, ss, dst, ds, S, stop, k));
     }
-    kb_dots<<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, stop, W.part_d.as<double2>());
+    kb_dots<VB><<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, dst, ds, stop, W.part_d.as<double2>());
     kb_dots_fin<<<dim3(k, S), 32, 0, st>>>(W.part_d.as<double2>(), BG, k, stop, W.h.as<double2>(), m + 1);
-    kb_update<<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, W.h.as<double2>(), m + 1, stop, W.part_n.as<double>());
+    kb_update<VB><<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, dst, ds, W.h.as<double2>(), m + 1, stop,
+                                              W.part_n.as<double>());
     kb_givens<<<S, 32, 0, st>>>(W.gs, m, k, W.h.as<double2>(), m + 1, W.part_n.as<double>(), BG);
-    kb_scale<<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, k, W.hn.as<double>(), stop);
+    kb_scale<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, k, W.hn.as<double>(), stop, xin);
     count_launch(5);
   }
   // x += R1(V y) ; r = V(:,1:k+1) res
-  kb_combine<<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, W.y.as<double2>(), m, stop, 0, W.t1.as<double2>(), n, 0);
+  kb_combine<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, W.y.as<double2>(), m, stop, 0, W.t1.as<double2>(), n, 0);
   count_launch();
   const double2* upd = W.t1.as<double2>();
   if (R1) {
@@ -476,7 +525,7 @@ static int cycle(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L
     upd = W.t2.as<double2>();
   }
   kb_add<<<dim3(gx(n), S), 256, 0, st>>>(upd, n, X, xs, n, stop);
-  kb_combine<<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, W.res.as<double2>(), m + 1, stop, 1, Rv, rs, 0);
+  kb_combine<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, W.res.as<double2>(), m + 1, stop, 1, Rv, rs, 0);
   count_launch(2);
   MARIE_CUDA_TRY(cudaGetLastError());
   return MARIE_OK;
@@ -485,12 +534,15 @@ static int cycle(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L
 int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const double2* B,
                 long long bs, long long n, int S, int restart, double tol, int maxit, double2* X, long long xs,
                 std::vector<GmresResult>& out, bool use_graph, const std::vector<int>* active_in,
-                bool true_residual) {
+                bool true_residual, bool fp32_basis) {
   if (restart < 1 || restart > 127) return set_error(MARIE_EINVAL, "restart must be in [1, 127]");
   if (S < 1) return set_error(MARIE_EINVAL, "need at least one system");
   cudaStream_t st = p->stream;
   BatchWork W;
-  MARIE_TRY(W.init(st, S, restart, n));
+  MARIE_TRY(W.init(st, S, restart, n, fp32_basis));
+  auto run_cycle = [&](double2* Xc, double2* Rc) {
+    return W.f32 ? cycle<float2>(p, W, A, L1, R1, Xc, xs, Rc, n) : cycle<double2>(p, W, A, L1, R1, Xc, xs, Rc, n);
+  };
   DBuf rb, bpb;
   MARIE_TRY(rb.alloc((size_t)S * n * sizeof(double2), st));
   double2* Rv = rb.as<double2>();
@@ -545,7 +597,7 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
       if (!W.exec) {
         cudaGraph_t graph;
         MARIE_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        const int s1 = cycle(p, W, A, L1, R1, X, xs, Rv, rs);
+        const int s1 = run_cycle(X, Rv);
         cudaError_t e = cudaStreamEndCapture(st, &graph);
         MARIE_TRY(s1);
         MARIE_CUDA_TRY(e);
@@ -559,7 +611,7 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
       MARIE_CUDA_TRY(cudaGraphLaunch(W.exec, st));
       count_launch(W.graph_nodes);
     } else {
-      MARIE_TRY(cycle(p, W, A, L1, R1, X, xs, Rv, rs));
+      MARIE_TRY(run_cycle(X, Rv));
     }
     ++cycles;
     MARIE_CUDA_TRY(cudaMemcpyAsync(stop.data(), W.stop.p, S * sizeof(int), cudaMemcpyDeviceToHost, st));

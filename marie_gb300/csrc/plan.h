@@ -1,6 +1,9 @@
 // Internal plan state shared by the C-ABI translation units.
 #pragma once
+#include <unistd.h>
+
 #include <functional>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -21,6 +24,7 @@ struct marie_plan {
   bool fuse = true;  // fused x+y / y+x passes when the grid has them
   int fvar = 0;      // x/y radix schedule of the fused passes (set by marie_plan_autotune)
   int zvar = 0;      // z-pass variant of the FP32 N matvec (set by marie_plan_autotune)
+  int inner_prec = MARIE_FP32;  // Krylov basis of the mixed-precision inner solves
   int oct = 0;  // 1: fN64/fN32 hold the (L+1)(M+1)(N+1) octant, 0: the full array
 
   // K operator (mv_K, H_field_Kop), same scaling and layouts with 3 components.
@@ -74,6 +78,28 @@ int stage_in(const void* user, size_t bytes, cudaStream_t st, DBuf& tmp, const v
 // Output view: device pointer to write to; finish_out copies back to host.
 int stage_out(void* user, size_t bytes, cudaStream_t st, DBuf& tmp, void** dev);
 int finish_out(void* user, const void* dev, size_t bytes, cudaStream_t st);
+
+// Faults in the pages of a host output buffer on a helper thread (one write
+// per page), so that the operating system's zero-fill of freshly mapped pages
+// runs while the device solves instead of inside the final device-to-host
+// copy.  Device pointers are left alone.  join() before writing the buffer.
+struct HostPrefault {
+  std::thread t;
+  void start(void* user, size_t bytes) {
+    if (!user || bytes == 0 || is_device_ptr(user)) return;
+    t = std::thread([user, bytes] {
+      const long pg = sysconf(_SC_PAGESIZE);
+      const size_t step = pg > 0 ? (size_t)pg : 4096;
+      volatile char* c = static_cast<volatile char*>(user);
+      for (size_t off = 0; off < bytes; off += step) c[off] = 0;
+      c[bytes - 1] = 0;
+    });
+  }
+  void join() {
+    if (t.joinable()) t.join();
+  }
+  ~HostPrefault() { join(); }
+};
 
 int ensure_workspace(marie_plan* p, int prec, long long nrhs, bool with_A = true);
 int ensure_pinned(marie_plan* p, size_t n_doubles);
@@ -130,7 +156,7 @@ struct BatchOp {
 int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const double2* B,
                 long long bs, long long n, int S, int restart, double tol, int maxit, double2* X, long long xs,
                 std::vector<GmresResult>& out, bool use_graph, const std::vector<int>* active_in,
-                bool true_residual);
+                bool true_residual, bool fp32_basis = false);
 
 // MATLAB bicgstab semantics (the solver 'B' of JVIE_Solver.m:451-499) on
 // device vectors: iter in half steps, resvec absolute (bicgstab.cu).

@@ -187,6 +187,11 @@ class Operator:
         check(self.lib.marie_plan_set_schedule(self.plan, int(fuse), int(fvar), int(zvar)))
         return self
 
+    def set_inner_precision(self, precision):
+        """Krylov basis of the inner solves of a 'mixed' plan: 'fp32' (default) or 'fp64'."""
+        check(self.lib.marie_plan_set_inner_precision(self.plan, {"fp32": 32, "fp64": 64}[precision]))
+        return self
+
     def to_array(self):
         """The FP64 operator as a 2L x 2M x 2N x 6 numpy array."""
         ptr, arr = _out((2 * self.L, 2 * self.M, 2 * self.N, 6), False)
