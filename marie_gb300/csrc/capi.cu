@@ -264,8 +264,8 @@ int build_coefficients(marie_plan* p, const int64_t* idx_dev, long long n, const
   return MARIE_OK;
 }
 
-template <typename T>
-static int run_matvec_t(marie_plan* p, const double2* J, long long js, double2* out, long long os, long long n,
+template <typename T, typename IO>
+static int run_matvec_t(marie_plan* p, const IO* J, long long js, IO* out, long long os, long long n,
                         int nrhs, const int* inv, const Prologue& pro, const Epilogue& ep, const cplx<T>* fN,
                         cplx<T>* const* tw, const int* stop, int step, int kind) {
   const int oct = kind == 0 ? p->oct : p->octK;
@@ -282,8 +282,8 @@ static int run_matvec_t(marie_plan* p, const double2* J, long long js, double2* 
     cplx<T>* A = reinterpret_cast<cplx<T>*>(p->wsA);
     cplx<T>* B = reinterpret_cast<cplx<T>*>(p->wsB);
     const long long sA = p->elems_A(), sB = p->elems_B();
-    const double2* Jc = J + r0 * js;
-    double2* oc = out + r0 * os;
+    const IO* Jc = J + r0 * js;
+    IO* oc = out + r0 * os;
     const bool prof = p->profile;
     if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[0], p->stream));
     if (fused) {
@@ -338,10 +338,23 @@ int run_matvec(marie_plan* p, int prec, const double2* J, long long js, double2*
   const double2* f64 = kind == 0 ? p->fN64 : p->fK64;
   if (prec == MARIE_FP32) {
     if (!f32) return set_error(MARIE_EINVAL, "plan was not created with FP32 arithmetic");
-    return run_matvec_t<float>(p, J, js, out, os, n, nrhs, inv, pro, ep, f32, p->tw32, stop, step, kind);
+    return run_matvec_t<float, double2>(p, J, js, out, os, n, nrhs, inv, pro, ep, f32, p->tw32, stop, step, kind);
   }
   if (!f64) return set_error(MARIE_EINVAL, "plan was not created with FP64 arithmetic");
-  return run_matvec_t<double>(p, J, js, out, os, n, nrhs, inv, pro, ep, f64, p->tw64, stop, step, kind);
+  return run_matvec_t<double, double2>(p, J, js, out, os, n, nrhs, inv, pro, ep, f64, p->tw64, stop, step, kind);
+}
+
+int run_matvec32(marie_plan* p, const float2* J, long long js, float2* out, long long os, long long n, int nrhs,
+                 const int* inv, const Prologue& pro, const Epilogue& ep, const int* stop, int step, int kind) {
+  if (kind == 0 && !p->has_op)
+    return set_error(MARIE_ENOOP, "plan has no operator: call marie_set_operator or marie_plan_assemble");
+  if (kind == 1 && !p->has_opK)
+    return set_error(MARIE_ENOOP, "plan has no K operator: call marie_set_operator_k or marie_plan_assemble_k");
+  const float2* f32 = kind == 0 ? p->fN32 : p->fK32;
+  if (!f32) return set_error(MARIE_EINVAL, "plan was not created with FP32 arithmetic");
+  if ((ep.a && !ep.af) || (ep.b && !ep.bf))
+    return set_error(MARIE_EINVAL, "FP32 matvec needs the FP32 copies of per-DOF coefficients");
+  return run_matvec_t<float, float2>(p, J, js, out, os, n, nrhs, inv, pro, ep, f32, p->tw32, stop, step, kind);
 }
 
 int run_matvec(marie_plan* p, int prec, const double2* J, double2* out, long long n, int nrhs, const int* inv,

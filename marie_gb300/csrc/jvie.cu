@@ -147,6 +147,27 @@ __global__ void k_diag_b(const double2* __restrict__ a, const double2* __restric
     y[s * ys + k] = cmul(a[k], x[s * xs + k]);
 }
 
+__global__ void k_diag_b32(const float2* __restrict__ a, const float2* __restrict__ x, long long xs,
+                           float2* __restrict__ y, long long ys, long long n, const int* __restrict__ stop, int step) {
+  const int s = blockIdx.y;
+  if (stop && stop[s] < step) return;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    y[s * ys + k] = cmul(a[k], x[s * xs + k]);
+}
+
+// FP32 copies of the four per-DOF coefficient arrays
+__global__ void k_coef_f32(const double2* __restrict__ a, const double2* __restrict__ b,
+                           const double2* __restrict__ pa, const double2* __restrict__ pb, long long n,
+                           float2* __restrict__ af, float2* __restrict__ bf, float2* __restrict__ paf,
+                           float2* __restrict__ pbf) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    af[k] = cvt<float2>(a[k]);
+    bf[k] = cvt<float2>(b[k]);
+    paf[k] = cvt<float2>(pa[k]);
+    pbf[k] = cvt<float2>(pb[k]);
+  }
+}
+
 __global__ void k_any_nonzero(const double2* __restrict__ b, long long n, int* __restrict__ nonzero) {
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
     if (b[k].x != 0.0 || b[k].y != 0.0) *nonzero = 1;
@@ -171,6 +192,7 @@ __global__ void k_add_b(const double2* __restrict__ d, double2* __restrict__ x, 
 struct JvieState {
   long long nS = 0, n = 0;
   DBuf idxS, idx3, inv, f, a, b, pa, pb;
+  DBuf af, bf, paf, pbf;  // FP32 copies of a, b, pa, pb (plans with an FP32 operator)
 };
 
 static int jvie_setup(marie_plan* p, const double2* er, double dx, double freq, int form, JvieState& S) {
@@ -212,6 +234,17 @@ static int jvie_setup(marie_plan* p, const double2* er, double dx, double freq, 
                                          S.b.as<double2>(), S.pa.as<double2>(), S.pb.as<double2>());
   count_launch();
   MARIE_CUDA_TRY(cudaGetLastError());
+  if (p->fN32) {
+    MARIE_TRY(S.af.alloc(n * sizeof(float2), st));
+    MARIE_TRY(S.bf.alloc(n * sizeof(float2), st));
+    MARIE_TRY(S.paf.alloc(n * sizeof(float2), st));
+    MARIE_TRY(S.pbf.alloc(n * sizeof(float2), st));
+    k_coef_f32<<<grid_n(n), 256, 0, st>>>(S.a.as<double2>(), S.b.as<double2>(), S.pa.as<double2>(),
+                                          S.pb.as<double2>(), n, S.af.as<float2>(), S.bf.as<float2>(),
+                                          S.paf.as<float2>(), S.pbf.as<float2>());
+    count_launch();
+    MARIE_CUDA_TRY(cudaGetLastError());
+  }
   MARIE_TRY(build_inverse_index(p, S.idx3.as<int64_t>(), n, S.inv.as<int>()));
   return MARIE_OK;
 }
@@ -233,10 +266,26 @@ static int any_nonzero(marie_plan* p, const double2* b, long long n, bool* nz) {
 // b that is identically zero leaves only the diagonal Gram*Mr product (the
 // circulant term is multiplied by zero in mv_AN.m:127-131), so no FFT runs.
 static BatchOp make_bop(marie_plan* p, int prec, const JvieState& S, const double2* a, const double2* b,
-                        bool diag_only) {
+                        bool diag_only, const float2* af = nullptr, const float2* bf = nullptr) {
   const long long n = S.n;
   const int* inv = S.inv.as<int>();
   BatchOp op;
+  if (prec == MARIE_FP32 && af && bf) {
+    op.apply32 = [p, n, inv, af, bf, diag_only](const float2* in, long long is, float2* out, long long os, int ns,
+                                                const int* stop, int step) -> int {
+      if (diag_only) {
+        k_diag_b32<<<dim3(grid_n(n), ns), 256, 0, p->stream>>>(af, in, is, out, os, n, stop, step);
+        count_launch();
+        MARIE_CUDA_TRY(cudaGetLastError());
+        return MARIE_OK;
+      }
+      Prologue pro{nullptr, 0};
+      Epilogue ep{};
+      ep.af = af;
+      ep.bf = bf;
+      return run_matvec32(p, in, is, out, os, n, ns, inv, pro, ep, stop, step);
+    };
+  }
   op.apply = [p, prec, n, inv, a, b, diag_only](const double2* in, long long is, double2* out, long long os, int ns,
                                                 const int* stop, int step) -> int {
     if (diag_only) {
@@ -328,8 +377,10 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
                           true));
   } else {
     // GMRES-IR: FP32-matvec pgmres on the residual, FP64 true residual and correction
-    BatchOp A32 = make_bop(p, MARIE_FP32, S, S.a.as<double2>(), S.b.as<double2>(), false);
-    BatchOp P32 = make_bop(p, MARIE_FP32, S, S.pa.as<double2>(), S.pb.as<double2>(), !pb_nz);
+    BatchOp A32 = make_bop(p, MARIE_FP32, S, S.a.as<double2>(), S.b.as<double2>(), false, S.af.as<float2>(),
+                           S.bf.as<float2>());
+    BatchOp P32 = make_bop(p, MARIE_FP32, S, S.pa.as<double2>(), S.pb.as<double2>(), !pb_nz, S.paf.as<float2>(),
+                           S.pbf.as<float2>());
     const BatchOp* L1m = precond == 'L' ? &P32 : nullptr;
     const BatchOp* R1m = precond == 'R' ? &P32 : nullptr;
     DBuf rb, db, flags;

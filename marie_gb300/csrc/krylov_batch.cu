@@ -17,12 +17,11 @@
 //
 // The Krylov basis is stored and combined in FP64 (VB = double2, the
 // reference's arithmetic) or, for the inner solves of mixed-precision
-// refinement, in FP32 (VB = float2): the dots, the Gram-Schmidt update and
-// the basis combinations then run as FP32 FMAs with FP64 reductions across
-// threads, and read half the bytes.  The matvec always takes and returns FP64
-// vectors: with an FP32 basis the current column is kept in an FP64 copy (xin)
-// and the matvec writes to an FP64 work vector (wt) that the update folds into
-// the basis.  Hessenberg entries, rotations and residual norms stay FP64.
+// refinement, in FP32 (VB = float2): the matvec then reads and writes FP32
+// basis columns (BatchOp::apply32), and the dots, the Gram-Schmidt update and
+// the basis combinations run as FP32 FMAs with FP64 reductions across
+// threads, reading half the bytes.  Hessenberg entries, rotations, residual
+// norms, the iterate and the restart residual stay FP64.
 #include <cmath>
 #include <type_traits>
 #include <vector>
@@ -99,22 +98,17 @@ __global__ void kb_norm_fin(const double* __restrict__ part, int G, const int* _
   if (threadIdx.x == 0) out[s] = sqrt(a);
 }
 
-// cycle start: V_s(:,0) = r_s / beta_s (and its FP64 copy xin_s for an FP32 basis)
+// cycle start: V_s(:,0) = r_s / beta_s
 template <typename VB>
 __global__ void kb_cycle_init(const double2* __restrict__ r, long long rs, VB* __restrict__ Vb, long long vs,
-                              long long n, const double* __restrict__ beta, const int* __restrict__ stop,
-                              double2* __restrict__ xin) {
+                              long long n, const double* __restrict__ beta, const int* __restrict__ stop) {
   const int s = blockIdx.y;
   if (stop[s] < 1) return;
   const double inv = 1.0 / beta[s];  // 0 -> Inf/NaN exactly as the reference's r / norm(r)
   const double2* x = r + s * rs;
   VB* v = Vb + s * vs;
-  double2* xi = xin ? xin + s * n : nullptr;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const VB q = cvt<VB>(mk<double2>(x[i].x * inv, x[i].y * inv));
-    v[i] = q;
-    if (xi) xi[i] = cvt<double2>(q);
-  }
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    v[i] = cvt<VB>(mk<double2>(x[i].x * inv, x[i].y * inv));
 }
 
 // One sweep over NC basis columns c0..c0+NC-1: the block's partial sums of
@@ -123,14 +117,14 @@ __global__ void kb_cycle_init(const double2* __restrict__ r, long long rs, VB* _
 // so that a short last sweep issues no idle work.  Each thread accumulates in
 // the basis precision; the sums across threads are FP64.
 template <int NC, typename VB>
-__device__ __forceinline__ void kb_dot_sweep(const VB* __restrict__ V, const double2* __restrict__ w,
+__device__ __forceinline__ void kb_dot_sweep(const VB* __restrict__ V, const VB* __restrict__ w,
                                              long long n, long long i0, long long i1, int c0,
                                              double2* __restrict__ part_s, double2 (*red)[8]) {
   VB acc[NC];
 #pragma unroll
   for (int q = 0; q < NC; ++q) acc[q] = mk<VB>(0, 0);
   for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    const VB wv = cvt<VB>(w[i]);
+    const VB wv = w[i];
 #pragma unroll
     for (int q = 0; q < NC; ++q) {
       const VB v = V[(long long)(c0 + q) * n + i];
@@ -153,16 +147,14 @@ __device__ __forceinline__ void kb_dot_sweep(const VB* __restrict__ V, const dou
   __syncthreads();  // red is reused by the next sweep
 }
 
-// partial[s][j][b] = sum over block rows of conj(V_s(:,j)) w_s, j < k, with
-// w_s = wb + s*ws the new matvec column (FP64)
+// partial[s][j][b] = sum over block rows of conj(V_s(:,j)) w_s, j < k, w_s = V_s(:,k)
 template <typename VB>
 __global__ void __launch_bounds__(BT) kb_dots(const VB* __restrict__ Vb, long long vs, long long n, int k,
-                                              const double2* __restrict__ wb, long long ws,
                                               const int* __restrict__ stop, double2* __restrict__ part) {
   const int s = blockIdx.y;
   if (skip(stop, s, k)) return;
   const VB* V = Vb + s * vs;
-  const double2* w = wb + s * ws;
+  const VB* w = V + (long long)k * n;
   double2* part_s = part + (long long)s * 128 * gridDim.x;
   __shared__ double2 red[BT / 32][8];
   long long i0, i1;
@@ -192,11 +184,10 @@ __global__ void kb_dots_fin(const double2* __restrict__ part, int G, int k, cons
   if (threadIdx.x == 0) h[(long long)s * hld + j] = a;
 }
 
-// V_s(:,k) = w_s - V_s(:,0:k) h_s ; partial norms of the new column.  With an
-// FP64 basis w_s is V_s(:,k) itself (updated in place).
+// w_s -= V_s(:,0:k) h_s with w_s = V_s(:,k) ; partial norms of the new w_s
 template <typename VB>
-__global__ void __launch_bounds__(BT) kb_update(VB* Vb, long long vs, long long n, int k, const double2* wb,
-                                                long long ws, const double2* __restrict__ h, int hld,
+__global__ void __launch_bounds__(BT) kb_update(VB* __restrict__ Vb, long long vs, long long n, int k,
+                                                const double2* __restrict__ h, int hld,
                                                 const int* __restrict__ stop, double* __restrict__ part) {
   using R = decltype(VB::x);
   const int s = blockIdx.y;
@@ -205,20 +196,19 @@ __global__ void __launch_bounds__(BT) kb_update(VB* Vb, long long vs, long long 
   for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = cvt<VB>(h[(long long)s * hld + j]);
   __syncthreads();
   VB* V = Vb + s * vs;
-  const double2* w = wb + s * ws;
-  VB* out = V + (long long)k * n;
+  VB* w = V + (long long)k * n;
   long long i0, i1;
   rows_of(n, i0, i1);
   R a = 0;
   for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    VB v = cvt<VB>(w[i]);
+    VB v = w[i];
     for (int j = 0; j < k; ++j) {
       const VB b = V[(long long)j * n + i];
       const VB c = hs[j];
       v.x = fmaT(-b.x, c.x, fmaT(b.y, c.y, v.x));
       v.y = fmaT(-b.x, c.y, fmaT(-b.y, c.x, v.y));
     }
-    out[i] = v;
+    w[i] = v;
     a = fmaT(v.x, v.x, fmaT(v.y, v.y, a));
   }
   const double2 r = bsum2(mk<double2>((double)a, 0));
@@ -342,23 +332,18 @@ __global__ void kb_givens(GState G, int m, int k, const double2* __restrict__ h,
   if (lane == 0) G.stop[s] = k;
 }
 
-// V_s(:,k) /= H(k+1,k)  (zero norm leaves a zero column instead of 0/0), and
-// the FP64 copy xin_s of the column for an FP32 basis
+// V_s(:,k) /= H(k+1,k)  (zero norm leaves a zero column instead of 0/0)
 template <typename VB>
 __global__ void kb_scale(VB* __restrict__ Vb, long long vs, long long n, int k, const double* __restrict__ hn,
-                         const int* __restrict__ stop, double2* __restrict__ xin) {
+                         const int* __restrict__ stop) {
   using R = decltype(VB::x);
   const int s = blockIdx.y;
   if (skip(stop, s, k)) return;
   const double h = hn[s];
   const R inv = (R)(h > 0 ? 1.0 / h : 0.0);
   VB* w = Vb + s * vs + (long long)k * n;
-  double2* xi = xin ? xin + s * n : nullptr;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const VB q = mk<VB>(w[i].x * inv, w[i].y * inv);
-    w[i] = q;
-    if (xi) xi[i] = cvt<double2>(q);
-  }
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    w[i] = mk<VB>(w[i].x * inv, w[i].y * inv);
 }
 
 // out_s = V_s(:, 0:c_s) coef_s with c_s = stop[s] + extra (skipped when
@@ -418,8 +403,8 @@ static inline int gx(long long n) {
 struct BatchWork {
   int S = 0, m = 0;
   long long n = 0;
-  bool f32 = false;  // FP32 basis (with the FP64 column copy xin and matvec output wt)
-  DBuf V, xin, wt, t1, t2, r, part_d, part_n, h, H, R, g, cs, sn, y, res, resv, beta, tol, hn, stop, norms;
+  bool f32 = false;  // FP32 basis (t1f, t2f: FP32 work vectors of the preconditioner chains)
+  DBuf V, t1, t2, t1f, t2f, r, part_d, part_n, h, H, R, g, cs, sn, y, res, resv, beta, tol, hn, stop, norms;
   GState gs{};
   cudaGraphExec_t exec = nullptr;
   long long graph_nodes = 0;
@@ -433,8 +418,8 @@ struct BatchWork {
     f32 = f32_;
     MARIE_TRY(V.alloc((size_t)S * (m + 1) * n * (f32 ? sizeof(float2) : sizeof(double2)), st));
     if (f32) {
-      MARIE_TRY(xin.alloc((size_t)S * n * sizeof(double2), st));
-      MARIE_TRY(wt.alloc((size_t)S * n * sizeof(double2), st));
+      MARIE_TRY(t1f.alloc((size_t)S * n * sizeof(float2), st));
+      MARIE_TRY(t2f.alloc((size_t)S * n * sizeof(float2), st));
     }
     MARIE_TRY(t1.alloc((size_t)S * n * sizeof(double2), st));
     MARIE_TRY(t2.alloc((size_t)S * n * sizeof(double2), st));
@@ -475,45 +460,63 @@ static int bnorms(marie_plan* p, BatchWork& W, const double2* X, long long xs, s
   return MARIE_OK;
 }
 
+// dst = L1 A R1 src for basis columns (stride vs), FP64 or FP32 vectors
+static int basis_matvec(BatchWork& W, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const double2* src,
+                        double2* dst, int k) {
+  const int S = W.S;
+  const long long n = W.n, vs = W.vs();
+  const int* stop = W.stop.as<int>();
+  long long ss = vs;
+  if (R1) {
+    MARIE_TRY(R1->apply(src, ss, W.t1.as<double2>(), n, S, stop, k));
+    src = W.t1.as<double2>();
+    ss = n;
+  }
+  if (L1) {
+    MARIE_TRY(A.apply(src, ss, W.t2.as<double2>(), n, S, stop, k));
+    return L1->apply(W.t2.as<double2>(), n, dst, vs, S, stop, k);
+  }
+  return A.apply(src, ss, dst, vs, S, stop, k);
+}
+static int basis_matvec(BatchWork& W, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const float2* src,
+                        float2* dst, int k) {
+  const int S = W.S;
+  const long long n = W.n, vs = W.vs();
+  const int* stop = W.stop.as<int>();
+  long long ss = vs;
+  if (R1) {
+    MARIE_TRY(R1->apply32(src, ss, W.t1f.as<float2>(), n, S, stop, k));
+    src = W.t1f.as<float2>();
+    ss = n;
+  }
+  if (L1) {
+    MARIE_TRY(A.apply32(src, ss, W.t2f.as<float2>(), n, S, stop, k));
+    return L1->apply32(W.t2f.as<float2>(), n, dst, vs, S, stop, k);
+  }
+  return A.apply32(src, ss, dst, vs, S, stop, k);
+}
+
 // one restart cycle for all systems with stop[s] = m (others stop[s] = 0)
 template <typename VB>
 static int cycle(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, double2* X,
                  long long xs, double2* Rv, long long rs) {
-  constexpr bool F32 = std::is_same<VB, float2>::value;
   cudaStream_t st = p->stream;
   const int S = W.S, m = W.m;
   const long long n = W.n, vs = W.vs();
   VB* V = W.V.as<VB>();
-  double2* xin = F32 ? W.xin.as<double2>() : nullptr;
   int* stop = W.stop.as<int>();
   kb_norm_part<<<dim3(BG, S), BT, 0, st>>>(Rv, rs, n, stop, 1, W.part_n.as<double>());
   kb_norm_fin<<<S, 32, 0, st>>>(W.part_n.as<double>(), BG, stop, 1, W.beta.as<double>());
-  kb_cycle_init<VB><<<dim3(gx(n), S), 256, 0, st>>>(Rv, rs, V, vs, n, W.beta.as<double>(), stop, xin);
+  kb_cycle_init<VB><<<dim3(gx(n), S), 256, 0, st>>>(Rv, rs, V, vs, n, W.beta.as<double>(), stop);
   count_launch(3);
   for (int k = 1; k <= m; ++k) {
-    // the matvec input: the previous column (its FP64 copy for an FP32 basis)
-    const double2* src = F32 ? (const double2*)xin : (const double2*)V + (long long)(k - 1) * n;
-    long long ss = F32 ? n : vs;
-    if (R1) {
-      MARIE_TRY(R1->apply(src, ss, W.t1.as<double2>(), n, S, stop, k));
-      src = W.t1.as<double2>();
-      ss = n;
-    }
-    // the matvec output: column k itself (FP64 basis) or the work vector
-    double2* dst = F32 ? W.wt.as<double2>() : (double2*)V + (long long)k * n;
-    const long long ds = F32 ? n : vs;
-    if (L1) {
-      MARIE_TRY(A.apply(src, ss, W.t2.as<double2>(), n, S, stop, k));
-      MARIE_TRY(L1->apply(W.t2.as<double2>(), n, dst, ds, S, stop, k));
-    } else {
-      MARIE_TRY(A.apply(src, ss, dst, ds, S, stop, k));
-    }
-    kb_dots<VB><<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, dst, ds, stop, W.part_d.as<double2>());
+    // V(:,k) = L1 A R1 V(:,k-1), in the basis precision
+    MARIE_TRY(basis_matvec(W, A, L1, R1, V + (long long)(k - 1) * n, V + (long long)k * n, k));
+    kb_dots<VB><<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, stop, W.part_d.as<double2>());
     kb_dots_fin<<<dim3(k, S), 32, 0, st>>>(W.part_d.as<double2>(), BG, k, stop, W.h.as<double2>(), m + 1);
-    kb_update<VB><<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, dst, ds, W.h.as<double2>(), m + 1, stop,
-                                              W.part_n.as<double>());
+    kb_update<VB><<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, W.h.as<double2>(), m + 1, stop, W.part_n.as<double>());
     kb_givens<<<S, 32, 0, st>>>(W.gs, m, k, W.h.as<double2>(), m + 1, W.part_n.as<double>(), BG);
-    kb_scale<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, k, W.hn.as<double>(), stop, xin);
+    kb_scale<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, k, W.hn.as<double>(), stop);
     count_launch(5);
   }
   // x += R1(V y) ; r = V(:,1:k+1) res
@@ -539,6 +542,8 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
   if (S < 1) return set_error(MARIE_EINVAL, "need at least one system");
   cudaStream_t st = p->stream;
   BatchWork W;
+  if (fp32_basis && (!A.apply32 || (L1 && !L1->apply32) || (R1 && !R1->apply32)))
+    return set_error(MARIE_EINVAL, "an FP32 Krylov basis needs operators on FP32 vectors");
   MARIE_TRY(W.init(st, S, restart, n, fp32_basis));
   auto run_cycle = [&](double2* Xc, double2* Rc) {
     return W.f32 ? cycle<float2>(p, W, A, L1, R1, Xc, xs, Rc, n) : cycle<double2>(p, W, A, L1, R1, Xc, xs, Rc, n);

@@ -48,9 +48,9 @@ template <typename T, int NL, int NM, int CS, bool NARROW = false> struct XYCfg 
                              FY::T <= THREADS;
 };
 
-template <typename T, int NL, int NM, int CS, bool NARROW>
+template <typename T, int NL, int NM, int CS, bool NARROW, typename IO>
 __global__ void __launch_bounds__(256, NARROW ? 4 : 0)
-k_xyfwd(const double2* __restrict__ J, long long js, const int* __restrict__ inv, Prologue pro,
+k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Prologue pro,
         cplx<T>* __restrict__ B, long long bs, Dims d, const cplx<T>* __restrict__ twx,
         const cplx<T>* __restrict__ twy) {
   if (rhs_skipped(d, blockIdx.y)) return;  // uniform over the cluster
@@ -67,7 +67,7 @@ k_xyfwd(const double2* __restrict__ J, long long js, const int* __restrict__ inv
   cg::cluster_group cluster = cg::this_cluster();
   const int q = (int)cluster.block_rank();
   const int plane = blockIdx.x / CS;  // z + N*c
-  const double2* Jr = J + blockIdx.y * js;
+  const IO* Jr = J + blockIdx.y * js;
   for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
   for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
   cluster.sync();  // every CTA of the cluster runs before remote stores; twiddles staged
@@ -92,16 +92,7 @@ k_xyfwd(const double2* __restrict__ J, long long js, const int* __restrict__ inv
           kk[b * R0 + r] = (valid && r < R0 / 2 && p < L) ? invr[p] : -1;
         }
 #pragma unroll
-      for (int i = 0; i < E; ++i) {
-        V val = mk<V>(0, 0);
-        if (kk[i] >= 0) {
-          double2 jv = Jr[kk[i]];
-          if (pro.conjin) jv.y = -jv.y;
-          if (pro.pre) jv = cmul(pro.pre[kk[i]], jv);
-          val = cvt<V>(jv);
-        }
-        reg[i] = val;
-      }
+      for (int i = 0; i < E; ++i) reg[i] = kk[i] >= 0 ? cvt<V>(prologue_in(Jr, pro, kk[i])) : mk<V>(0, 0);
       FX::run_half(reg, xb + s * C::ROWP, SAddr(1, true), t, twx_s);
       if (valid) {
 #pragma unroll
@@ -147,11 +138,11 @@ k_xyfwd(const double2* __restrict__ J, long long js, const int* __restrict__ inv
   }
 }
 
-template <typename T, int NL, int NM, int CS, bool NARROW>
+template <typename T, int NL, int NM, int CS, bool NARROW, typename IO>
 __global__ void __launch_bounds__(256, (XYCfg<T, NL, NM, CS, NARROW>::FXI::E <= 16 &&
                                         XYCfg<T, NL, NM, CS, NARROW>::FYI::E <= 16) ? 3 : 1)
-k_yxinv(const cplx<T>* __restrict__ B, long long bs, const double2* __restrict__ J, long long js,
-        const int* __restrict__ inv, Epilogue ep, double2* __restrict__ out, long long os, Dims d,
+k_yxinv(const cplx<T>* __restrict__ B, long long bs, const IO* __restrict__ J, long long js,
+        const int* __restrict__ inv, Epilogue ep, IO* __restrict__ out, long long os, Dims d,
         const cplx<T>* __restrict__ twx, const cplx<T>* __restrict__ twy) {
   if (rhs_skipped(d, blockIdx.y)) return;  // uniform over the cluster
   using C = XYCfg<T, NL, NM, CS, NARROW>;
@@ -206,8 +197,8 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const double2* __restrict__
   {
     constexpr int E = FXI::E, RL = FXI::RL;
     const int t = threadIdx.x % FXI::T, s = threadIdx.x / FXI::T;
-    const double2* Jr = J + blockIdx.y * js;
-    double2* outr = out + blockIdx.y * os;
+    const IO* Jr = J + blockIdx.y * js;
+    IO* outr = out + blockIdx.y * os;
     for (int row0 = 0; row0 < C::RYP; row0 += C::SX) {
       const int yl = row0 + s;
       const bool valid = yl < C::RY;
@@ -232,28 +223,28 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const double2* __restrict__
           constexpr int EPI = 2;
 #pragma unroll
           for (int i0 = 0; i0 < E; i0 += EPI) {
-            double2 jv[EPI], ak[EPI], bk[EPI];
+            IO jv[EPI], ak[EPI], bk[EPI];
 #pragma unroll
             for (int j = 0; j < EPI; ++j) {
               const int k = kk[i0 + j];
               if (k < 0) continue;
               jv[j] = Jr[k];
-              ak[j] = ep.a ? ep.a[k] : ep.a_s;
-              bk[j] = ep.b ? ep.b[k] : ep.b_s;
+              ak[j] = EpiIO<IO>::a(ep, k);
+              bk[j] = EpiIO<IO>::b(ep, k);
             }
 #pragma unroll
             for (int j = 0; j < EPI; ++j) {
               const int k = kk[i0 + j];
               if (k < 0) continue;
-              // the diagonal Gram*Mr*J term in FP64; the circulant term in the
-              // transform's precision
-              double2 res = cmul(ak[j], jv[j]);
+              // the diagonal Gram*Mr*J term in the vectors' precision; the
+              // circulant term in the transform's precision
+              IO res = cmul(ak[j], jv[j]);
               if (ep.conjout) {
-                const double2 v = cvt<double2>(reg[i0 + j]);
+                const IO v = cvt<IO>(reg[i0 + j]);
                 res.x -= v.x;
                 res.y += v.y;
               } else {
-                res = csub(res, cvt<double2>(cmul(cvt<V>(bk[j]), reg[i0 + j])));
+                res = csub(res, cvt<IO>(cmul(cvt<V>(bk[j]), reg[i0 + j])));
               }
               outr[k] = res;
             }
@@ -268,16 +259,14 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const double2* __restrict__
               if (x >= L) continue;
               const int k = invr[x];
               if (k < 0) continue;
-              const double2 jv = Jr[k];
-              const double2 A_k = ep.a ? ep.a[k] : ep.a_s;
-              double2 res = cmul(A_k, jv);
+              const IO jv = Jr[k];
+              IO res = cmul(EpiIO<IO>::a(ep, k), jv);
               if (ep.conjout) {
-                const double2 v = cvt<double2>(reg[b * RL + r]);
+                const IO v = cvt<IO>(reg[b * RL + r]);
                 res.x -= v.x;
                 res.y += v.y;
               } else {
-                const double2 B_k = ep.b ? ep.b[k] : ep.b_s;
-                res = csub(res, cvt<double2>(cmul(cvt<V>(B_k), reg[b * RL + r])));
+                res = csub(res, cvt<IO>(cmul(cvt<V>(EpiIO<IO>::b(ep, k)), reg[b * RL + r])));
               }
               outr[k] = res;
             }

@@ -9,28 +9,28 @@ namespace marie {
 template <typename T> struct MatvecImpl {
   using V = cplx<T>;
 
-  template <int NL>
-  static cudaError_t xfwd_n(const double2* J, long long js, const int* inv, Prologue pro, V* A, long long as,
+  template <int NL, typename IO>
+  static cudaError_t xfwd_n(const IO* J, long long js, const int* inv, Prologue pro, V* A, long long as,
                             const Dims& d, const V* tw, int nrhs, cudaStream_t st) {
     constexpr int S = RowCfg<cplx<T>, NL>::S;
     const size_t smem = (size_t)(NL + NL * (S + 1)) * sizeof(V);
-    cudaError_t e = opt_in_smem(k_xfwd<T, NL>, smem);
+    cudaError_t e = opt_in_smem(k_xfwd<T, NL, IO>, smem);
     if (e != cudaSuccess) return e;
     const int rows = d.M * d.N * 3;
     dim3 grid((rows + S - 1) / S, nrhs);
-    k_xfwd<T, NL><<<grid, RowCfg<cplx<T>, NL>::THREADS, smem, st>>>(J, js, inv, pro, A, as, d, tw);
+    k_xfwd<T, NL, IO><<<grid, RowCfg<cplx<T>, NL>::THREADS, smem, st>>>(J, js, inv, pro, A, as, d, tw);
     return cudaGetLastError();
   }
-  template <int NL>
-  static cudaError_t xinv_n(const V* A, long long as, const double2* J, long long js, const int* inv, Epilogue ep,
-                            double2* out, long long os, const Dims& d, const V* tw, int nrhs, cudaStream_t st) {
+  template <int NL, typename IO>
+  static cudaError_t xinv_n(const V* A, long long as, const IO* J, long long js, const int* inv, Epilogue ep,
+                            IO* out, long long os, const Dims& d, const V* tw, int nrhs, cudaStream_t st) {
     constexpr int S = RowCfg<cplx<T>, NL>::S;
     const size_t smem = (size_t)(NL + NL * (S + 1)) * sizeof(V);
-    cudaError_t e = opt_in_smem(k_xinv<T, NL>, smem);
+    cudaError_t e = opt_in_smem(k_xinv<T, NL, IO>, smem);
     if (e != cudaSuccess) return e;
     const int rows = d.M * d.N * 3;
     dim3 grid((rows + S - 1) / S, nrhs);
-    k_xinv<T, NL><<<grid, RowCfg<cplx<T>, NL>::THREADS, smem, st>>>(A, as, J, js, inv, ep, out, os, d, tw);
+    k_xinv<T, NL, IO><<<grid, RowCfg<cplx<T>, NL>::THREADS, smem, st>>>(A, as, J, js, inv, ep, out, os, d, tw);
     return cudaGetLastError();
   }
   template <int NC, bool INV>
@@ -70,19 +70,21 @@ template <typename T> struct MatvecImpl {
     return zmul_nk<NZ, 0, 0>(B, bs, fN, oct, d, tw, nrhs, st);
   }
 
-  static cudaError_t xfwd(const double2* J, long long js, const int* inv, Prologue pro, V* A, long long as,
+  template <typename IO>
+  static cudaError_t xfwd(const IO* J, long long js, const int* inv, Prologue pro, V* A, long long as,
                           const Dims& d, const V* tw, int nrhs, cudaStream_t st) {
     switch (d.Lp) {
-#define MARIE_CASE(n_) case n_: return xfwd_n<n_>(J, js, inv, pro, A, as, d, tw, nrhs, st);
+#define MARIE_CASE(n_) case n_: return xfwd_n<n_, IO>(J, js, inv, pro, A, as, d, tw, nrhs, st);
       MARIE_FFT_LENGTHS(MARIE_CASE)
 #undef MARIE_CASE
     }
     return cudaErrorInvalidValue;
   }
-  static cudaError_t xinv(const V* A, long long as, const double2* J, long long js, const int* inv, Epilogue ep,
-                          double2* out, long long os, const Dims& d, const V* tw, int nrhs, cudaStream_t st) {
+  template <typename IO>
+  static cudaError_t xinv(const V* A, long long as, const IO* J, long long js, const int* inv, Epilogue ep,
+                          IO* out, long long os, const Dims& d, const V* tw, int nrhs, cudaStream_t st) {
     switch (d.Lp) {
-#define MARIE_CASE(n_) case n_: return xinv_n<n_>(A, as, J, js, inv, ep, out, os, d, tw, nrhs, st);
+#define MARIE_CASE(n_) case n_: return xinv_n<n_, IO>(A, as, J, js, inv, ep, out, os, d, tw, nrhs, st);
       MARIE_FFT_LENGTHS(MARIE_CASE)
 #undef MARIE_CASE
     }
@@ -149,51 +151,51 @@ template <typename T> struct FusedImpl {
     cfg.numAttrs = 1;
     return cudaLaunchKernelExC(&cfg, (const void*)kern, args);
   }
-  template <int NL, int NM, int CS, bool NARROW>
-  static cudaError_t xyfwd_nv(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
+  template <int NL, int NM, int CS, bool NARROW, typename IO>
+  static cudaError_t xyfwd_nv(const IO* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
                               Dims d, const V* twx, const V* twy, int nrhs, cudaStream_t st) {
     void* args[] = {(void*)&J, (void*)&js, (void*)&inv, (void*)&pro, (void*)&B, (void*)&bs, (void*)&d,
                     (void*)&twx, (void*)&twy};
-    return launch(k_xyfwd<T, NL, NM, CS, NARROW>, CS, CS * 3 * d.N, nrhs, XYCfg<T, NL, NM, CS, NARROW>::fwd_smem, st,
-                  args);
+    return launch(k_xyfwd<T, NL, NM, CS, NARROW, IO>, CS, CS * 3 * d.N, nrhs, XYCfg<T, NL, NM, CS, NARROW>::fwd_smem,
+                  st, args);
   }
-  template <int NL, int NM, int CS, bool NARROW>
-  static cudaError_t yxinv_nv(const V* B, long long bs, const double2* J, long long js, const int* inv, Epilogue ep,
-                              double2* out, long long os, Dims d, const V* twx, const V* twy, int nrhs,
+  template <int NL, int NM, int CS, bool NARROW, typename IO>
+  static cudaError_t yxinv_nv(const V* B, long long bs, const IO* J, long long js, const int* inv, Epilogue ep,
+                              IO* out, long long os, Dims d, const V* twx, const V* twy, int nrhs,
                               cudaStream_t st) {
     void* args[] = {(void*)&B, (void*)&bs, (void*)&J, (void*)&js, (void*)&inv, (void*)&ep, (void*)&out,
                     (void*)&os, (void*)&d, (void*)&twx, (void*)&twy};
-    return launch(k_yxinv<T, NL, NM, CS, NARROW>, CS, CS * 3 * d.N, nrhs, XYCfg<T, NL, NM, CS, NARROW>::inv_smem, st,
-                  args);
+    return launch(k_yxinv<T, NL, NM, CS, NARROW, IO>, CS, CS * 3 * d.N, nrhs, XYCfg<T, NL, NM, CS, NARROW>::inv_smem,
+                  st, args);
   }
   // a narrow variant exists where either transform has a wide schedule
   template <int NL, int NM> static constexpr bool has_narrow() {
     return sizeof(T) == 4 && (HasWide<NL>::value || HasWide<NM>::value);
   }
-  template <int NL, int NM, int CS>
-  static cudaError_t xyfwd_n(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
+  template <int NL, int NM, int CS, typename IO>
+  static cudaError_t xyfwd_n(const IO* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
                              Dims d, const V* twx, const V* twy, int nrhs, cudaStream_t st, int fvar) {
     if constexpr (usable<NL, NM, CS>()) {
       if constexpr (has_narrow<NL, NM>())
-        if (fvar == 1) return xyfwd_nv<NL, NM, CS, true>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
+        if (fvar == 1) return xyfwd_nv<NL, NM, CS, true, IO>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
       if constexpr (CS >= 4 && usable<NL, NM, CS / 2>())
-        if (fvar == 2) return xyfwd_nv<NL, NM, CS / 2, false>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
-      return xyfwd_nv<NL, NM, CS, false>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
+        if (fvar == 2) return xyfwd_nv<NL, NM, CS / 2, false, IO>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
+      return xyfwd_nv<NL, NM, CS, false, IO>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st);
     } else {
       return cudaErrorNotSupported;
     }
   }
-  template <int NL, int NM, int CS>
-  static cudaError_t yxinv_n(const V* B, long long bs, const double2* J, long long js, const int* inv, Epilogue ep,
-                             double2* out, long long os, Dims d, const V* twx, const V* twy, int nrhs,
+  template <int NL, int NM, int CS, typename IO>
+  static cudaError_t yxinv_n(const V* B, long long bs, const IO* J, long long js, const int* inv, Epilogue ep,
+                             IO* out, long long os, Dims d, const V* twx, const V* twy, int nrhs,
                              cudaStream_t st, int fvar) {
     if constexpr (usable<NL, NM, CS>()) {
       if constexpr (has_narrow<NL, NM>())
-        if (fvar == 1) return yxinv_nv<NL, NM, CS, true>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
+        if (fvar == 1) return yxinv_nv<NL, NM, CS, true, IO>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
       if constexpr (CS >= 4 && usable<NL, NM, CS / 2>())
         if (fvar == 2)
-          return yxinv_nv<NL, NM, CS / 2, false>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
-      return yxinv_nv<NL, NM, CS, false>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
+          return yxinv_nv<NL, NM, CS / 2, false, IO>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
+      return yxinv_nv<NL, NM, CS, false, IO>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st);
     } else {
       return cudaErrorNotSupported;
     }
@@ -208,37 +210,42 @@ template <typename T> bool MatvecLaunch<T>::fused(const Dims& d) {
   return false;
 }
 template <typename T>
-cudaError_t MatvecLaunch<T>::xyfwd(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
+template <typename IO>
+cudaError_t MatvecLaunch<T>::xyfwd(const IO* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
                                    const Dims& d, const V* twx, const V* twy, int nrhs, cudaStream_t st, int fvar) {
 #define MARIE_CASE(a_, b_, c_)    \
   if (d.Lp == a_ && d.Mp == b_) \
-    return FusedImpl<T>::template xyfwd_n<a_, b_, c_>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st, fvar);
+    return FusedImpl<T>::template xyfwd_n<a_, b_, c_, IO>(J, js, inv, pro, B, bs, d, twx, twy, nrhs, st, fvar);
   MARIE_FUSED_PAIRS(MARIE_CASE)
 #undef MARIE_CASE
   return cudaErrorNotSupported;
 }
 template <typename T>
-cudaError_t MatvecLaunch<T>::yxinv(const V* B, long long bs, const double2* J, long long js, const int* inv,
-                                   Epilogue ep, double2* out, long long os, const Dims& d, const V* twx, const V* twy,
+template <typename IO>
+cudaError_t MatvecLaunch<T>::yxinv(const V* B, long long bs, const IO* J, long long js, const int* inv,
+                                   Epilogue ep, IO* out, long long os, const Dims& d, const V* twx, const V* twy,
                                    int nrhs, cudaStream_t st, int fvar) {
 #define MARIE_CASE(a_, b_, c_)    \
   if (d.Lp == a_ && d.Mp == b_) \
-    return FusedImpl<T>::template yxinv_n<a_, b_, c_>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st, fvar);
+    return FusedImpl<T>::template yxinv_n<a_, b_, c_, IO>(B, bs, J, js, inv, ep, out, os, d, twx, twy, nrhs, st, \
+                                                          fvar);
   MARIE_FUSED_PAIRS(MARIE_CASE)
 #undef MARIE_CASE
   return cudaErrorNotSupported;
 }
 
 template <typename T>
-cudaError_t MatvecLaunch<T>::xfwd(const double2* J, long long js, const int* inv, Prologue pro, V* A, long long as,
+template <typename IO>
+cudaError_t MatvecLaunch<T>::xfwd(const IO* J, long long js, const int* inv, Prologue pro, V* A, long long as,
                                   const Dims& d, const V* tw, int nrhs, cudaStream_t st) {
-  return MatvecImpl<T>::xfwd(J, js, inv, pro, A, as, d, tw, nrhs, st);
+  return MatvecImpl<T>::template xfwd<IO>(J, js, inv, pro, A, as, d, tw, nrhs, st);
 }
 template <typename T>
-cudaError_t MatvecLaunch<T>::xinv(const V* A, long long as, const double2* J, long long js, const int* inv,
-                                  Epilogue ep, double2* out, long long os, const Dims& d, const V* tw, int nrhs,
+template <typename IO>
+cudaError_t MatvecLaunch<T>::xinv(const V* A, long long as, const IO* J, long long js, const int* inv,
+                                  Epilogue ep, IO* out, long long os, const Dims& d, const V* tw, int nrhs,
                                   cudaStream_t st) {
-  return MatvecImpl<T>::xinv(A, as, J, js, inv, ep, out, os, d, tw, nrhs, st);
+  return MatvecImpl<T>::template xinv<IO>(A, as, J, js, inv, ep, out, os, d, tw, nrhs, st);
 }
 template <typename T>
 cudaError_t MatvecLaunch<T>::cols(bool inv, int NC, const V* in, long long in_w, long long in_rhs, int n_in, V* out,

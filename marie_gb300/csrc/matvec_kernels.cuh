@@ -39,12 +39,40 @@ struct Epilogue {
   const double2* b;  // per-DOF, or null -> b_s
   double2 a_s, b_s;
   int conjout;
+  // FP32 copies of a and b for matvecs on FP32 vectors (IO = float2)
+  const float2* af;
+  const float2* bf;
 };
 // Prologue: x_in[k] = (pre ? pre[k] : 1) * (conjin ? conj(J[k]) : J[k])
 struct Prologue {
   const double2* pre;
   int conjin;
 };
+
+// The matvec's input and output vectors are FP64 (IO = double2) or, for the
+// inner solves of mixed-precision refinement, FP32 (IO = float2); the
+// epilogue then runs in that precision with the FP32 coefficient copies.
+template <typename IO> struct EpiIO;
+template <> struct EpiIO<double2> {
+  __device__ __forceinline__ static double2 a(const Epilogue& ep, int k) { return ep.a ? ep.a[k] : ep.a_s; }
+  __device__ __forceinline__ static double2 b(const Epilogue& ep, int k) { return ep.b ? ep.b[k] : ep.b_s; }
+};
+template <> struct EpiIO<float2> {
+  __device__ __forceinline__ static float2 a(const Epilogue& ep, int k) {
+    return ep.af ? ep.af[k] : cvt<float2>(ep.a_s);
+  }
+  __device__ __forceinline__ static float2 b(const Epilogue& ep, int k) {
+    return ep.bf ? ep.bf[k] : cvt<float2>(ep.b_s);
+  }
+};
+// J[k] with the prologue applied, in the precision of IO
+template <typename IO>
+__device__ __forceinline__ IO prologue_in(const IO* __restrict__ J, const Prologue& pro, int k) {
+  IO jv = J[k];
+  if (pro.conjin) jv.y = -jv.y;
+  if (pro.pre) jv = cmul(cvt<IO>(pro.pre[k]), jv);
+  return jv;
+}
 
 template <typename V, int N> struct RowCfg {
   static constexpr int T = FFT<V, N, false>::T;
@@ -61,9 +89,9 @@ __device__ __forceinline__ void stage_twiddles(V* tw_s, const V* __restrict__ tw
 // ---------------------------------------------------------------------------
 // xfwd: gather + forward x transform.  grid.x = ceil(rows / S), grid.y = rhs
 // ---------------------------------------------------------------------------
-template <typename T, int NL>
+template <typename T, int NL, typename IO>
 __global__ void __launch_bounds__(RowCfg<cplx<T>, NL>::THREADS)
-k_xfwd(const double2* __restrict__ J, long long j_stride, const int* __restrict__ inv, Prologue pro,
+k_xfwd(const IO* __restrict__ J, long long j_stride, const int* __restrict__ inv, Prologue pro,
        cplx<T>* __restrict__ A, long long a_stride, Dims d, const cplx<T>* __restrict__ tw) {
   using V = cplx<T>;
   using F = FFT<V, NL, false>;
@@ -75,8 +103,7 @@ k_xfwd(const double2* __restrict__ J, long long j_stride, const int* __restrict_
   if (rhs_skipped(d, blockIdx.y)) return;
   const int rows = d.M * d.N * 3;
   const int row0 = blockIdx.x * S;
-  const double2* Jr = J + blockIdx.y * j_stride;
-  const double2* prer = pro.pre;  // prologue coefficients are shared by all rhs
+  const IO* Jr = J + blockIdx.y * j_stride;
   stage_twiddles(tw_s, tw, NL);
   // gather: x fastest across threads
   for (int i = threadIdx.x; i < S * d.L; i += blockDim.x) {
@@ -86,12 +113,7 @@ k_xfwd(const double2* __restrict__ J, long long j_stride, const int* __restrict_
     if (row < rows) {
       const long long g3 = (long long)row * d.L + x;  // row = y + M*(z + N*c)
       const int k = inv[g3];
-      if (k >= 0) {
-        double2 jv = Jr[k];
-        if (pro.conjin) jv.y = -jv.y;
-        if (prer) jv = cmul(prer[k], jv);
-        val = cvt<V>(jv);
-      }
+      if (k >= 0) val = cvt<V>(prologue_in(Jr, pro, k));
     }
     buf[x * ES + s] = val;
   }
@@ -114,10 +136,10 @@ k_xfwd(const double2* __restrict__ J, long long j_stride, const int* __restrict_
 // ---------------------------------------------------------------------------
 // xinv: inverse x transform + crop + epilogue + scatter to DOFs.
 // ---------------------------------------------------------------------------
-template <typename T, int NL>
+template <typename T, int NL, typename IO>
 __global__ void __launch_bounds__(RowCfg<cplx<T>, NL>::THREADS)
-k_xinv(const cplx<T>* __restrict__ A, long long a_stride, const double2* __restrict__ J, long long j_stride,
-       const int* __restrict__ inv, Epilogue ep, double2* __restrict__ out, long long o_stride, Dims d,
+k_xinv(const cplx<T>* __restrict__ A, long long a_stride, const IO* __restrict__ J, long long j_stride,
+       const int* __restrict__ inv, Epilogue ep, IO* __restrict__ out, long long o_stride, Dims d,
        const cplx<T>* __restrict__ tw) {
   using V = cplx<T>;
   using F = FFT<V, NL, true>;
@@ -144,8 +166,8 @@ k_xinv(const cplx<T>* __restrict__ A, long long a_stride, const double2* __restr
   __syncthreads();
   F::store(reg, buf + s, ES, t);
   __syncthreads();
-  const double2* Jr = J + blockIdx.y * j_stride;
-  double2* outr = out + blockIdx.y * o_stride;
+  const IO* Jr = J + blockIdx.y * j_stride;
+  IO* outr = out + blockIdx.y * o_stride;
   for (int i = threadIdx.x; i < S * d.L; i += blockDim.x) {
     const int ss = i / d.L, x = i - ss * d.L;
     const int row = row0 + ss;
@@ -153,16 +175,14 @@ k_xinv(const cplx<T>* __restrict__ A, long long a_stride, const double2* __restr
     const long long g3 = (long long)row * d.L + x;
     const int k = inv[g3];
     if (k < 0) continue;
-    const double2 v = cvt<double2>(buf[x * ES + ss]);
-    const double2 jv = Jr[k];
-    const double2 A_k = ep.a ? ep.a[k] : ep.a_s;
-    double2 r = cmul(A_k, jv);
+    const IO v = cvt<IO>(buf[x * ES + ss]);
+    const IO jv = Jr[k];
+    IO r = cmul(EpiIO<IO>::a(ep, k), jv);
     if (ep.conjout) {
       r.x -= v.x;
       r.y += v.y;
     } else {
-      const double2 B_k = ep.b ? ep.b[k] : ep.b_s;
-      r = csub(r, cmul(B_k, v));
+      r = csub(r, cmul(EpiIO<IO>::b(ep, k), v));
     }
     outr[k] = r;
   }

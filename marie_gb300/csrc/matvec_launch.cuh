@@ -26,12 +26,16 @@ template <typename K> inline cudaError_t opt_in_smem(K kernel, size_t bytes) {
   return e;
 }
 
+// IO: the type of the matvec's input and output vectors (double2, or float2
+// for FP32 arithmetic T = float)
 template <typename T> struct MatvecLaunch {
   using V = cplx<T>;
-  static cudaError_t xfwd(const double2* J, long long js, const int* inv, Prologue pro, V* A, long long as,
+  template <typename IO>
+  static cudaError_t xfwd(const IO* J, long long js, const int* inv, Prologue pro, V* A, long long as,
                           const Dims& d, const V* tw, int nrhs, cudaStream_t st);
-  static cudaError_t xinv(const V* A, long long as, const double2* J, long long js, const int* inv, Epilogue ep,
-                          double2* out, long long os, const Dims& d, const V* tw, int nrhs, cudaStream_t st);
+  template <typename IO>
+  static cudaError_t xinv(const V* A, long long as, const IO* J, long long js, const int* inv, Epilogue ep,
+                          IO* out, long long os, const Dims& d, const V* tw, int nrhs, cudaStream_t st);
   static cudaError_t cols(bool inv, int NC, const V* in, long long in_w, long long in_rhs, int n_in, V* out,
                           long long out_w, long long out_rhs, int n_out, int Lp, int nw, const V* tw, int nrhs,
                           cudaStream_t st, const int* stop = nullptr, int step = 0);
@@ -42,10 +46,12 @@ template <typename T> struct MatvecLaunch {
   // fused x+y passes (thread-block clusters); fused() says whether this grid has them
   static bool fused(const Dims& d);
   // fvar: 0 the default x/y radix schedules, 1 the narrow (radix-8) ones
-  static cudaError_t xyfwd(const double2* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
+  template <typename IO>
+  static cudaError_t xyfwd(const IO* J, long long js, const int* inv, Prologue pro, V* B, long long bs,
                            const Dims& d, const V* twx, const V* twy, int nrhs, cudaStream_t st, int fvar = 0);
-  static cudaError_t yxinv(const V* B, long long bs, const double2* J, long long js, const int* inv, Epilogue ep,
-                           double2* out, long long os, const Dims& d, const V* twx, const V* twy, int nrhs,
+  template <typename IO>
+  static cudaError_t yxinv(const V* B, long long bs, const IO* J, long long js, const int* inv, Epilogue ep,
+                           IO* out, long long os, const Dims& d, const V* twx, const V* twy, int nrhs,
                            cudaStream_t st, int fvar = 0);
 };
 

@@ -116,6 +116,10 @@ int run_matvec(marie_plan* p, int prec, const double2* J, double2* out, long lon
 int run_matvec(marie_plan* p, int prec, const double2* J, long long js, double2* out, long long os, long long n,
                int nrhs, const int* inv, const Prologue& pro, const Epilogue& ep, const int* stop, int step,
                int kind = 0);
+// FP32 matvec on FP32 vectors (FP32 arithmetic throughout, the epilogue's
+// per-DOF coefficients from ep.af / ep.bf).
+int run_matvec32(marie_plan* p, const float2* J, long long js, float2* out, long long os, long long n, int nrhs,
+                 const int* inv, const Prologue& pro, const Epilogue& ep, const int* stop, int step, int kind = 0);
 
 // Scale fN by 1/(8LMN) into the plan's FP64/FP32 copies (fN_dev: full layout).
 // kind 0: the N operator (6 components), 1: the K operator (3 components).
@@ -147,6 +151,10 @@ struct GmresResult {
 struct BatchOp {
   std::function<int(const double2* in, long long is, double2* out, long long os, int S, const int* stop, int step)>
       apply;
+  // the same operator on FP32 vectors in FP32 arithmetic (set on plans with an
+  // FP32 operator; used by GMRES with an FP32 Krylov basis)
+  std::function<int(const float2* in, long long is, float2* out, long long os, int S, const int* stop, int step)>
+      apply32;
 };
 
 // pgmres semantics for S systems sharing one operator, device-driven (one
