@@ -31,6 +31,10 @@
 namespace marie {
 
 static constexpr int BG = 152 * 2;  // row blocks per system for the reductions
+// row blocks of the dots and the update with an FP32 basis: these stream the
+// basis at HBM speed rather than at the FP64 rate, so they want more loads in
+// flight (four blocks per SM)
+static constexpr int BG32 = 152 * 4;
 static constexpr int BT = 256;
 
 __device__ __forceinline__ double2 wsum2(double2 v) {
@@ -111,6 +115,23 @@ __global__ void kb_cycle_init(const double2* __restrict__ r, long long rs, VB* _
     v[i] = cvt<VB>(mk<double2>(x[i].x * inv, x[i].y * inv));
 }
 
+// The block that finishes last (counted in cnt[s], reset by that block) runs
+// the reduction over the blocks' partials: the usual fence-then-count
+// pattern, no waiting.  The final sums have a fixed order whichever block
+// runs them.
+__device__ __forceinline__ bool last_block(unsigned* cnt) {
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (is_last) {
+    __threadfence();
+    if (threadIdx.x == 0) *cnt = 0;
+  }
+  return is_last;
+}
+
 // One sweep over NC basis columns c0..c0+NC-1: the block's partial sums of
 // conj(V(:,j)) w, reduced in the block (warp sums, then warp partials in warp
 // order by one thread per column: a fixed order).  NC is a template argument
@@ -123,6 +144,7 @@ __device__ __forceinline__ void kb_dot_sweep(const VB* __restrict__ V, const VB*
   VB acc[NC];
 #pragma unroll
   for (int q = 0; q < NC; ++q) acc[q] = mk<VB>(0, 0);
+#pragma unroll 4
   for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
     const VB wv = w[i];
 #pragma unroll
@@ -147,10 +169,12 @@ __device__ __forceinline__ void kb_dot_sweep(const VB* __restrict__ V, const VB*
   __syncthreads();  // red is reused by the next sweep
 }
 
-// partial[s][j][b] = sum over block rows of conj(V_s(:,j)) w_s, j < k, w_s = V_s(:,k)
+// partial[s][j][b] = sum over block rows of conj(V_s(:,j)) w_s, j < k, w_s = V_s(:,k);
+// h[s][j] = sum_b partial[s][j][b]
 template <typename VB>
 __global__ void __launch_bounds__(BT) kb_dots(const VB* __restrict__ Vb, long long vs, long long n, int k,
-                                              const int* __restrict__ stop, double2* __restrict__ part) {
+                                              const int* __restrict__ stop, double2* __restrict__ part,
+                                              unsigned* __restrict__ cnt, double2* __restrict__ h, int hld) {
   const int s = blockIdx.y;
   if (skip(stop, s, k)) return;
   const VB* V = Vb + s * vs;
@@ -171,49 +195,17 @@ __global__ void __launch_bounds__(BT) kb_dots(const VB* __restrict__ Vb, long lo
     case 7: kb_dot_sweep<7>(V, w, n, i0, i1, c0, part_s, red); break;
     default: break;
   }
-}
-
-// h[s][j] = sum_b part[s][j][b]  (grid k x S, one warp each)
-__global__ void kb_dots_fin(const double2* __restrict__ part, int G, int k, const int* __restrict__ stop,
-                            double2* __restrict__ h, int hld) {
-  const int j = blockIdx.x, s = blockIdx.y;
-  if (skip(stop, s, k)) return;
-  double2 a = mk<double2>(0, 0);
-  for (int b = threadIdx.x; b < G; b += 32) a = cadd(a, part[((long long)s * 128 + j) * G + b]);
-  a = wsum2(a);
-  if (threadIdx.x == 0) h[(long long)s * hld + j] = a;
-}
-
-// w_s -= V_s(:,0:k) h_s with w_s = V_s(:,k) ; partial norms of the new w_s
-template <typename VB>
-__global__ void __launch_bounds__(BT) kb_update(VB* __restrict__ Vb, long long vs, long long n, int k,
-                                                const double2* __restrict__ h, int hld,
-                                                const int* __restrict__ stop, double* __restrict__ part) {
-  using R = decltype(VB::x);
-  const int s = blockIdx.y;
-  if (skip(stop, s, k)) return;
-  __shared__ VB hs[128];
-  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = cvt<VB>(h[(long long)s * hld + j]);
-  __syncthreads();
-  VB* V = Vb + s * vs;
-  VB* w = V + (long long)k * n;
-  long long i0, i1;
-  rows_of(n, i0, i1);
-  R a = 0;
-  for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    VB v = w[i];
-    for (int j = 0; j < k; ++j) {
-      const VB b = V[(long long)j * n + i];
-      const VB c = hs[j];
-      v.x = fmaT(-b.x, c.x, fmaT(b.y, c.y, v.x));
-      v.y = fmaT(-b.x, c.y, fmaT(-b.y, c.x, v.y));
-    }
-    w[i] = v;
-    a = fmaT(v.x, v.x, fmaT(v.y, v.y, a));
+  // h[s][j] = sum_b part[s][j][b] by the last block, one warp per column
+  if (!last_block(cnt + s)) return;
+  const int G = gridDim.x, lane = threadIdx.x & 31;
+  for (int j = threadIdx.x >> 5; j < k; j += BT / 32) {
+    double2 a = mk<double2>(0, 0);
+    for (int b = lane; b < G; b += 32) a = cadd(a, __ldcg(part_s + (long long)j * G + b));
+    a = wsum2(a);
+    if (lane == 0) h[(long long)s * hld + j] = a;
   }
-  const double2 r = bsum2(mk<double2>((double)a, 0));
-  if (threadIdx.x == 0) part[(long long)s * gridDim.x + blockIdx.x] = r.x;
 }
+
 
 struct GState {
   double2* H;    // [S][(m+1)*m] unrotated, column-major
@@ -241,10 +233,9 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
 // per-step stop test needs no solve; y = R \ g and the explicit residual
 // res = rhs - Hc y (which restarts the next cycle as V*res) are formed once,
 // at the step that ends the cycle.
-__global__ void kb_givens(GState G, int m, int k, const double2* __restrict__ h, int hld,
-                          const double* __restrict__ npart, int NB) {
-  const int s = blockIdx.x;
-  const int lane = threadIdx.x;
+// Run by one full warp (lane = 0..31) for system s.
+__device__ void givens_warp(const GState& G, int m, int k, const double2* __restrict__ h, int hld,
+                            const double* __restrict__ npart, int NB, int s, int lane) {
   if (G.stop[s] < k) return;
   const int ld = m + 1;
   double2* H = G.H + (long long)s * ld * m;
@@ -258,7 +249,7 @@ __global__ void kb_givens(GState G, int m, int k, const double2* __restrict__ h,
   __shared__ double cs_s[128];
   const int kk = k - 1;
   double nn = 0;
-  for (int b = lane; b < NB; b += 32) nn += npart[(long long)s * NB + b];
+  for (int b = lane; b < NB; b += 32) nn += __ldcg(npart + (long long)s * NB + b);
   nn = wsum(nn);
   const double hnv = sqrt(nn);
   for (int i = lane; i < k; i += 32) {
@@ -331,6 +322,42 @@ __global__ void kb_givens(GState G, int m, int k, const double2* __restrict__ h,
   }
   if (lane == 0) G.stop[s] = k;
 }
+// w_s -= V_s(:,0:k) h_s with w_s = V_s(:,k) ; partial norms of the new w_s,
+// then the Givens step of the system (givens_warp) by the last block
+template <typename VB>
+__global__ void __launch_bounds__(BT) kb_update(VB* __restrict__ Vb, long long vs, long long n, int k,
+                                                const double2* __restrict__ h, int hld,
+                                                const int* __restrict__ stop, double* __restrict__ part,
+                                                unsigned* __restrict__ cnt, GState G, int m) {
+  using R = decltype(VB::x);
+  const int s = blockIdx.y;
+  if (skip(stop, s, k)) return;
+  __shared__ VB hs[128];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = cvt<VB>(h[(long long)s * hld + j]);
+  __syncthreads();
+  VB* V = Vb + s * vs;
+  VB* w = V + (long long)k * n;
+  long long i0, i1;
+  rows_of(n, i0, i1);
+  R a = 0;
+  for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    VB v = w[i];
+#pragma unroll 8
+    for (int j = 0; j < k; ++j) {
+      const VB b = V[(long long)j * n + i];
+      const VB c = hs[j];
+      v.x = fmaT(-b.x, c.x, fmaT(b.y, c.y, v.x));
+      v.y = fmaT(-b.x, c.y, fmaT(-b.y, c.x, v.y));
+    }
+    w[i] = v;
+    a = fmaT(v.x, v.x, fmaT(v.y, v.y, a));
+  }
+  const double2 r = bsum2(mk<double2>((double)a, 0));
+  if (threadIdx.x == 0) part[(long long)s * gridDim.x + blockIdx.x] = r.x;
+  if (!last_block(cnt + s)) return;
+  if (threadIdx.x < 32) givens_warp(G, m, k, h, hld, part, gridDim.x, s, threadIdx.x);
+}
+
 
 // V_s(:,k) /= H(k+1,k)  (zero norm leaves a zero column instead of 0/0)
 template <typename VB>
@@ -404,7 +431,9 @@ struct BatchWork {
   int S = 0, m = 0;
   long long n = 0;
   bool f32 = false;  // FP32 basis (t1f, t2f: FP32 work vectors of the preconditioner chains)
+  int bg = BG;       // row blocks of kb_dots / kb_update
   DBuf V, t1, t2, t1f, t2f, r, part_d, part_n, h, H, R, g, cs, sn, y, res, resv, beta, tol, hn, stop, norms;
+  DBuf cnt;  // [2][S] last-block counters of kb_dots and kb_update (zero between launches)
   GState gs{};
   cudaGraphExec_t exec = nullptr;
   long long graph_nodes = 0;
@@ -423,8 +452,9 @@ struct BatchWork {
     }
     MARIE_TRY(t1.alloc((size_t)S * n * sizeof(double2), st));
     MARIE_TRY(t2.alloc((size_t)S * n * sizeof(double2), st));
-    MARIE_TRY(part_d.alloc((size_t)S * 128 * BG * sizeof(double2), st));
-    MARIE_TRY(part_n.alloc((size_t)S * BG * sizeof(double), st));
+    bg = f32 ? BG32 : BG;
+    MARIE_TRY(part_d.alloc((size_t)S * 128 * bg * sizeof(double2), st));
+    MARIE_TRY(part_n.alloc((size_t)S * (bg > BG ? bg : BG) * sizeof(double), st));
     MARIE_TRY(h.alloc((size_t)S * (m + 1) * sizeof(double2), st));
     MARIE_TRY(H.alloc((size_t)S * (m + 1) * m * sizeof(double2), st));
     MARIE_TRY(R.alloc((size_t)S * (m + 1) * m * sizeof(double2), st));
@@ -439,6 +469,8 @@ struct BatchWork {
     MARIE_TRY(hn.alloc((size_t)S * sizeof(double), st));
     MARIE_TRY(stop.alloc((size_t)S * sizeof(int), st));
     MARIE_TRY(norms.alloc((size_t)S * sizeof(double), st));
+    MARIE_TRY(cnt.alloc((size_t)2 * S * sizeof(unsigned), st));
+    MARIE_CUDA_TRY(cudaMemsetAsync(cnt.p, 0, (size_t)2 * S * sizeof(unsigned), st));
     gs = GState{H.as<double2>(), R.as<double2>(), g.as<double2>(), cs.as<double>(), sn.as<double2>(),
                 y.as<double2>(), res.as<double2>(), resv.as<double>(), beta.as<double>(), tol.as<double>(),
                 hn.as<double>(), stop.as<int>()};
@@ -512,12 +544,13 @@ static int cycle(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L
   for (int k = 1; k <= m; ++k) {
     // V(:,k) = L1 A R1 V(:,k-1), in the basis precision
     MARIE_TRY(basis_matvec(W, A, L1, R1, V + (long long)(k - 1) * n, V + (long long)k * n, k));
-    kb_dots<VB><<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, stop, W.part_d.as<double2>());
-    kb_dots_fin<<<dim3(k, S), 32, 0, st>>>(W.part_d.as<double2>(), BG, k, stop, W.h.as<double2>(), m + 1);
-    kb_update<VB><<<dim3(BG, S), BT, 0, st>>>(V, vs, n, k, W.h.as<double2>(), m + 1, stop, W.part_n.as<double>());
-    kb_givens<<<S, 32, 0, st>>>(W.gs, m, k, W.h.as<double2>(), m + 1, W.part_n.as<double>(), BG);
+    unsigned* cnt = W.cnt.as<unsigned>();
+    kb_dots<VB><<<dim3(W.bg, S), BT, 0, st>>>(V, vs, n, k, stop, W.part_d.as<double2>(), cnt, W.h.as<double2>(),
+                                              m + 1);
+    kb_update<VB><<<dim3(W.bg, S), BT, 0, st>>>(V, vs, n, k, W.h.as<double2>(), m + 1, stop,
+                                                W.part_n.as<double>(), cnt + S, W.gs, m);
     kb_scale<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, k, W.hn.as<double>(), stop);
-    count_launch(5);
+    count_launch(3);
   }
   // x += R1(V y) ; r = V(:,1:k+1) res
   kb_combine<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, W.y.as<double2>(), m, stop, 0, W.t1.as<double2>(), n, 0);
