@@ -102,17 +102,72 @@ __global__ void kb_norm_fin(const double* __restrict__ part, int G, const int* _
   if (threadIdx.x == 0) out[s] = sqrt(a);
 }
 
-// cycle start: V_s(:,0) = r_s / beta_s
+// Load unit of the streaming basis kernels: one complex for the FP64 basis,
+// two for the FP32 basis (16-byte loads; its column stride ld is even and the
+// padding rows [n, ld) hold zeros).  Accumulators are the basis precision.
+template <typename VB> struct BUnit;
+template <> struct BUnit<double2> {
+  using U = double2;
+  static constexpr int W = 1;
+  __device__ __forceinline__ static U zero() { return mk<double2>(0, 0); }
+  // acc += conj(v) w
+  __device__ __forceinline__ static void dot(double2& acc, U v, U w) {
+    acc.x = fmaT(v.x, w.x, fmaT(v.y, w.y, acc.x));
+    acc.y = fmaT(v.x, w.y, fmaT(-v.y, w.x, acc.y));
+  }
+  // w -= v c
+  __device__ __forceinline__ static void axpy(U& w, U v, double2 c) {
+    w.x = fmaT(-v.x, c.x, fmaT(v.y, c.y, w.x));
+    w.y = fmaT(-v.x, c.y, fmaT(-v.y, c.x, w.y));
+  }
+  __device__ __forceinline__ static double norm2(U w, double a) { return fmaT(w.x, w.x, fmaT(w.y, w.y, a)); }
+  __device__ __forceinline__ static U scale(U w, double f) { return mk<double2>(w.x * f, w.y * f); }
+};
+template <> struct BUnit<float2> {
+  using U = float4;  // (re, im) of rows 2i and 2i+1
+  static constexpr int W = 2;
+  __device__ __forceinline__ static U zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+  __device__ __forceinline__ static void dot(float2& acc, U v, U w) {
+    acc.x = fmaT(v.x, w.x, fmaT(v.y, w.y, fmaT(v.z, w.z, fmaT(v.w, w.w, acc.x))));
+    acc.y = fmaT(v.x, w.y, fmaT(-v.y, w.x, fmaT(v.z, w.w, fmaT(-v.w, w.z, acc.y))));
+  }
+  __device__ __forceinline__ static void axpy(U& w, U v, float2 c) {
+    w.x = fmaT(-v.x, c.x, fmaT(v.y, c.y, w.x));
+    w.y = fmaT(-v.x, c.y, fmaT(-v.y, c.x, w.y));
+    w.z = fmaT(-v.z, c.x, fmaT(v.w, c.y, w.z));
+    w.w = fmaT(-v.z, c.y, fmaT(-v.w, c.x, w.w));
+  }
+  __device__ __forceinline__ static float norm2(U w, float a) {
+    return fmaT(w.x, w.x, fmaT(w.y, w.y, fmaT(w.z, w.z, fmaT(w.w, w.w, a))));
+  }
+  __device__ __forceinline__ static U scale(U w, float f) { return make_float4(w.x * f, w.y * f, w.z * f, w.w * f); }
+};
+
+__device__ __forceinline__ float2 wsum2f(float2 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  return v;
+}
+// warp sum of per-lane partial dots: FP64 lanes in FP64; FP32 lanes in FP32
+// (a few more roundings on a 32-term sum), then FP64 across warps and blocks
+__device__ __forceinline__ double2 warp_dot_sum(double2 v) { return wsum2(v); }
+__device__ __forceinline__ double2 warp_dot_sum(float2 v) { return cvt<double2>(wsum2f(v)); }
+
+// cycle start: V_s(:,0) = r_s / beta_s (zeros in the padding rows n..ld)
 template <typename VB>
 __global__ void kb_cycle_init(const double2* __restrict__ r, long long rs, VB* __restrict__ Vb, long long vs,
-                              long long n, const double* __restrict__ beta, const int* __restrict__ stop) {
+                              long long n, long long ld, const double* __restrict__ beta,
+                              const int* __restrict__ stop) {
   const int s = blockIdx.y;
   if (stop[s] < 1) return;
   const double inv = 1.0 / beta[s];  // 0 -> Inf/NaN exactly as the reference's r / norm(r)
   const double2* x = r + s * rs;
   VB* v = Vb + s * vs;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    v[i] = cvt<VB>(mk<double2>(x[i].x * inv, x[i].y * inv));
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ld; i += (long long)gridDim.x * blockDim.x)
+    v[i] = i < n ? cvt<VB>(mk<double2>(x[i].x * inv, x[i].y * inv)) : mk<VB>(0, 0);
 }
 
 // The block that finishes last (counted in cnt[s], reset by that block) runs
@@ -132,32 +187,29 @@ __device__ __forceinline__ bool last_block(unsigned* cnt) {
   return is_last;
 }
 
-// One sweep over NC basis columns c0..c0+NC-1: the block's partial sums of
-// conj(V(:,j)) w, reduced in the block (warp sums, then warp partials in warp
-// order by one thread per column: a fixed order).  NC is a template argument
-// so that a short last sweep issues no idle work.  Each thread accumulates in
-// the basis precision; the sums across threads are FP64.
+// One sweep over NC basis columns c0..c0+NC-1 (units of U, column stride nu):
+// the block's partial sums of conj(V(:,j)) w, reduced in the block (warp sums,
+// then warp partials in warp order by one thread per column: a fixed order).
+// NC is a template argument so that a short last sweep issues no idle work.
 template <int NC, typename VB>
-__device__ __forceinline__ void kb_dot_sweep(const VB* __restrict__ V, const VB* __restrict__ w,
-                                             long long n, long long i0, long long i1, int c0,
-                                             double2* __restrict__ part_s, double2 (*red)[8]) {
+__device__ __forceinline__ void kb_dot_sweep(const typename BUnit<VB>::U* __restrict__ V,
+                                             const typename BUnit<VB>::U* __restrict__ w, long long nu,
+                                             long long i0, long long i1, int c0, double2* __restrict__ part_s,
+                                             double2 (*red)[8]) {
+  using BU = BUnit<VB>;
   VB acc[NC];
 #pragma unroll
   for (int q = 0; q < NC; ++q) acc[q] = mk<VB>(0, 0);
 #pragma unroll 4
   for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    const VB wv = w[i];
+    const typename BU::U wv = w[i];
 #pragma unroll
-    for (int q = 0; q < NC; ++q) {
-      const VB v = V[(long long)(c0 + q) * n + i];
-      acc[q].x = fmaT(v.x, wv.x, fmaT(v.y, wv.y, acc[q].x));
-      acc[q].y = fmaT(v.x, wv.y, fmaT(-v.y, wv.x, acc[q].y));
-    }
+    for (int q = 0; q < NC; ++q) BU::dot(acc[q], V[(long long)(c0 + q) * nu + i], wv);
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q < NC; ++q) {
-    const double2 r = wsum2(cvt<double2>(acc[q]));
+    const double2 r = warp_dot_sum(acc[q]);
     if (lane == 0) red[wid][q] = r;
   }
   __syncthreads();
@@ -170,29 +222,31 @@ __device__ __forceinline__ void kb_dot_sweep(const VB* __restrict__ V, const VB*
 }
 
 // partial[s][j][b] = sum over block rows of conj(V_s(:,j)) w_s, j < k, w_s = V_s(:,k);
-// h[s][j] = sum_b partial[s][j][b]
+// h[s][j] = sum_b partial[s][j][b].  ld: column stride in complex elements.
 template <typename VB>
-__global__ void __launch_bounds__(BT) kb_dots(const VB* __restrict__ Vb, long long vs, long long n, int k,
+__global__ void __launch_bounds__(BT) kb_dots(const VB* __restrict__ Vb, long long vs, long long ld, int k,
                                               const int* __restrict__ stop, double2* __restrict__ part,
                                               unsigned* __restrict__ cnt, double2* __restrict__ h, int hld) {
+  using U = typename BUnit<VB>::U;
   const int s = blockIdx.y;
   if (skip(stop, s, k)) return;
-  const VB* V = Vb + s * vs;
-  const VB* w = V + (long long)k * n;
+  const long long nu = ld / BUnit<VB>::W;
+  const U* V = reinterpret_cast<const U*>(Vb + s * vs);
+  const U* w = V + (long long)k * nu;
   double2* part_s = part + (long long)s * 128 * gridDim.x;
   __shared__ double2 red[BT / 32][8];
   long long i0, i1;
-  rows_of(n, i0, i1);
+  rows_of(nu, i0, i1);
   int c0 = 0;
-  for (; c0 + 8 <= k; c0 += 8) kb_dot_sweep<8>(V, w, n, i0, i1, c0, part_s, red);
+  for (; c0 + 8 <= k; c0 += 8) kb_dot_sweep<8, VB>(V, w, nu, i0, i1, c0, part_s, red);
   switch (k - c0) {
-    case 1: kb_dot_sweep<1>(V, w, n, i0, i1, c0, part_s, red); break;
-    case 2: kb_dot_sweep<2>(V, w, n, i0, i1, c0, part_s, red); break;
-    case 3: kb_dot_sweep<3>(V, w, n, i0, i1, c0, part_s, red); break;
-    case 4: kb_dot_sweep<4>(V, w, n, i0, i1, c0, part_s, red); break;
-    case 5: kb_dot_sweep<5>(V, w, n, i0, i1, c0, part_s, red); break;
-    case 6: kb_dot_sweep<6>(V, w, n, i0, i1, c0, part_s, red); break;
-    case 7: kb_dot_sweep<7>(V, w, n, i0, i1, c0, part_s, red); break;
+    case 1: kb_dot_sweep<1, VB>(V, w, nu, i0, i1, c0, part_s, red); break;
+    case 2: kb_dot_sweep<2, VB>(V, w, nu, i0, i1, c0, part_s, red); break;
+    case 3: kb_dot_sweep<3, VB>(V, w, nu, i0, i1, c0, part_s, red); break;
+    case 4: kb_dot_sweep<4, VB>(V, w, nu, i0, i1, c0, part_s, red); break;
+    case 5: kb_dot_sweep<5, VB>(V, w, nu, i0, i1, c0, part_s, red); break;
+    case 6: kb_dot_sweep<6, VB>(V, w, nu, i0, i1, c0, part_s, red); break;
+    case 7: kb_dot_sweep<7, VB>(V, w, nu, i0, i1, c0, part_s, red); break;
     default: break;
   }
   // h[s][j] = sum_b part[s][j][b] by the last block, one warp per column
@@ -205,7 +259,6 @@ __global__ void __launch_bounds__(BT) kb_dots(const VB* __restrict__ Vb, long lo
     if (lane == 0) h[(long long)s * hld + j] = a;
   }
 }
-
 
 struct GState {
   double2* H;    // [S][(m+1)*m] unrotated, column-major
@@ -325,32 +378,30 @@ __device__ void givens_warp(const GState& G, int m, int k, const double2* __rest
 // w_s -= V_s(:,0:k) h_s with w_s = V_s(:,k) ; partial norms of the new w_s,
 // then the Givens step of the system (givens_warp) by the last block
 template <typename VB>
-__global__ void __launch_bounds__(BT) kb_update(VB* __restrict__ Vb, long long vs, long long n, int k,
+__global__ void __launch_bounds__(BT) kb_update(VB* __restrict__ Vb, long long vs, long long ld, int k,
                                                 const double2* __restrict__ h, int hld,
                                                 const int* __restrict__ stop, double* __restrict__ part,
                                                 unsigned* __restrict__ cnt, GState G, int m) {
+  using BU = BUnit<VB>;
+  using U = typename BU::U;
   using R = decltype(VB::x);
   const int s = blockIdx.y;
   if (skip(stop, s, k)) return;
   __shared__ VB hs[128];
   for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = cvt<VB>(h[(long long)s * hld + j]);
   __syncthreads();
-  VB* V = Vb + s * vs;
-  VB* w = V + (long long)k * n;
+  const long long nu = ld / BU::W;
+  U* V = reinterpret_cast<U*>(Vb + s * vs);
+  U* w = V + (long long)k * nu;
   long long i0, i1;
-  rows_of(n, i0, i1);
+  rows_of(nu, i0, i1);
   R a = 0;
   for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    VB v = w[i];
+    U v = w[i];
 #pragma unroll 8
-    for (int j = 0; j < k; ++j) {
-      const VB b = V[(long long)j * n + i];
-      const VB c = hs[j];
-      v.x = fmaT(-b.x, c.x, fmaT(b.y, c.y, v.x));
-      v.y = fmaT(-b.x, c.y, fmaT(-b.y, c.x, v.y));
-    }
+    for (int j = 0; j < k; ++j) BU::axpy(v, V[(long long)j * nu + i], hs[j]);
     w[i] = v;
-    a = fmaT(v.x, v.x, fmaT(v.y, v.y, a));
+    a = BU::norm2(v, a);
   }
   const double2 r = bsum2(mk<double2>((double)a, 0));
   if (threadIdx.x == 0) part[(long long)s * gridDim.x + blockIdx.x] = r.x;
@@ -358,27 +409,29 @@ __global__ void __launch_bounds__(BT) kb_update(VB* __restrict__ Vb, long long v
   if (threadIdx.x < 32) givens_warp(G, m, k, h, hld, part, gridDim.x, s, threadIdx.x);
 }
 
-
 // V_s(:,k) /= H(k+1,k)  (zero norm leaves a zero column instead of 0/0)
 template <typename VB>
-__global__ void kb_scale(VB* __restrict__ Vb, long long vs, long long n, int k, const double* __restrict__ hn,
+__global__ void kb_scale(VB* __restrict__ Vb, long long vs, long long ld, int k, const double* __restrict__ hn,
                          const int* __restrict__ stop) {
+  using BU = BUnit<VB>;
+  using U = typename BU::U;
   using R = decltype(VB::x);
   const int s = blockIdx.y;
   if (skip(stop, s, k)) return;
   const double h = hn[s];
   const R inv = (R)(h > 0 ? 1.0 / h : 0.0);
-  VB* w = Vb + s * vs + (long long)k * n;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    w[i] = mk<VB>(w[i].x * inv, w[i].y * inv);
+  const long long nu = ld / BU::W;
+  U* w = reinterpret_cast<U*>(Vb + s * vs) + (long long)k * nu;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nu; i += (long long)gridDim.x * blockDim.x)
+    w[i] = BU::scale(w[i], inv);
 }
 
 // out_s = V_s(:, 0:c_s) coef_s with c_s = stop[s] + extra (skipped when
 // stop[s] < 1), summed in the basis precision; accumulate adds out_s (FP64)
 template <typename VB>
-__global__ void kb_combine(const VB* __restrict__ Vb, long long vs, long long n, const double2* __restrict__ coef,
-                           int cld, const int* __restrict__ stop, int extra, double2* __restrict__ out, long long os,
-                           int accumulate) {
+__global__ void kb_combine(const VB* __restrict__ Vb, long long vs, long long n, long long ld,
+                           const double2* __restrict__ coef, int cld, const int* __restrict__ stop, int extra,
+                           double2* __restrict__ out, long long os, int accumulate) {
   const int s = blockIdx.y;
   const int k = stop[s];
   if (k < 1) return;
@@ -391,7 +444,7 @@ __global__ void kb_combine(const VB* __restrict__ Vb, long long vs, long long n,
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     VB v = mk<VB>(0, 0);
     for (int j = 0; j < nc; ++j) {
-      const VB b = V[(long long)j * n + i];
+      const VB b = V[(long long)j * ld + i];
       v.x = fmaT(b.x, cf[j].x, fmaT(-b.y, cf[j].y, v.x));
       v.y = fmaT(b.x, cf[j].y, fmaT(b.y, cf[j].x, v.y));
     }
@@ -429,7 +482,7 @@ static inline int gx(long long n) {
 
 struct BatchWork {
   int S = 0, m = 0;
-  long long n = 0;
+  long long n = 0, ld = 0;  // rows; column stride of the basis
   bool f32 = false;  // FP32 basis (t1f, t2f: FP32 work vectors of the preconditioner chains)
   int bg = BG;       // row blocks of kb_dots / kb_update
   DBuf V, t1, t2, t1f, t2f, r, part_d, part_n, h, H, R, g, cs, sn, y, res, resv, beta, tol, hn, stop, norms;
@@ -445,8 +498,13 @@ struct BatchWork {
     m = m_;
     n = n_;
     f32 = f32_;
-    MARIE_TRY(V.alloc((size_t)S * (m + 1) * n * (f32 ? sizeof(float2) : sizeof(double2)), st));
+    // FP32 basis columns padded to a multiple of 64 rows (16-byte loads of
+    // row pairs); the padding stays zero: the matvec writes rows < n only and
+    // the updates of zero rows give zeros
+    ld = f32 ? (n + 63) / 64 * 64 : n;
+    MARIE_TRY(V.alloc((size_t)S * (m + 1) * ld * (f32 ? sizeof(float2) : sizeof(double2)), st));
     if (f32) {
+      MARIE_CUDA_TRY(cudaMemsetAsync(V.p, 0, (size_t)S * (m + 1) * ld * sizeof(float2), st));
       MARIE_TRY(t1f.alloc((size_t)S * n * sizeof(float2), st));
       MARIE_TRY(t2f.alloc((size_t)S * n * sizeof(float2), st));
     }
@@ -476,7 +534,7 @@ struct BatchWork {
                 hn.as<double>(), stop.as<int>()};
     return MARIE_OK;
   }
-  long long vs() const { return (long long)(m + 1) * n; }
+  long long vs() const { return (long long)(m + 1) * ld; }
 };
 
 // batched norms of X_s (stride xs) into host array
@@ -534,26 +592,27 @@ static int cycle(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L
                  long long xs, double2* Rv, long long rs) {
   cudaStream_t st = p->stream;
   const int S = W.S, m = W.m;
-  const long long n = W.n, vs = W.vs();
+  const long long n = W.n, ld = W.ld, vs = W.vs();
   VB* V = W.V.as<VB>();
   int* stop = W.stop.as<int>();
   kb_norm_part<<<dim3(BG, S), BT, 0, st>>>(Rv, rs, n, stop, 1, W.part_n.as<double>());
   kb_norm_fin<<<S, 32, 0, st>>>(W.part_n.as<double>(), BG, stop, 1, W.beta.as<double>());
-  kb_cycle_init<VB><<<dim3(gx(n), S), 256, 0, st>>>(Rv, rs, V, vs, n, W.beta.as<double>(), stop);
+  kb_cycle_init<VB><<<dim3(gx(ld), S), 256, 0, st>>>(Rv, rs, V, vs, n, ld, W.beta.as<double>(), stop);
   count_launch(3);
   for (int k = 1; k <= m; ++k) {
     // V(:,k) = L1 A R1 V(:,k-1), in the basis precision
-    MARIE_TRY(basis_matvec(W, A, L1, R1, V + (long long)(k - 1) * n, V + (long long)k * n, k));
+    MARIE_TRY(basis_matvec(W, A, L1, R1, V + (long long)(k - 1) * ld, V + (long long)k * ld, k));
     unsigned* cnt = W.cnt.as<unsigned>();
-    kb_dots<VB><<<dim3(W.bg, S), BT, 0, st>>>(V, vs, n, k, stop, W.part_d.as<double2>(), cnt, W.h.as<double2>(),
+    kb_dots<VB><<<dim3(W.bg, S), BT, 0, st>>>(V, vs, ld, k, stop, W.part_d.as<double2>(), cnt, W.h.as<double2>(),
                                               m + 1);
-    kb_update<VB><<<dim3(W.bg, S), BT, 0, st>>>(V, vs, n, k, W.h.as<double2>(), m + 1, stop,
+    kb_update<VB><<<dim3(W.bg, S), BT, 0, st>>>(V, vs, ld, k, W.h.as<double2>(), m + 1, stop,
                                                 W.part_n.as<double>(), cnt + S, W.gs, m);
-    kb_scale<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, k, W.hn.as<double>(), stop);
+    kb_scale<VB><<<dim3(gx(ld / BUnit<VB>::W), S), 256, 0, st>>>(V, vs, ld, k, W.hn.as<double>(), stop);
     count_launch(3);
   }
   // x += R1(V y) ; r = V(:,1:k+1) res
-  kb_combine<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, W.y.as<double2>(), m, stop, 0, W.t1.as<double2>(), n, 0);
+  kb_combine<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, ld, W.y.as<double2>(), m, stop, 0, W.t1.as<double2>(), n,
+                                                 0);
   count_launch();
   const double2* upd = W.t1.as<double2>();
   if (R1) {
@@ -561,7 +620,7 @@ static int cycle(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L
     upd = W.t2.as<double2>();
   }
   kb_add<<<dim3(gx(n), S), 256, 0, st>>>(upd, n, X, xs, n, stop);
-  kb_combine<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, W.res.as<double2>(), m + 1, stop, 1, Rv, rs, 0);
+  kb_combine<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, ld, W.res.as<double2>(), m + 1, stop, 1, Rv, rs, 0);
   count_launch(2);
   MARIE_CUDA_TRY(cudaGetLastError());
   return MARIE_OK;
