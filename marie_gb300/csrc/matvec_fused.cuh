@@ -21,6 +21,15 @@ namespace marie {
 
 namespace cg = cooperative_groups;
 
+// Split cluster barrier: a CTA may store into another CTA's shared memory only
+// once that CTA is running.  Arriving right after the kernel's set-up and
+// waiting just before the first remote store lets the first gathers and
+// transforms overlap the barrier (every thread arrives once, then waits once).
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
+
 // NARROW: the radix-8 schedules for the x and y transforms (twice the threads
 // per transform, half the exchange buffer, one more CTA per SM for xyfwd); an
 // autotuner variant for the lengths that have a wide schedule.
@@ -68,32 +77,43 @@ k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Pro
   const int q = (int)cluster.block_rank();
   const int plane = blockIdx.x / CS;  // z + N*c
   const IO* Jr = J + blockIdx.y * js;
+  constexpr int EX = FX::E, R0X = FX::R0;
+  const int tx = threadIdx.x % FX::T, sx = threadIdx.x / FX::T;
+  // DOF indices of one sweep of rows (the zero half of each row is skipped)
+  auto load_idx = [&](int* kk, int row0) {
+    const int yl = row0 + sx;
+    const bool valid = yl < C::RY;
+    const int* invr = inv + (long long)L * (q * C::RY + yl + (long long)M * plane);
+#pragma unroll
+    for (int b = 0; b < EX / R0X; ++b)
+#pragma unroll
+      for (int r = 0; r < R0X; ++r) {
+        const int p = FX::in_pos(tx, b, r);
+        kk[b * R0X + r] = (valid && r < R0X / 2 && p < L) ? invr[p] : -1;
+      }
+  };
+  // the first sweep's index loads are in flight while the twiddles are staged
+  int kk[EX];
+  load_idx(kk, 0);
   for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
   for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
-  cluster.sync();  // every CTA of the cluster runs before remote stores; twiddles staged
+  __syncthreads();  // twiddles staged
+  cluster_arrive_relaxed();
 
   // ---- x transforms of the owned rows, results to the owners of their columns
   {
-    constexpr int E = FX::E, R0 = FX::R0, RL = FX::RL;
-    const int t = threadIdx.x % FX::T, s = threadIdx.x / FX::T;
+    constexpr int E = FX::E, RL = FX::RL;
+    const int t = tx, s = sx;
     for (int row0 = 0; row0 < C::RY; row0 += C::SX) {
       const int yl = row0 + s;
       const bool valid = yl < C::RY;
       const int y = q * C::RY + yl;
       V reg[E];
-      // all index loads first, then all value loads: one exposed latency per level
-      int kk[E];
-      const int* invr = inv + (long long)L * (y + (long long)M * plane);
-#pragma unroll
-      for (int b = 0; b < E / R0; ++b)
-#pragma unroll
-        for (int r = 0; r < R0; ++r) {
-          const int p = FX::in_pos(t, b, r);
-          kk[b * R0 + r] = (valid && r < R0 / 2 && p < L) ? invr[p] : -1;
-        }
+      if (row0 > 0) load_idx(kk, row0);
 #pragma unroll
       for (int i = 0; i < E; ++i) reg[i] = kk[i] >= 0 ? cvt<V>(prologue_in(Jr, pro, kk[i])) : mk<V>(0, 0);
       FX::run_half(reg, xb + s * C::ROWP, SAddr(1, true), t, twx_s);
+      if (row0 == 0) cluster_wait();  // every CTA of the cluster runs before remote stores
       if (valid) {
 #pragma unroll
         for (int b = 0; b < E / RL; ++b)
@@ -158,9 +178,6 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const IO* __restrict__ J, l
   cg::cluster_group cluster = cg::this_cluster();
   const int q = (int)cluster.block_rank();
   const int plane = blockIdx.x / CS;
-  for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
-  for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
-  cluster.sync();
   const SAddr rowa(1, true);
 
   // ---- inverse y transforms of the owned columns, kept rows to their owners
@@ -168,17 +185,29 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const IO* __restrict__ J, l
     constexpr int E = FYI::E, R0 = FYI::R0, RL = FYI::RL;
     const int s = threadIdx.x % C::SY, t = threadIdx.x / C::SY;
     const V* Bp = B + blockIdx.y * bs + (long long)plane * NM * NL + q * C::CW;
-    for (int c0 = 0; c0 < C::CW; c0 += C::SY) {
+    auto load_cols = [&](V* reg, int c0) {
       const int col = c0 + s;
       const bool valid = col < C::CW;
-      const int kx = q * C::CW + col;
-      V reg[E];
 #pragma unroll
       for (int b = 0; b < E / R0; ++b)
 #pragma unroll
         for (int r = 0; r < R0; ++r)
           reg[b * R0 + r] = valid ? Bp[(long long)FYI::in_pos(t, b, r) * NL + col] : mk<V>(0, 0);
+    };
+    // the first columns' loads are in flight while the twiddles are staged
+    V reg[E];
+    load_cols(reg, 0);
+    for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
+    for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
+    __syncthreads();  // twiddles staged
+    cluster_arrive_relaxed();
+    for (int c0 = 0; c0 < C::CW; c0 += C::SY) {
+      const int col = c0 + s;
+      const bool valid = col < C::CW;
+      const int kx = q * C::CW + col;
+      if (c0 > 0) load_cols(reg, c0);
       FYI::run(reg, xb + s, SAddr(C::SY + 1), t, twy_s);
+      if (c0 == 0) cluster_wait();  // every CTA of the cluster runs before remote stores
 #pragma unroll
       for (int b = 0; b < E / RL; ++b)
 #pragma unroll
