@@ -28,6 +28,7 @@ namespace cg = cooperative_groups;
 __device__ __forceinline__ void cluster_arrive_relaxed() {
   asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
 }
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
 
 // NARROW: the radix-8 schedules for the x and y transforms (twice the threads
@@ -96,8 +97,7 @@ k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Pro
   int kk[EX];
   load_idx(kk, 0);
   for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
-  for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
-  __syncthreads();  // twiddles staged
+  __syncthreads();  // x twiddles staged
   cluster_arrive_relaxed();
 
   // ---- x transforms of the owned rows, results to the owners of their columns
@@ -126,7 +126,12 @@ k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Pro
       }
     }
   }
-  cluster.sync();  // all rows delivered
+  // all rows delivered: arrive (release), stage the y twiddles while the
+  // cluster meets, wait (acquire)
+  cluster_arrive();
+  for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
+  cluster_wait();
+  __syncthreads();  // y twiddles staged (written after this thread's arrive)
 
   // ---- y transforms of the owned columns, straight to B
   {
@@ -220,7 +225,6 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const IO* __restrict__ J, l
         }
     }
   }
-  cluster.sync();
 
   // ---- inverse x transforms of the owned rows, epilogue, scatter
   {
@@ -228,6 +232,24 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const IO* __restrict__ J, l
     const int t = threadIdx.x % FXI::T, s = threadIdx.x / FXI::T;
     const IO* Jr = J + blockIdx.y * js;
     IO* outr = out + blockIdx.y * os;
+    // DOF indices of the epilogue of one sweep of rows
+    auto load_epi_idx = [&](int* kk, int row0) {
+      const int yl = row0 + s;
+      const int* invr = inv + (long long)L * (q * C::RY + yl + (long long)M * plane);
+#pragma unroll
+      for (int b = 0; b < E / RL; ++b)
+#pragma unroll
+        for (int r = 0; r < RL; ++r) {
+          const int x = FXI::out_pos(t, b, r);
+          kk[b * RL + r] = (yl < C::RY && x < L) ? invr[x] : -1;
+        }
+    };
+    // rows delivered: arrive (release) now and wait (acquire) once the first
+    // sweep's epilogue indices are in flight
+    cluster_arrive();
+    int kk[E <= 16 ? E : 1];
+    if constexpr (E <= 16) load_epi_idx(kk, 0);
+    cluster_wait();
     for (int row0 = 0; row0 < C::RYP; row0 += C::SX) {
       const int yl = row0 + s;
       const bool valid = yl < C::RY;
@@ -236,18 +258,12 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const IO* __restrict__ J, l
       V reg[E];
       FXI::load(reg, base, rowa, t, NL);
       FXI::run(reg, base, rowa, t, twx_s);
+      if constexpr (E <= 16)
+        if (row0 > 0) load_epi_idx(kk, row0);
       if (valid) {
         const int* invr = inv + (long long)L * (y + (long long)M * plane);
         if constexpr (E <= 16) {
-          // index loads, then the per-DOF loads, then the epilogue arithmetic
-          int kk[E];
-#pragma unroll
-          for (int b = 0; b < E / RL; ++b)
-#pragma unroll
-            for (int r = 0; r < RL; ++r) {
-              const int x = FXI::out_pos(t, b, r);
-              kk[b * RL + r] = x < L ? invr[x] : -1;
-            }
+          // index loads (above), then the per-DOF loads, then the epilogue arithmetic
           // per-DOF loads in groups of EPI (bounded registers)
           constexpr int EPI = 2;
 #pragma unroll
