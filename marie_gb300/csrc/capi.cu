@@ -702,6 +702,13 @@ int marie_plan_set_inner_precision(marie_plan* p, int precision) {
   return MARIE_OK;
 }
 
+int marie_plan_set_inner_restart(marie_plan* p, int restart) {
+  if (!p) return set_error(MARIE_EINVAL, "NULL plan");
+  if (restart < 0 || restart > 127) return set_error(MARIE_EINVAL, "inner restart must be 0 or in [1, 127]");
+  p->inner_restart = restart;
+  return MARIE_OK;
+}
+
 int64_t marie_launch_count(void) { return g_launches.load(); }
 
 void marie_inject_alloc_failure(int64_t nth) { g_fail_alloc_in.store(nth > 0 ? nth : 0); }

@@ -413,7 +413,8 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
       }
       if (!any) break;
       std::vector<GmresResult> ri;
-      MARIE_TRY(gmres_batch(p, A32, L1m, R1m, Rr, n, n, S_exc, inner_it, inner_tol, outer_it, D, n, ri, true, &act,
+      const int m_in = p->inner_restart > 0 ? p->inner_restart : inner_it;
+      MARIE_TRY(gmres_batch(p, A32, L1m, R1m, Rr, n, n, S_exc, m_in, inner_tol, outer_it, D, n, ri, true, &act,
                             false, p->inner_prec == MARIE_FP32));
       MARIE_CUDA_TRY(cudaMemcpyAsync(flags.p, act.data(), S_exc * sizeof(int), cudaMemcpyHostToDevice, st));
       k_add_b<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(D, X, n, flags.as<int>());

@@ -192,6 +192,11 @@ class Operator:
         check(self.lib.marie_plan_set_inner_precision(self.plan, {"fp32": 32, "fp64": 64}[precision]))
         return self
 
+    def set_inner_restart(self, restart):
+        """Restart length of the inner GMRES of a 'mixed' plan (0: the solver's inner_it)."""
+        check(self.lib.marie_plan_set_inner_restart(self.plan, int(restart)))
+        return self
+
     def to_array(self):
         """The FP64 operator as a 2L x 2M x 2N x 6 numpy array."""
         ptr, arr = _out((2 * self.L, 2 * self.M, 2 * self.N, 6), False)
