@@ -214,6 +214,19 @@ int marie_jvie_adjoint_grad(marie_plan* plan, const double* Einc, const double* 
                             int inner_it, int outer_it, double* F, double* dF_deps,
                             double* dF_dsigma, int* flags, int* iters);
 
+/* Replaces jvie2solver(Vrhs, fVIE, fVIEGPU, tol, Vini)
+ * (src_vie/src_solver/jvie2solver.m:1), the inner J-VIE solve that
+ * fVIEsolver_Assembly.m:196 hands to the coil solvers: BiCGSTAB (MATLAB
+ * semantics, max_it iterations, no preconditioner, x0 = Vini or zero) on the
+ * operator mv_AN(J, fN, Mr, Mc, Gram, 'notransp', idx) of the plan.  An
+ * all-zero Vrhs is returned as the solution.  idx: 1-based DOF indices into
+ * 3LMN (n_idx of them); Mr, Mc: L x M x N complex; Vrhs, Vini, Vsol: n_idx
+ * complex, host or device.  A MARIE_MIXED plan refines FP32-matvec solves
+ * with FP64 residuals.  flag / relres / iter (half steps) as bicgstab. */
+int marie_jvie2solver(marie_plan* plan, const int64_t* idx, int64_t n_idx, const double* Mr, const double* Mc,
+                      double Gram, const double* Vrhs, double tol, int max_it, const double* Vini, double* Vsol,
+                      int* flag, double* relres, double* iter, double* solvert);
+
 int marie_jvie_solve_batch(marie_plan* plan, const double* Einc, int64_t nexc, const double* e_r,
                            double dx, double freq, int form, char precond, double tol, int inner_it,
                            int outer_it, double* Je, int* flag, double* relres, int* iter,

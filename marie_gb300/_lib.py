@@ -72,6 +72,8 @@ SIGNATURES = {
                                           C.c_double, C.c_int, C.c_int, _vp, _ip, _dp, _ip, _dp]),
     "marie_jvie_adjoint_grad": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_int, _vp, C.c_double, C.c_int,
                                           C.c_int, _dp, _vp, _vp, _ip, _ip]),
+    "marie_jvie2solver": (C.c_int, [_vp, _vp, C.c_int64, _vp, _vp, C.c_double, _vp, C.c_double, C.c_int, _vp, _vp,
+                                    _ip, _dp, _dp, _dp]),
     "marie_jvie_solve_batch": (C.c_int, [_vp, _vp, C.c_int64, _vp, C.c_double, C.c_double, C.c_int, C.c_char,
                                          C.c_double, C.c_int, C.c_int, _vp, _ip, _dp, _ip, _dp]),
     "marie_e_field_nop": (C.c_int, [_vp, _vp, C.c_double, C.c_double, _vp, _vp, C.c_int]),

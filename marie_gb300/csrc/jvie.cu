@@ -319,7 +319,8 @@ struct SolverArgs {
 static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, int S_exc, double2* X, char precond,
                          double tol, int inner_it, int outer_it, SolveOut& out);
 static int solve_single(marie_plan* p, const JvieState& S, const double2* Bv, double2* X, char precond, double tol,
-                        int inner_it, int outer_it, const SolverArgs& sa, SolveOut& out);
+                        int inner_it, int outer_it, const SolverArgs& sa, SolveOut& out,
+                        const double2* x0 = nullptr);
 
 // Solves the S excitations E (3V x S, column stride es) of one body.
 static int jvie_solve_core(marie_plan* p, const double2* E, long long es, int S_exc, const double2* er, double dx,
@@ -451,7 +452,7 @@ static DevOp single(const BatchOp& op, long long n) {
 // 'L' or 'R' alike, is bicgstab's M1) or pgmresDR ('D', :400-446).  MARIE_MIXED
 // plans refine: FP32-matvec solves of A d = r, x += d, FP64 r = b - A x.
 static int solve_single(marie_plan* p, const JvieState& S, const double2* Bv, double2* X, char precond, double tol,
-                        int inner_it, int outer_it, const SolverArgs& sa, SolveOut& out) {
+                        int inner_it, int outer_it, const SolverArgs& sa, SolveOut& out, const double2* x0) {
   cudaStream_t st = p->stream;
   const long long n = S.n;
   bool pb_nz = true;
@@ -459,16 +460,16 @@ static int solve_single(marie_plan* p, const JvieState& S, const double2* Bv, do
   const int prec_main = (p->precision == MARIE_FP32) ? MARIE_FP32 : MARIE_FP64;
   const DevOp A64 = single(make_bop(p, prec_main, S, S.a.as<double2>(), S.b.as<double2>(), false), n);
   const DevOp P64 = single(make_bop(p, prec_main, S, S.pa.as<double2>(), S.pb.as<double2>(), !pb_nz), n);
-  auto run = [&](const DevOp& A, const DevOp& P, const double2* b, double t, double2* x, BicgResult& rb,
-                 GmresResult& rg) -> int {
-    if (sa.solver == 'B') return bicgstab(p, A, precond ? &P : nullptr, nullptr, b, n, t, sa.max_it, nullptr, x, rb);
+  auto run = [&](const DevOp& A, const DevOp& P, const double2* b, double t, const double2* xs, double2* x,
+                 BicgResult& rb, GmresResult& rg) -> int {
+    if (sa.solver == 'B') return bicgstab(p, A, precond ? &P : nullptr, nullptr, b, n, t, sa.max_it, xs, x, rb);
     const DevOp* L1 = precond == 'L' ? &P : nullptr;
     const DevOp* R1 = precond == 'R' ? &P : nullptr;
-    return gmres_dr(p, A, L1, nullptr, R1, nullptr, b, n, inner_it, t, outer_it, sa.ritz, nullptr, x, rg);
+    return gmres_dr(p, A, L1, nullptr, R1, nullptr, b, n, inner_it, t, outer_it, sa.ritz, xs, x, rg);
   };
   if (p->precision != MARIE_MIXED) {
     GmresResult rg;
-    MARIE_TRY(run(A64, P64, Bv, tol, X, out.b, rg));
+    MARIE_TRY(run(A64, P64, Bv, tol, x0, X, out.b, rg));
     out.r[0] = rg;
     return MARIE_OK;
   }
@@ -482,17 +483,27 @@ static int solve_single(marie_plan* p, const JvieState& S, const double2* Bv, do
   MARIE_CUDA_TRY(cudaMemcpyAsync(one.p, &on, sizeof(int), cudaMemcpyHostToDevice, st));
   double2* Rr = rb.as<double2>();
   double2* D = db.as<double2>();
-  MARIE_CUDA_TRY(cudaMemsetAsync(X, 0, (size_t)n * sizeof(double2), st));
-  MARIE_CUDA_TRY(cudaMemcpyAsync(Rr, Bv, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  if (x0) {
+    // start from x0: r = b - A x0 in FP64
+    MARIE_CUDA_TRY(cudaMemcpyAsync(X, x0, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    MARIE_TRY(A64(X, Rr));
+    k_sub_b<<<dim3(grid_n(n), 1), 256, 0, st>>>(Bv, Rr, n, one.as<int>());
+    count_launch();
+    MARIE_CUDA_TRY(cudaGetLastError());
+  } else {
+    MARIE_CUDA_TRY(cudaMemsetAsync(X, 0, (size_t)n * sizeof(double2), st));
+    MARIE_CUDA_TRY(cudaMemcpyAsync(Rr, Bv, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  }
   double bn = 0;
   MARIE_TRY(dev_norm2(p, Bv, n, &bn));
   double rn = bn;
+  if (x0) MARIE_TRY(dev_norm2(p, Rr, n, &rn));
   BicgResult& B = out.b;
   GmresResult& G = out.r[0];
   B = BicgResult();
   G = GmresResult();
-  B.resvec.push_back(bn);
-  G.resvec.push_back(1.0);
+  B.resvec.push_back(rn);
+  G.resvec.push_back(bn > 0 ? rn / bn : 0.0);
   double biter = 0;
   int inner_total = 0, last_p = 0, last_flag = 1;
   for (int it = 0; it < 20 && rn > tol * bn; ++it) {
@@ -500,7 +511,7 @@ static int solve_single(marie_plan* p, const JvieState& S, const double2* Bv, do
     const double inner_tol = std::max(0.5 * tol * bn / rn, 1e-5);
     BicgResult ib;
     GmresResult ig;
-    MARIE_TRY(run(A32, P32, Rr, inner_tol, D, ib, ig));
+    MARIE_TRY(run(A32, P32, Rr, inner_tol, nullptr, D, ib, ig));
     k_add_b<<<dim3(grid_n(n), 1), 256, 0, st>>>(D, X, n, one.as<int>());
     count_launch();
     MARIE_TRY(A64(X, Rr));
@@ -808,6 +819,70 @@ int marie_jvie_solve(marie_plan* p, const double* Einc, const double* e_r, doubl
   if (resvec)
     for (int64_t i = 0; i < (int64_t)rv.size() && i < resvec_cap; ++i) resvec[i] = rv[i];
   if (solvert) *solvert = std::chrono::duration<double>(t1 - t0).count();
+  return MARIE_OK;
+}
+
+int marie_jvie2solver(marie_plan* p, const int64_t* idx, int64_t n_idx, const double* Mr, const double* Mc,
+                      double Gram, const double* Vrhs, double tol, int max_it, const double* Vini, double* Vsol,
+                      int* flag, double* relres, double* iter, double* solvert) {
+  if (!p || !idx || !Mr || !Mc || !Vrhs || !Vsol || n_idx < 1) return set_error(MARIE_EINVAL, "NULL argument");
+  if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator");
+  if (!(tol > 0)) return set_error(MARIE_EINVAL, "tol must be positive");
+  if (max_it < 1) return set_error(MARIE_EINVAL, "max_it must be >= 1");
+  const auto t0 = std::chrono::steady_clock::now();
+  cudaStream_t st = p->stream;
+  const long long V = p->d.V, n = n_idx;
+  DBuf tidx, tMr, tMc, tb, tx0, tx;
+  const void *idx_d, *Mr_d, *Mc_d, *b_d, *x0_d = nullptr;
+  void* x_d;
+  MARIE_TRY(stage_in(idx, n * sizeof(int64_t), st, tidx, &idx_d));
+  MARIE_TRY(stage_in(Mr, V * sizeof(double2), st, tMr, &Mr_d));
+  MARIE_TRY(stage_in(Mc, V * sizeof(double2), st, tMc, &Mc_d));
+  MARIE_TRY(stage_in(Vrhs, n * sizeof(double2), st, tb, &b_d));
+  if (Vini) MARIE_TRY(stage_in(Vini, n * sizeof(double2), st, tx0, &x0_d));
+  MARIE_TRY(stage_out(Vsol, n * sizeof(double2), st, tx, &x_d));
+  HostPrefault pf;
+  pf.start(Vsol, n * sizeof(double2));
+  if (flag) *flag = 0;
+  if (relres) *relres = 0;
+  if (iter) *iter = 0;
+  // jvie2solver.m:35-38: an all-zero right-hand side is returned as the solution
+  bool nz = true;
+  MARIE_TRY(any_nonzero(p, (const double2*)b_d, n, &nz));
+  if (!nz) {
+    MARIE_CUDA_TRY(cudaMemcpyAsync(x_d, b_d, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  } else {
+    // the mv_AN('notransp') operator on the DOFs idx (jvie2solver's fVIE): a = Gram Mr(idx), b = Mc(idx)
+    JvieState S;
+    S.n = n;
+    MARIE_TRY(S.idx3.alloc(n * sizeof(int64_t), st));
+    MARIE_CUDA_TRY(cudaMemcpyAsync(S.idx3.p, idx_d, n * sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
+    MARIE_TRY(S.a.alloc(n * sizeof(double2), st));
+    MARIE_TRY(S.b.alloc(n * sizeof(double2), st));
+    MARIE_TRY(S.pa.alloc(n * sizeof(double2), st));  // no preconditioner: pa, pb unused (pb = 0)
+    MARIE_TRY(S.pb.alloc(n * sizeof(double2), st));
+    MARIE_CUDA_TRY(cudaMemsetAsync(S.pa.p, 0, n * sizeof(double2), st));
+    MARIE_CUDA_TRY(cudaMemsetAsync(S.pb.p, 0, n * sizeof(double2), st));
+    MARIE_TRY(S.inv.alloc(3 * V * sizeof(int), st));
+    MARIE_TRY(build_inverse_index(p, S.idx3.as<int64_t>(), n, S.inv.as<int>()));
+    MARIE_TRY(build_coefficients(p, S.idx3.as<int64_t>(), n, (const double2*)Mr_d, (const double2*)Mc_d, Gram, 0,
+                                 S.a.as<double2>(), S.b.as<double2>()));
+    // bicgstab(fVIE, Vrhs, tol, max_it, [], [], Vini) (jvie2solver.m:54-77)
+    SolverArgs sa;
+    sa.solver = 'B';
+    sa.max_it = max_it;
+    SolveOut so;
+    so.r.assign(1, GmresResult());
+    MARIE_TRY(solve_single(p, S, (const double2*)b_d, (double2*)x_d, 0, tol, 50, 200, sa, so,
+                           (const double2*)x0_d));
+    if (flag) *flag = so.b.flag;
+    if (relres) *relres = so.b.relres;
+    if (iter) *iter = so.b.iter;
+  }
+  pf.join();
+  MARIE_TRY(finish_out(Vsol, x_d, n * sizeof(double2), st));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+  if (solvert) *solvert = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return MARIE_OK;
 }
 

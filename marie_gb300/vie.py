@@ -22,6 +22,8 @@ argument order, defaults and return tuples:
                                                  src_vie/src_solver/Scat_Solver.m:1
     E_field_Nop(J, fN, Gram, freq, Einc, GPU_flag)
                                                  src_vie/src_fields/src_op/E_field_Nop.m:1
+    fVIEsolver_Assembly(RHBM, freq, gpu_flag)    src_vie/src_solver/fVIEsolver_Assembly.m:1
+    jvie2solver(Vrhs, ..., tol, Vini)            src_vie/src_solver/jvie2solver.m:1
     PlaneWave_Excitation(r, k, omega_mu, Eo)     src_vie/src_fields/src_excitations/PlaneWave_Excitation.m:1
     Dipole_Excitation(r, k, DipJ, DipCoord)      src_vie/src_fields/src_excitations/Dipole_Excitation.m:1
 
@@ -680,6 +682,123 @@ def JVIE_Solver_bodies(bodies, freq, tol=None, form=None, precond=None, inner_it
         res.append((outs[b], flag[o:o + k], relres[o:o + k], it.reshape(-1, 2)[o:o + k]))
         o += k
     return res, solvert.value
+
+
+# ---------------------------------------------------------------------------
+# the J-VIE solve as the inner solver of the coil solvers
+# ---------------------------------------------------------------------------
+# grid sizes L (per axis) whose 2L the FFT engine transforms
+SUPPORTED_L = (4, 8, 12, 16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 192, 256)
+
+
+def supported_size(n):
+    """The smallest grid size >= n per axis that the matvec transforms (2n in
+    the FFT engine's length list); larger grids are extended with air."""
+    for L in SUPPORTED_L:
+        if L >= n:
+            return L
+    raise ValueError(f"grid dimension {n} exceeds the largest supported size {SUPPORTED_L[-1]}")
+
+
+def jvie2solver(Vrhs, fN, idx, Mr, Mc, Gram, tol, Vini=None, max_it=1000):
+    """jvie2solver.m:1-79: BiCGSTAB (max_it iterations, no preconditioner, x0 =
+    Vini) on mv_AN(J, fN, Mr, Mc, Gram, 'notransp', idx); an all-zero Vrhs is
+    returned unchanged.  fN: an Operator (or a 2L x 2M x 2N x 6 array).  Returns
+    (Vsol, flag, relres, iter, solvert); iter counts half steps."""
+    opr, tmp = _operator_for(fN, "fp64")
+    try:
+        n = int(np.asarray(idx).size) if not _is_cuda(idx) else int(idx.numel())
+        ip, ik = _in(idx, np.int64)
+        mrp, mrk = _in(Mr)
+        mcp, mck = _in(Mc)
+        bp, bk = _in(Vrhs)
+        xp, xk = _in(Vini) if Vini is not None else (None, None)
+        op_, out = _out((n,), _is_cuda(Vrhs))
+        flag = C.c_int()
+        relres = C.c_double()
+        it = C.c_double()
+        solvert = C.c_double()
+        check(opr.lib.marie_jvie2solver(opr.plan, ip, n, mrp, mcp, float(Gram), bp, float(tol), int(max_it), xp, op_,
+                                        C.byref(flag), C.byref(relres), C.byref(it), C.byref(solvert)))
+        return out, flag.value, relres.value, it.value, solvert.value
+    finally:
+        if tmp:
+            opr.close()
+
+
+def _crop_box(r, e_r, dx):
+    """Index ranges of fVIEsolver_Assembly.m:82-94: the grid lines within one
+    voxel of the non-air voxels' bounding box."""
+    nonair = np.abs(e_r - 1) > 1e-12
+    ranges = []
+    for a in range(3):
+        coord = r[..., a][nonair]
+        lo, hi = coord.min() - dx, coord.max() + dx
+        line = np.moveaxis(r[..., a], a, 0)[:, 0, 0]
+        ranges.append(np.flatnonzero((line >= lo) & (line <= hi)))
+    return ranges
+
+
+def fVIEsolver_Assembly(RHBM, freq, gpu_flag=1, precision="fp64"):
+    """fVIEsolver_Assembly.m:1-210: prepares a body for repeated J-VIE solves.
+
+    RHBM: dict with r (L,M,N,3), epsilon_r, sigma_e (L,M,N) and optionally fN
+    (an Operator or array for the full grid) and freqfN.  The domain is cropped
+    to one voxel around the non-air bounding box when that is below 70 % of the
+    voxels, or when no operator for this frequency is given (then the operator
+    is assembled on the device); the cropped grid is then extended with air to
+    the next size the FFT engine transforms (the matvec on the non-air DOFs is
+    unchanged by air padding).  Returns (fVIEsolver, Gram, tau3, Scoord, op):
+    fVIEsolver(Vrhs, tol, Vini) -> Vsol solves the form-2 system on the DOFs in
+    the order of Scoord (tau3 turns incident fields at those voxels into the
+    right-hand side); op is the Operator that holds fN on the device."""
+    omega = 2 * np.pi * freq
+    r = np.asarray(RHBM["r"], dtype=np.float64)
+    e_r = np.asarray(RHBM["epsilon_r"]) - 1j * np.asarray(RHBM["sigma_e"]) / (EPS0 * omega)
+    dx = float(r[1, 0, 0, 0] - r[0, 0, 0, 0])
+    Gram = dx**3
+    L, M, N = e_r.shape
+    ND = L * M * N
+    idxS = np.flatnonzero(np.abs(e_r.reshape(-1, order="F") - 1) > 1e-12)
+    Scoord = np.stack([r[..., a].reshape(-1, order="F")[idxS] for a in range(3)], axis=1)
+    ix, iy, iz = _crop_box(r, e_r, dx)
+    Lf, Mf, Nf = len(ix), len(iy), len(iz)
+    fN = RHBM.get("fN")
+    if Lf * Mf * Nf < 0.7 * ND or fN is None or RHBM.get("freqfN") != freq:
+        e_r = e_r[np.ix_(ix, iy, iz)]
+        Ls, Ms, Ns = supported_size(Lf), supported_size(Mf), supported_size(Nf)
+        e_pad = np.ones((Ls, Ms, Ns), complex, order="F")
+        e_pad[:Lf, :Mf, :Nf] = e_r
+        e_r = e_pad
+        op = Operator.assemble(Ls, Ms, Ns, dx, freq, precision=precision)
+    else:
+        op = fN if isinstance(fN, Operator) else Operator.from_array(fN, precision=precision)
+    e_r = np.asfortranarray(e_r)
+    Lc, Mc_, Nc = e_r.shape
+    NDc = Lc * Mc_ * Nc
+    idxS = np.flatnonzero(np.abs(e_r.reshape(-1, order="F") - 1) > 1e-12)
+    idxS3 = np.concatenate([idxS, NDc + idxS, 2 * NDc + idxS]).astype(np.int64) + 1
+    Mr = np.asfortranarray(e_r / e_r)
+    Mcoef = np.asfortranarray((e_r - 1.0) / e_r)
+    tau = (1j * omega * EPS0 * Mcoef).reshape(-1, order="F")[idxS]
+    tau3 = np.concatenate([tau, tau, tau])
+    if torch is not None and torch.cuda.is_available():
+        # the per-body arrays stay on the device between solves
+        idx_d = torch.from_numpy(idxS3).cuda()
+        Mr_d = _colmajor_cuda_from_numpy(Mr)
+        Mc_d = _colmajor_cuda_from_numpy(Mcoef)
+    else:
+        idx_d, Mr_d, Mc_d = idxS3, Mr, Mcoef
+
+    def fVIEsolver(Vrhs, tol, Vini=None):
+        return jvie2solver(Vrhs, op, idx_d, Mr_d, Mc_d, Gram, tol, Vini)[0]
+
+    return fVIEsolver, Gram, tau3, Scoord, op
+
+
+def _colmajor_cuda_from_numpy(a):
+    t = torch.from_numpy(np.ascontiguousarray(a.transpose(*range(a.ndim - 1, -1, -1)))).cuda()
+    return t.permute(*range(a.ndim - 1, -1, -1))
 
 
 # ---------------------------------------------------------------------------

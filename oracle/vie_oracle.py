@@ -970,6 +970,61 @@ def getOPERATORS(r, f, op="N", typ="FFTofC", sing=None):
 # ---------------------------------------------------------------------------
 # grid helpers (grid3d.m:35-61 layout: L x M x N x 3 voxel centres)
 # ---------------------------------------------------------------------------
+def jvie2solver(Vrhs, fVIE, tol, Vini=None, max_it=1000):
+    """jvie2solver.m:35-77: an all-zero right-hand side is its own solution;
+    otherwise bicgstab(fVIE, Vrhs, tol, max_it, [], [], Vini)."""
+    if not np.any(Vrhs):
+        return Vrhs.copy(), 0, 0.0, 0.0
+    x, flag, relres, it, resvec = bicgstab(fVIE, Vrhs, tol, max_it, None, None, Vini)
+    return x, flag, relres, it
+
+
+def fVIEsolver_Assembly(RHBM, freq):
+    """fVIEsolver_Assembly.m:41-196 without the GPU branch: e_r, Gram, the
+    non-air DOFs and their coordinates (:54-71), the crop to one voxel around
+    the non-air bounding box (:77-94) when it is below 70 % of the voxels or
+    no operator for this frequency is cached (:100-122), Mr, Mc and tau3
+    (:130-138), and the solver handle of jvie2solver (:196).  Returns
+    (fVIEsolver, Gram, tau3, Scoord, (e_r, idxS3, fN)) with the cropped
+    e_r, its 1-based DOF indices and the operator."""
+    eo = EPS0
+    omega = 2 * np.pi * freq
+    r = RHBM["r"]
+    e_r = RHBM["epsilon_r"] - 1j * RHBM["sigma_e"] / (eo * omega)
+    dx = r[1, 0, 0, 0] - r[0, 0, 0, 0]
+    Gram = dx**3
+    L, M, N = e_r.shape
+    ND = L * M * N
+    idxS = np.flatnonzero(np.abs(e_r.reshape(-1, order="F") - 1) > 1e-12)
+    Scoord = np.stack([r[..., a].reshape(-1, order="F")[idxS] for a in range(3)], axis=1)
+    lims = []
+    for a in range(3):
+        c = r[..., a].reshape(-1, order="F")[idxS]
+        lims.append((c.min() - dx, c.max() + dx))
+    gx, gy, gz = r[:, 0, 0, 0], r[0, :, 0, 1], r[0, 0, :, 2]
+    idxX = np.flatnonzero((gx >= lims[0][0]) & (gx <= lims[0][1]))
+    idxY = np.flatnonzero((gy >= lims[1][0]) & (gy <= lims[1][1]))
+    idxZ = np.flatnonzero((gz >= lims[2][0]) & (gz <= lims[2][1]))
+    e_rnew = e_r[np.ix_(idxX, idxY, idxZ)]
+    Lf, Mf, Nf = e_rnew.shape
+    fN = RHBM.get("fN")
+    if Lf * Mf * Nf < 0.7 * ND or fN is None or RHBM.get("freqfN") != freq:
+        rnew = r[np.ix_(idxX, idxY, idxZ)]
+        fN = getOPERATORS(rnew, freq)
+        e_r = e_rnew
+        L, M, N = e_r.shape
+        ND = L * M * N
+        idxS = np.flatnonzero(np.abs(e_r.reshape(-1, order="F") - 1) > 1e-12)
+    idxS3 = np.concatenate([idxS, ND + idxS, 2 * ND + idxS]) + 1
+    Mr = e_r / e_r
+    Mc = (e_r - 1.0) / e_r
+    tau = (1j * omega * eo * Mc).reshape(-1, order="F")[idxS]
+    tau3 = np.concatenate([tau, tau, tau])
+    fVIE = lambda J: mv_AN(J, fN, Mr, Mc, Gram, "notransp", idxS3)
+    fVIEsolver = lambda Vrhs, tol, Vini=None: jvie2solver(Vrhs, fVIE, tol, Vini)
+    return fVIEsolver, Gram, tau3, Scoord, (e_r, idxS3, fN)
+
+
 def grid(L, M, N, dx, center=(0.0, 0.0, 0.0)):
     xs = (np.arange(L) - (L - 1) / 2) * dx + center[0]
     ys = (np.arange(M) - (M - 1) / 2) * dx + center[1]
