@@ -110,6 +110,7 @@ k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Pro
       const int y = q * C::RY + yl;
       V reg[E];
       if (row0 > 0) load_idx(kk, row0);
+      if (row0 == 0) pdl_wait();  // J is the previous pass's output
 #pragma unroll
       for (int i = 0; i < E; ++i) reg[i] = kk[i] >= 0 ? cvt<V>(prologue_in(Jr, pro, kk[i])) : mk<V>(0, 0);
       FX::run_half(reg, xb + s * C::ROWP, SAddr(1, true), t, twx_s);
@@ -132,6 +133,8 @@ k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Pro
   for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
   cluster_wait();
   __syncthreads();  // y twiddles staged (written after this thread's arrive)
+
+  pdl_trigger();
 
   // ---- y transforms of the owned columns, straight to B
   {
@@ -199,11 +202,12 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const IO* __restrict__ J, l
         for (int r = 0; r < R0; ++r)
           reg[b * R0 + r] = valid ? Bp[(long long)FYI::in_pos(t, b, r) * NL + col] : mk<V>(0, 0);
     };
-    // the first columns' loads are in flight while the twiddles are staged
-    V reg[E];
-    load_cols(reg, 0);
+    // twiddles staged before the wait for the spectrum of the previous pass
     for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
     for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
+    pdl_wait();
+    V reg[E];
+    load_cols(reg, 0);
     __syncthreads();  // twiddles staged
     cluster_arrive_relaxed();
     for (int c0 = 0; c0 < C::CW; c0 += C::SY) {

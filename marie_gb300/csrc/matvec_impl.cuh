@@ -54,9 +54,18 @@ template <typename T> struct MatvecImpl {
     const size_t smem = (size_t)ZC::bytes(S);  // S columns, 3 component buffers, operator tile
     cudaError_t e = opt_in_smem(k_zmul<T, NZ, KIND, VAR>, smem);
     if (e != cudaSuccess) return e;
-    dim3 grid((d.Lp + S - 1) / S, d.Mp, nrhs);
-    k_zmul<T, NZ, KIND, VAR><<<grid, ZC::THREADS, smem, st>>>(B, bs, fN, oct, d, tw);
-    return cudaGetLastError();
+    // the pass waits (griddepcontrol) before reading the previous pass's output
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((d.Lp + S - 1) / S, d.Mp, nrhs);
+    cfg.blockDim = dim3(ZC::THREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_zmul<T, NZ, KIND, VAR>, B, bs, fN, oct, d, tw);
   }
   template <int NZ>
   static cudaError_t zmul_n(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
@@ -142,13 +151,16 @@ template <typename T> struct FusedImpl {
     cfg.blockDim = dim3(256, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)CS;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
+    // the pass waits (griddepcontrol) before reading the previous pass's output
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = 2;
     return cudaLaunchKernelExC(&cfg, (const void*)kern, args);
   }
   template <int NL, int NM, int CS, bool NARROW, typename IO>

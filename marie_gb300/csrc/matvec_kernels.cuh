@@ -33,6 +33,15 @@ struct Dims {
 
 __device__ __forceinline__ bool rhs_skipped(const Dims& d, int rhs) { return d.stop && d.stop[rhs] < d.step; }
 
+// Programmatic dependent launch: a pass launched with the
+// programmatic-serialization attribute may start while the previous pass
+// finishes.  It loads what does not depend on that pass (operator tile,
+// twiddles, index map), then waits for it to complete (pdl_wait; a no-op
+// when launched without the attribute) before reading its output.  A pass
+// signals with pdl_trigger, in its last phase, that the next one may start.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Epilogue: out[k] = A_k * J[k] - (conjout ? conj(v) : B_k * v)
 struct Epilogue {
   const double2* a;  // per-DOF, or null -> a_s
@@ -465,6 +474,7 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
     }
   }
   stage_twiddles(tw_s, tw, NZ);
+  pdl_wait();  // the spectrum B is the previous pass's output
   V reg[E];
 #pragma unroll
   for (int b = 0; b < E / R0; ++b)
@@ -525,6 +535,7 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
     else
       zrow_k<2, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, bc, ad);
   }
+  pdl_trigger();
   FI::run(reg, my, ad, t, tw_s);
 #pragma unroll
   for (int b = 0; b < E / RLI; ++b)
