@@ -244,7 +244,7 @@ def run_gpu(args, world, rank, local):
     solve(op, Eh, erh, r)
     barrier(world)
     torch.cuda.synchronize()
-    ne2e = max(1, min(args.steps, 3))
+    ne2e = max(1, min(args.steps, 5))
     e2e_ms, e2e_lib_ms = [], []
     t0 = time.perf_counter()
     for _ in range(ne2e):
