@@ -63,7 +63,6 @@ __global__ void __launch_bounds__(256, NARROW ? 4 : 0)
 k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Prologue pro,
         cplx<T>* __restrict__ B, long long bs, Dims d, const cplx<T>* __restrict__ twx,
         const cplx<T>* __restrict__ twy) {
-  if (rhs_skipped(d, blockIdx.y)) return;  // uniform over the cluster
   using C = XYCfg<T, NL, NM, CS, NARROW>;
   using V = cplx<T>;
   using FX = typename C::FX;
@@ -93,10 +92,14 @@ k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Pro
         kk[b * R0X + r] = (valid && r < R0X / 2 && p < L) ? invr[p] : -1;
       }
   };
-  // the first sweep's index loads are in flight while the twiddles are staged
+  // the twiddles are staged before the wait for the previous pass; the index
+  // map, the skip mask and J are read after it (a caller may have built the
+  // map in the kernel just before)
+  for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
+  pdl_wait();
+  if (rhs_skipped(d, blockIdx.y)) return;  // uniform over the cluster, before any cluster barrier
   int kk[EX];
   load_idx(kk, 0);
-  for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
   __syncthreads();  // x twiddles staged
   cluster_arrive_relaxed();
 
@@ -110,7 +113,6 @@ k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Pro
       const int y = q * C::RY + yl;
       V reg[E];
       if (row0 > 0) load_idx(kk, row0);
-      if (row0 == 0) pdl_wait();  // J is the previous pass's output
 #pragma unroll
       for (int i = 0; i < E; ++i) reg[i] = kk[i] >= 0 ? cvt<V>(prologue_in(Jr, pro, kk[i])) : mk<V>(0, 0);
       FX::run_half(reg, xb + s * C::ROWP, SAddr(1, true), t, twx_s);

@@ -34,11 +34,13 @@ struct Dims {
 __device__ __forceinline__ bool rhs_skipped(const Dims& d, int rhs) { return d.stop && d.stop[rhs] < d.step; }
 
 // Programmatic dependent launch: a pass launched with the
-// programmatic-serialization attribute may start while the previous pass
-// finishes.  It loads what does not depend on that pass (operator tile,
-// twiddles, index map), then waits for it to complete (pdl_wait; a no-op
-// when launched without the attribute) before reading its output.  A pass
-// signals with pdl_trigger, in its last phase, that the next one may start.
+// programmatic-serialization attribute may start while the previous kernel
+// finishes.  It loads only what that kernel cannot have written (the plan's
+// operator tile and twiddles), then waits for it to complete (pdl_wait; a
+// no-op when launched without the attribute) before reading anything else.
+// The skip mask read at the top of the z and y+x passes is written by the
+// Givens step at least two kernels earlier.  A pass signals with pdl_trigger,
+// in its last phase, that the next one may start.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
