@@ -182,6 +182,19 @@ def test_mixed_inner_basis_fp32_and_fp64(precond):
     assert all(e < 1e-6 for e in errs.values()), errs
 
 
+def test_inner_settings_validated():
+    import marie_gb300 as mg
+
+    op = mg.Operator(8, 8, 8, precision="mixed")
+    op.set_inner_precision("fp64").set_inner_precision("fp32").set_inner_restart(0).set_inner_restart(127)
+    with pytest.raises(mg.MarieError):
+        op.set_inner_restart(128)
+    with pytest.raises(mg.MarieError):
+        op.set_inner_restart(-1)
+    with pytest.raises(KeyError):
+        op.set_inner_precision("fp16")
+
+
 def mie_error(L, dx, R, precision="fp64"):
     import marie_gb300 as mg
 
