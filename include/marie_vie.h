@@ -129,13 +129,24 @@ int marie_mv_L(marie_plan* plan, const double* JIn0, double Gram, const int64_t*
 int marie_mv_K(marie_plan* plan, const double* JIn0, const int64_t* idx, int64_t n_idx,
                double* JOut, int64_t nrhs, int precision);
 
+/* Binds mv_AN(., fN, Mr, Mc, Gram, transp_flag, idx) (src_vie/src_mvp/mv_AN.m:1)
+ * to the plan, the handle fA = @(J) mv_AN(J, ...) that JVIE_Solver.m:211-297
+ * passes to its solvers: marie_pgmres, marie_pgmres_dr and marie_bicgstab
+ * called with a NULL operator apply it on the device.  Arguments as
+ * marie_mv_AN; the plan keeps device copies of the DOF map and coefficients
+ * until the next bind or marie_plan_destroy. */
+int marie_plan_bind_mv_AN(marie_plan* plan, const double* Mr, const double* Mc, double Gram, int transp,
+                          const int64_t* idx, int64_t n_idx);
+
 /* Replaces pgmres(A, b, restart, tol, maxit, L1, L2, R1, R2, x0)
  * (src_numeric/src_iterative/pgmres.m:70-181, pgmres_iter.m:22-150): restarted
  * GMRES with classical Gram-Schmidt, function-handle preconditioners applied as
  * products, true residual recomputed at the end.  All vectors are device or
  * host (n complex); A/L1/L2/R1/R2 receive device vectors.  NULL L1..R2 = none;
- * NULL x0 = zero start.  Outputs: x, flag (0 converged / 1 not), relres,
- * iter = {inner, outer}, resvec (relative, length written to *resvec_len). */
+ * NULL A = the mv_AN bound to the plan (marie_plan_bind_mv_AN), applied on the
+ * device without a callback.  NULL x0 = zero start.  Outputs: x, flag (0
+ * converged / 1 not), relres, iter = {inner, outer}, resvec (relative, length
+ * written to *resvec_len). */
 int marie_pgmres(marie_plan* plan, marie_op_fn A, void* A_ctx, const double* b, int64_t n,
                  int restart, double tol, int maxit, marie_op_fn L1, void* L1_ctx,
                  marie_op_fn L2, void* L2_ctx, marie_op_fn R1, void* R1_ctx, marie_op_fn R2,
@@ -157,7 +168,7 @@ int marie_pgmres_dr(marie_plan* plan, marie_op_fn A, void* A_ctx, const double* 
  * of JVIE_Solver.m:451-499 (a MATLAB built-in, outside the reference
  * sources): BiCGSTAB with MATLAB's outputs.  Vectors device or host (n
  * complex); A/M1/M2 receive device vectors, M1/M2 applied as ph = M2(M1(p)),
- * NULL = none; NULL x0 = zero start.  flag 0 converged / 1 maxit / 2
+ * NULL = none (NULL A: the plan's bound mv_AN); NULL x0 = zero start.  flag 0 converged / 1 maxit / 2
  * preconditioner output not finite / 3 stagnation / 4 breakdown; iter in half
  * steps; resvec the absolute residual norms (initial, then one per half
  * step). */

@@ -83,6 +83,7 @@ SIGNATURES = {
     "marie_plan_set_schedule": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
     "marie_plan_set_inner_precision": (C.c_int, [_vp, C.c_int]),
     "marie_plan_set_inner_restart": (C.c_int, [_vp, C.c_int]),
+    "marie_plan_bind_mv_AN": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, _vp, C.c_int64]),
     "marie_inject_alloc_failure": (None, [C.c_int64]),
     "marie_plan_profile": (C.c_int, [_vp, C.c_int, _dp, _i64p]),
     "marie_dipole_field": (C.c_int, [_vp, C.c_int64, C.c_int64, C.c_int64, C.c_double, _vp, _vp, C.c_int64,

@@ -420,7 +420,7 @@ extern "C" int marie_bicgstab(marie_plan* p, marie_op_fn A, void* A_ctx, const d
                               int maxit, marie_op_fn M1, void* M1_ctx, marie_op_fn M2, void* M2_ctx, const double* x0,
                               double* x, int* flag, double* relres, double* iter, double* resvec, int64_t resvec_cap,
                               int64_t* resvec_len) {
-  if (!p || !A || !b || !x || n < 1) return set_error(MARIE_EINVAL, "NULL argument or n < 1");
+  if (!p || !b || !x || n < 1) return set_error(MARIE_EINVAL, "NULL argument or n < 1");
   // user operators run outside the plan's stream: finish the plan's work first
   auto wrap = [p](marie_op_fn f, void* ctx, long long nn) -> DevOp {
     return [p, f, ctx, nn](const double2* xi, double2* yo) -> int {
@@ -430,7 +430,11 @@ extern "C" int marie_bicgstab(marie_plan* p, marie_op_fn A, void* A_ctx, const d
       return MARIE_OK;
     };
   };
-  DevOp opA = wrap(A, A_ctx, n), oM1, oM2;
+  DevOp opA, oM1, oM2;
+  if (A)
+    opA = wrap(A, A_ctx, n);
+  else
+    MARIE_TRY(bound_operator(p, n, &opA));  // NULL A: the plan's bound mv_AN
   if (M1) oM1 = wrap(M1, M1_ctx, n);
   if (M2) oM2 = wrap(M2, M2_ctx, n);
   const size_t bytes = (size_t)n * sizeof(double2);

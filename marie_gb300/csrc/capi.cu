@@ -522,6 +522,42 @@ int install_operator(marie_plan* p, const double2* fN_dev, int kind) {
 
 using namespace marie;
 
+static void free_bound(marie_plan* p) {
+  cudaFree(p->bnd_idx);
+  cudaFree(p->bnd_inv);
+  cudaFree(p->bnd_a);
+  cudaFree(p->bnd_b);
+  p->bnd_idx = nullptr;
+  p->bnd_inv = nullptr;
+  p->bnd_a = p->bnd_b = nullptr;
+  p->bnd_n = 0;
+}
+
+namespace marie {
+
+int bound_operator(marie_plan* p, long long n, DevOp* op) {
+  if (!p->bnd_n) return set_error(MARIE_EINVAL, "NULL operator and no mv_AN bound to the plan (marie_plan_bind_mv_AN)");
+  if (p->bnd_n != n) return set_error(MARIE_EINVAL, "vector length %lld differs from the bound mv_AN's %lld DOFs", n,
+                                      p->bnd_n);
+  const int prec = p->fN64 ? MARIE_FP64 : MARIE_FP32;
+  *op = [p, n, prec](const double2* x, double2* y) -> int {
+    Prologue pro{nullptr, 0};
+    Epilogue ep{};
+    if (p->bnd_transp == 0) {
+      ep.a = p->bnd_a;
+      ep.b = p->bnd_b;
+    } else {
+      pro.pre = p->bnd_b;
+      pro.conjin = 1;
+      ep.a = p->bnd_a;
+      ep.conjout = 1;
+    }
+    return run_matvec(p, prec, x, y, n, 1, p->bnd_inv, pro, ep);
+  };
+  return MARIE_OK;
+}
+}  // namespace marie
+
 extern "C" {
 
 const char* marie_last_error(void) { return g_err; }
@@ -574,10 +610,48 @@ int marie_plan_create(int64_t L, int64_t M, int64_t N, int precision, int64_t nr
   return MARIE_OK;
 }
 
+int marie_plan_bind_mv_AN(marie_plan* p, const double* Mr, const double* Mc, double Gram, int transp,
+                          const int64_t* idx, int64_t n_idx) {
+  if (!p || !Mr || !Mc || !idx || n_idx < 1) return set_error(MARIE_EINVAL, "NULL argument or n_idx < 1");
+  if (transp != 0 && transp != 1) return set_error(MARIE_EINVAL, "transp must be 0 ('notransp') or 1 ('transp')");
+  if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator");
+  MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  free_bound(p);
+  const long long V = p->d.V, n = n_idx;
+  DBuf tMr, tMc;
+  const void *Mr_d, *Mc_d, *idx_d;
+  DBuf tidx;
+  MARIE_TRY(stage_in(Mr, V * sizeof(double2), p->stream, tMr, &Mr_d));
+  MARIE_TRY(stage_in(Mc, V * sizeof(double2), p->stream, tMc, &Mc_d));
+  MARIE_TRY(stage_in(idx, n * sizeof(int64_t), p->stream, tidx, &idx_d));
+  if (cudaMalloc(&p->bnd_idx, n * sizeof(int64_t)) != cudaSuccess ||
+      cudaMalloc(&p->bnd_inv, 3 * V * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&p->bnd_a, n * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&p->bnd_b, n * sizeof(double2)) != cudaSuccess) {
+    cudaGetLastError();
+    free_bound(p);
+    return set_error(MARIE_ENOMEM, "bound mv_AN: device allocation failed");
+  }
+  MARIE_CUDA_TRY(cudaMemcpyAsync(p->bnd_idx, idx_d, n * sizeof(int64_t), cudaMemcpyDeviceToDevice, p->stream));
+  int s = build_inverse_index(p, p->bnd_idx, n, p->bnd_inv);
+  if (s == MARIE_OK)
+    s = build_coefficients(p, p->bnd_idx, n, (const double2*)Mr_d, (const double2*)Mc_d, Gram, transp, p->bnd_a,
+                           p->bnd_b);
+  if (s == MARIE_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) s = set_error(MARIE_ECUDA, "bind mv_AN failed");
+  if (s != MARIE_OK) {
+    free_bound(p);
+    return s;
+  }
+  p->bnd_n = n;
+  p->bnd_transp = transp;
+  return MARIE_OK;
+}
+
 int marie_plan_destroy(marie_plan* p) {
   if (!p) return MARIE_OK;
   if (p->stream) cudaStreamSynchronize(p->stream);
   release_cufft_state(p);
+  free_bound(p);
   if (p->wsA) cudaFreeAsync(p->wsA, p->stream);
   if (p->wsB) cudaFreeAsync(p->wsB, p->stream);
   if (p->stream) cudaStreamSynchronize(p->stream);

@@ -490,7 +490,7 @@ extern "C" int marie_pgmres_dr(marie_plan* p, marie_op_fn A, void* A_ctx, const 
                                void* L2_ctx, marie_op_fn R1, void* R1_ctx, marie_op_fn R2, void* R2_ctx,
                                const double* x0, double* x, int* flag, double* relres, int* iter, double* resvec,
                                int64_t resvec_cap, int64_t* resvec_len) {
-  if (!p || !A || !b || !x || n < 1) return set_error(MARIE_EINVAL, "NULL argument or n < 1");
+  if (!p || !b || !x || n < 1) return set_error(MARIE_EINVAL, "NULL argument or n < 1");
   auto wrap = [p](marie_op_fn f, void* ctx, long long nn) -> DevOp {
     return [p, f, ctx, nn](const double2* xi, double2* yo) -> int {
       MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
@@ -499,7 +499,11 @@ extern "C" int marie_pgmres_dr(marie_plan* p, marie_op_fn A, void* A_ctx, const 
       return MARIE_OK;
     };
   };
-  DevOp opA = wrap(A, A_ctx, n), oL1, oL2, oR1, oR2;
+  DevOp opA, oL1, oL2, oR1, oR2;
+  if (A)
+    opA = wrap(A, A_ctx, n);
+  else
+    MARIE_TRY(bound_operator(p, n, &opA));  // NULL A: the plan's bound mv_AN
   if (L1) oL1 = wrap(L1, L1_ctx, n);
   if (L2) oL2 = wrap(L2, L2_ctx, n);
   if (R1) oR1 = wrap(R1, R1_ctx, n);

@@ -441,7 +441,7 @@ extern "C" int marie_pgmres(marie_plan* p, marie_op_fn A, void* A_ctx, const dou
                             marie_op_fn R1, void* R1_ctx, marie_op_fn R2, void* R2_ctx, const double* x0, double* x,
                             int* flag, double* relres, int* iter, double* resvec, int64_t resvec_cap,
                             int64_t* resvec_len) {
-  if (!p || !A || !b || !x || n < 1) return set_error(MARIE_EINVAL, "NULL argument or n < 1");
+  if (!p || !b || !x || n < 1) return set_error(MARIE_EINVAL, "NULL argument or n < 1");
   // User operators run outside the plan's stream: finish the plan's work
   // before handing them x; they return with y complete.
   auto wrap = [p](marie_op_fn f, void* ctx, long long nn) -> DevOp {
@@ -452,7 +452,11 @@ extern "C" int marie_pgmres(marie_plan* p, marie_op_fn A, void* A_ctx, const dou
       return MARIE_OK;
     };
   };
-  DevOp opA = wrap(A, A_ctx, n);
+  DevOp opA;
+  if (A)
+    opA = wrap(A, A_ctx, n);
+  else
+    MARIE_TRY(bound_operator(p, n, &opA));  // NULL A: the plan's bound mv_AN
   DevOp oL1, oL2, oR1, oR2;
   if (L1) oL1 = wrap(L1, L1_ctx, n);
   if (L2) oL2 = wrap(L2, L2_ctx, n);

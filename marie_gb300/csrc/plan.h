@@ -49,6 +49,16 @@ struct marie_plan {
   float pass_ms[5] = {0, 0, 0, 0, 0};
   long long profiled = 0;
 
+  // mv_AN bound by marie_plan_bind_mv_AN: the operator of marie_pgmres,
+  // marie_pgmres_dr and marie_bicgstab when their A is NULL (DOF indices,
+  // inverse map, epilogue / prologue coefficients; device, plan-owned).
+  int64_t* bnd_idx = nullptr;
+  int* bnd_inv = nullptr;
+  double2* bnd_a = nullptr;
+  double2* bnd_b = nullptr;
+  long long bnd_n = 0;
+  int bnd_transp = 0;
+
   // Pinned host staging for small scalars (reductions, Hessenberg columns).
   double* pinned = nullptr;
   size_t pinned_len = 0;
@@ -139,6 +149,10 @@ int dev_norm2(marie_plan* p, const double2* x, long long n, double* out_host);
 
 // A linear operator on device vectors of length n.
 using DevOp = std::function<int(const double2* x, double2* y)>;
+
+// The plan's bound mv_AN as a DevOp on n DOFs (fails with MARIE_EINVAL when
+// nothing is bound or n differs).
+int bound_operator(marie_plan* p, long long n, DevOp* op);
 
 struct GmresResult {
   int flag = 1;

@@ -194,6 +194,20 @@ class Operator:
         check(self.lib.marie_plan_set_inner_precision(self.plan, {"fp32": 32, "fp64": 64}[precision]))
         return self
 
+    def bind_mv_AN(self, Mr, Mc, Gram, transp_flag, idx):
+        """Binds mv_AN(., fN, Mr, Mc, Gram, transp_flag, idx) to this plan:
+        pgmres / pgmresDR / bicgstab given the Operator as A apply it on the
+        device (the C ABI's NULL operator)."""
+        if transp_flag not in ("notransp", "transp"):
+            raise ValueError("transp_flag must be 'notransp' or 'transp'")
+        mrp, mrk = _in(Mr)
+        mcp, mck = _in(Mc)
+        ip, ik = _in(idx, np.int64)
+        n = int(np.asarray(idx).size) if not _is_cuda(idx) else int(idx.numel())
+        check(self.lib.marie_plan_bind_mv_AN(self.plan, mrp, mcp, float(Gram), 1 if transp_flag == "transp" else 0,
+                                             ip, n))
+        return self
+
     def set_inner_restart(self, restart):
         """Restart length of the inner GMRES of a 'mixed' plan (0: the solver's inner_it)."""
         check(self.lib.marie_plan_set_inner_restart(self.plan, int(restart)))
@@ -414,7 +428,8 @@ def _vector_plan():
 
 
 def _handles(A, others, host):
-    cbs = [_wrap_handle(A, host)]
+    # an Operator with a bound mv_AN is passed as the NULL handle
+    cbs = [_lib.OP_FN() if isinstance(A, Operator) else _wrap_handle(A, host)]
     slots = []
     for h in others:
         if h is None:
@@ -438,12 +453,14 @@ def pgmres(A, b, restart=50, tol=1e-3, maxit=10, L1=None, L2=None, R1=None, R2=N
     """pgmres.m:70-181 on the device.  A, L1, L2, R1, R2 are function handles
     (preconditioners are applied as products, like the reference).  With a
     numpy b the handles receive and return numpy vectors; with a CUDA tensor b
-    they receive and return CUDA tensors.  Returns (x, flag, relres, iter, resvec)."""
+    they receive and return CUDA tensors.  A may also be an Operator with a
+    bound mv_AN (Operator.bind_mv_AN): the matvec then stays on the device with
+    no handle round trip.  Returns (x, flag, relres, iter, resvec)."""
     restart = 50 if restart is None else restart
     tol = 1e-3 if tol is None else tol
     maxit = 10 if maxit is None else maxit
     host = not _is_cuda(b)
-    opr = _vector_plan()
+    opr = A if isinstance(A, Operator) else _vector_plan()
     n = b.shape[0]
     cbs, h = _handles(A, (L1, L2, R1, R2), host)
     bp, bk = _in(b)
@@ -466,7 +483,7 @@ def pgmresDR(A, b, restart=50, tol=1e-3, maxit=10, ritz=None, L1=None, L2=None, 
     tol = 1e-3 if tol is None else tol
     maxit = 10 if maxit is None else maxit
     host = not _is_cuda(b)
-    opr = _vector_plan()
+    opr = A if isinstance(A, Operator) else _vector_plan()
     n = b.shape[0]
     cbs, h = _handles(A, (L1, L2, R1, R2), host)
     bp, bk = _in(b)
@@ -490,7 +507,7 @@ def bicgstab(A, b, tol=1e-6, maxit=None, M1=None, M2=None, x0=None):
     n = b.shape[0]
     maxit = min(n, 20) if maxit is None else maxit
     host = not _is_cuda(b)
-    opr = _vector_plan()
+    opr = A if isinstance(A, Operator) else _vector_plan()
     cbs, h = _handles(A, (M1, M2), host)
     bp, bk = _in(b)
     x0p, x0k = _in(x0) if x0 is not None else (None, None)
