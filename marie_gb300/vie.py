@@ -7,6 +7,7 @@ argument order, defaults and return tuples:
     mv_AN(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, GPU_flag)
                                                  src_vie/src_mvp/mv_AN.m:1
     mv_L(JIn0, fN, r, Gram, idx, GPU_flag)       src_vie/src_mvp/mv_L.m:1
+    mv_N(JIn0, fN, r, idx, GPU_flag)             src_vie/src_mvp/mv_N.m:1
     mv_K(JIn0, fK, r, idx, GPU_flag)             src_vie/src_mvp/mv_K.m:1
     H_field_Kop(J, fK, Gram, Hinc, GPU_flag)     src_vie/src_fields/src_op/H_field_Kop.m:1
     pgmres(A, b, restart, tol, maxit, L1, L2, R1, R2, x0)
@@ -323,6 +324,11 @@ def mv_L(JIn0, fN, r, Gram, idx, GPU_flag=1, precision="fp64"):
     finally:
         if tmp:
             opr.close()
+
+
+def mv_N(JIn0, fN, r, idx, GPU_flag=1, precision="fp64"):
+    """mv_N.m: crop(N J) on the entries idx (marie_mv_L with Gram = 0)."""
+    return mv_L(JIn0, fN, r, 0.0, idx, GPU_flag, precision)
 
 
 def _k_operator_for(fK, precision):

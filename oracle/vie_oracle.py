@@ -69,6 +69,12 @@ def mv_AN(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, workers=None):
     return JOut.reshape(-1, order="F")[np.asarray(idx) - 1]
 
 
+def mv_N(JIn0, fN, r_shape, idx, workers=None):
+    """src_vie/src_mvp/mv_N.m:1-95: crop(N J) on the entries idx (mv_L without
+    the Gram term)."""
+    return mv_L(JIn0, fN, r_shape, 0.0, idx, workers)
+
+
 def mv_L(JIn0, fN, r_shape, Gram, idx, workers=None):
     """src_vie/src_mvp/mv_L.m:30-97: crop(N J) - Gram J on the entries idx."""
     LfN, MfN, NfN, _ = fN.shape

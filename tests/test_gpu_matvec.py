@@ -80,6 +80,8 @@ def test_mv_L_matches_oracle():
         ref = vo.mv_L(x, fN, (L, M, N), 0.5, ix)
         out = mg.mv_L(x, fN, None, 0.5, ix)
         assert relerr(out, ref) < 1e-12
+        # mv_N.m: the same without the Gram term
+        assert relerr(mg.mv_N(x, fN, None, ix), vo.mv_N(x, fN, (L, M, N), ix)) < 1e-12
 
 
 def test_batched_rhs_and_device_pointers(cuda):
