@@ -168,29 +168,35 @@ __device__ __forceinline__ double2 warp_sum2(double2 v) {
   return v;
 }
 
-// Sum over Np x Np point pairs of w_p w_q exp(-j ko R)/R for one face pair;
-// lanes of one warp split the point pairs.  Points are in shared memory.
-__device__ double2 face_pair_sum(const CubArgs& A, const double* __restrict__ w, const double* __restrict__ u,
-                                 const double* __restrict__ v, int Np, int io, int is, const double rm[3],
-                                 int lane, int nl) {
+// Quadrature points of face f: X[i] = o + a u_i + b v_i, stored [i][3].
+__device__ __forceinline__ void face_points(const CubArgs& A, int f, const double* __restrict__ u,
+                                            const double* __restrict__ v, int Np, double* X, int t0, int nt) {
+  for (int i = t0; i < Np; i += nt) {
+    const double ui = u[i], vi = v[i];
+    for (int c = 0; c < 3; ++c) X[3 * i + c] = A.face_o[f][c] + A.face_a[f][c] * ui + A.face_b[f][c] * vi;
+  }
+}
+
+// Sum over Np x Np point pairs of w_p w_q exp(-j ko R)/R for one face pair
+// (points of the observation face P, of the source face Q, both [i][3] in
+// shared memory; the observation voxel is displaced by rm); threads t0,
+// t0 + nt, ... split the pairs.  1/R comes from one reciprocal square root
+// (R = R^2 / R), not a square root and a division: the FP64 pipe is the limit.
+__device__ double2 face_pair_sum(const double* __restrict__ P, const double* __restrict__ Q,
+                                 const double* __restrict__ w, int Np, double ko, const double rm[3], int t0,
+                                 int nt) {
   double2 acc = mk<double2>(0, 0);
-  const double* po = A.face_o[io];
-  const double* pa = A.face_a[io];
-  const double* pb = A.face_b[io];
-  const double* qo = A.face_o[is];
-  const double* qa = A.face_a[is];
-  const double* qb = A.face_b[is];
-  const long long tot = (long long)Np * Np;
-  for (long long t = lane; t < tot; t += nl) {
-    const int ip = (int)(t / Np), iq = (int)(t - (long long)ip * Np);
-    const double up = u[ip], vp = v[ip], uq = u[iq], vq = v[iq];
-    const double dx0 = (qo[0] + qa[0] * uq + qb[0] * vq) - (po[0] + pa[0] * up + pb[0] * vp + rm[0]);
-    const double dx1 = (qo[1] + qa[1] * uq + qb[1] * vq) - (po[1] + pa[1] * up + pb[1] * vp + rm[1]);
-    const double dx2 = (qo[2] + qa[2] * uq + qb[2] * vq) - (po[2] + pa[2] * up + pb[2] * vp + rm[2]);
-    const double R = sqrt(dx0 * dx0 + dx1 * dx1 + dx2 * dx2);
+  const int tot = Np * Np;
+  for (int t = t0; t < tot; t += nt) {
+    const int ip = t / Np, iq = t - ip * Np;
+    const double dx0 = Q[3 * iq] - (P[3 * ip] + rm[0]);
+    const double dx1 = Q[3 * iq + 1] - (P[3 * ip + 1] + rm[1]);
+    const double dx2 = Q[3 * iq + 2] - (P[3 * ip + 2] + rm[2]);
+    const double R2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
+    const double Ri = rsqrt(R2);
     double s, c;
-    sincos(A.ko * R, &s, &c);
-    const double wt = w[ip] * w[iq] / R;
+    sincos(ko * (R2 * Ri), &s, &c);
+    const double wt = w[ip] * w[iq] * Ri;
     acc.x += wt * c;
     acc.y -= wt * s;
   }
@@ -229,11 +235,14 @@ __device__ void finish_offset(const CubArgs& A, const double2* J21, int mx, int 
 __global__ void k_cub_far(CubArgs A, const double* __restrict__ gw, const double* __restrict__ gu,
                           const double* __restrict__ gv, int Np, int n_medium, double2* __restrict__ G) {
   __shared__ double w[16], u[16], v[16];
+  __shared__ double X[6][16 * 3];  // quadrature points of the six faces
   if (threadIdx.x < Np) {
     w[threadIdx.x] = gw[threadIdx.x];
     u[threadIdx.x] = gu[threadIdx.x];
     v[threadIdx.x] = gv[threadIdx.x];
   }
+  __syncthreads();
+  for (int f = 0; f < 6; ++f) face_points(A, f, u, v, Np, X[f], threadIdx.x, blockDim.x);
   __syncthreads();
   const long long V = (long long)A.L * A.M * A.N;
   const int lane = threadIdx.x & 31;
@@ -245,7 +254,8 @@ __global__ void k_cub_far(CubArgs A, const double* __restrict__ gw, const double
     if (mx < n_medium && my < n_medium && mz < n_medium) continue;
     const double rm[3] = {mx * A.dx, my * A.dx, mz * A.dx};
     double2 J21[21];
-    for (int p = 0; p < 21; ++p) J21[p] = warp_sum2(face_pair_sum(A, w, u, v, Np, c_pair_obs[p], c_pair_src[p], rm, lane, 32));
+    for (int p = 0; p < 21; ++p)
+      J21[p] = warp_sum2(face_pair_sum(X[c_pair_obs[p]], X[c_pair_src[p]], w, Np, A.ko, rm, lane, 32));
     if (lane == 0) finish_offset(A, J21, mx, my, mz, false, G, V, off);
   }
 }
@@ -257,6 +267,8 @@ __global__ void k_cub_region(CubArgs A, const double* __restrict__ gw, const dou
   double* w = sh;
   double* u = sh + Np;
   double* v = sh + 2 * Np;
+  double* P = sh + 3 * Np;  // points of the observation face, [i][3]
+  double* Q = P + 3 * Np;   // points of the source face
   for (int i = threadIdx.x; i < Np; i += blockDim.x) {
     w[i] = gw[i];
     u[i] = gu[i];
@@ -264,10 +276,13 @@ __global__ void k_cub_region(CubArgs A, const double* __restrict__ gw, const dou
   }
   __syncthreads();
   const int pair = blockIdx.y;
+  face_points(A, c_pair_obs[pair], u, v, Np, P, threadIdx.x, blockDim.x);
+  face_points(A, c_pair_src[pair], u, v, Np, Q, threadIdx.x, blockDim.x);
+  __syncthreads();
   const int o = blockIdx.x;
   const int mx = o % nr, my = (o / nr) % nr, mz = o / (nr * nr);
   const double rm[3] = {mx * A.dx, my * A.dx, mz * A.dx};
-  double2 acc = face_pair_sum(A, w, u, v, Np, c_pair_obs[pair], c_pair_src[pair], rm, threadIdx.x, blockDim.x);
+  double2 acc = face_pair_sum(P, Q, w, Np, A.ko, rm, threadIdx.x, blockDim.x);
   acc = warp_sum2(acc);
   __shared__ double2 ws[32];
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
@@ -536,8 +551,11 @@ static int assemble_toeplitz(int L, int M, int N, double dx, double ko, const do
     DBuf J21;
     MARIE_TRY(J21.alloc((size_t)nO * 21 * sizeof(double2), st));
     dim3 grid(nO, 21);
-    k_cub_region<<<grid, 256, 3 * R.Np * sizeof(double), st>>>(A, R.w.as<double>(), R.u.as<double>(), R.v.as<double>(),
-                                                            R.Np, nr, J21.as<double2>());
+    const size_t smem = 9 * R.Np * sizeof(double);  // w, u, v and the two faces' points
+    if (smem > 48 * 1024)
+      MARIE_CUDA_TRY(cudaFuncSetAttribute(k_cub_region, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_cub_region<<<grid, 256, smem, st>>>(A, R.w.as<double>(), R.u.as<double>(), R.v.as<double>(), R.Np, nr,
+                                          J21.as<double2>());
     count_launch();
     MARIE_CUDA_TRY(cudaGetLastError());
     k_region_finish<<<(nO + 127) / 128, 128, 0, st>>>(A, J21.as<double2>(), nr, pass == 1, G);
