@@ -612,31 +612,25 @@ __constant__ int c_kop_obs[12] = {0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5};
 __constant__ int c_kop_src[12] = {0, 1, 0, 1, 2, 3, 2, 3, 4, 5, 4, 5};
 __constant__ double c_kop_sign[12] = {1, -1, -1, 1, 1, -1, -1, 1, 1, -1, -1, 1};
 
-// sum over point pairs of w_p w_q G(R) (r_p - r_q) for one face pair
-__device__ void kop_pair_sum(const CubArgs& A, const double* __restrict__ w, const double* __restrict__ u,
-                             const double* __restrict__ v, int Np, int io, int is, const double rm[3], int lane,
-                             int nl, double2 out[3]) {
+// sum over point pairs of w_p w_q G(R) (r_p - r_q) for one face pair (points
+// of the observation face P and of the source face Q in shared memory, [i][3];
+// R and 1/R^3 from one reciprocal square root, as in face_pair_sum)
+__device__ void kop_pair_sum(const double* __restrict__ P, const double* __restrict__ Q,
+                             const double* __restrict__ w, int Np, double ko, const double rm[3], int lane, int nl,
+                             double2 out[3]) {
   out[0] = out[1] = out[2] = mk<double2>(0, 0);
-  const double* po = A.face_o[io];
-  const double* pa = A.face_a[io];
-  const double* pb = A.face_b[io];
-  const double* qo = A.face_o[is];
-  const double* qa = A.face_a[is];
-  const double* qb = A.face_b[is];
-  const long long tot = (long long)Np * Np;
-  for (long long t = lane; t < tot; t += nl) {
-    const int ip = (int)(t / Np), iq = (int)(t - (long long)ip * Np);
-    const double up = u[ip], vp = v[ip], uq = u[iq], vq = v[iq];
+  const int tot = Np * Np;
+  for (int t = lane; t < tot; t += nl) {
+    const int ip = t / Np, iq = t - ip * Np;
     double d[3];
-    for (int c = 0; c < 3; ++c)
-      d[c] = (po[c] + pa[c] * up + pb[c] * vp + rm[c]) - (qo[c] + qa[c] * uq + qb[c] * vq);
-    const double R = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    const double kR = A.ko * R;
+    for (int c = 0; c < 3; ++c) d[c] = (P[3 * ip + c] + rm[c]) - Q[3 * iq + c];
+    const double R2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const double Ri = rsqrt(R2);
+    const double kR = ko * (R2 * Ri);
     double sn, cs;
     sincos(kR, &sn, &cs);
     // 1 - exp(-j kR) (1 + j kR) = (1 - cs - kR sn) - j (kR cs - sn)
-    const double R3 = R * R * R;
-    const double wt = w[ip] * w[iq] / R3;
+    const double wt = w[ip] * w[iq] * (Ri * Ri * Ri);
     const double gr = wt * (1.0 - cs - kR * sn), gi = -wt * (kR * cs - sn);
     for (int c = 0; c < 3; ++c) {
       out[c].x += gr * d[c];
@@ -649,11 +643,14 @@ __device__ void kop_pair_sum(const CubArgs& A, const double* __restrict__ w, con
 __global__ void k_kop_far(CubArgs A, const double* __restrict__ gw, const double* __restrict__ gu,
                           const double* __restrict__ gv, int Np, int n_medium, double2* __restrict__ K) {
   __shared__ double w[16], u[16], v[16];
+  __shared__ double X[6][16 * 3];  // quadrature points of the six faces
   if (threadIdx.x < Np) {
     w[threadIdx.x] = gw[threadIdx.x];
     u[threadIdx.x] = gu[threadIdx.x];
     v[threadIdx.x] = gv[threadIdx.x];
   }
+  __syncthreads();
+  for (int f = 0; f < 6; ++f) face_points(A, f, u, v, Np, X[f], threadIdx.x, blockDim.x);
   __syncthreads();
   const long long V = (long long)A.L * A.M * A.N;
   const int lane = threadIdx.x & 31;
@@ -668,7 +665,7 @@ __global__ void k_kop_far(CubArgs A, const double* __restrict__ gw, const double
     double2 acc[3] = {mk<double2>(0, 0), mk<double2>(0, 0), mk<double2>(0, 0)};
     for (int p = 0; p < 12; ++p) {
       double2 o[3];
-      kop_pair_sum(A, w, u, v, Np, c_kop_obs[p], c_kop_src[p], rm, lane, 32, o);
+      kop_pair_sum(X[c_kop_obs[p]], X[c_kop_src[p]], w, Np, A.ko, rm, lane, 32, o);
       for (int c = 0; c < 3; ++c) acc[c] = cadd(acc[c], cscale(o[c], c_kop_sign[p]));
     }
     for (int c = 0; c < 3; ++c) acc[c] = warp_sum2(acc[c]);
@@ -685,6 +682,8 @@ __global__ void k_kop_region(CubArgs A, const double* __restrict__ gw, const dou
   double* w = sh;
   double* u = sh + Np;
   double* v = sh + 2 * Np;
+  double* P = sh + 3 * Np;  // points of the observation face, [i][3]
+  double* Q = P + 3 * Np;   // points of the source face
   for (int i = threadIdx.x; i < Np; i += blockDim.x) {
     w[i] = gw[i];
     u[i] = gu[i];
@@ -692,13 +691,16 @@ __global__ void k_kop_region(CubArgs A, const double* __restrict__ gw, const dou
   }
   __syncthreads();
   const int pair = blockIdx.y;
+  const int io = near ? c_pair_obs[pair] : c_kop_obs[pair];
+  const int is = near ? c_pair_src[pair] : c_kop_src[pair];
+  face_points(A, io, u, v, Np, P, threadIdx.x, blockDim.x);
+  face_points(A, is, u, v, Np, Q, threadIdx.x, blockDim.x);
+  __syncthreads();
   const int o = blockIdx.x;
   const int mx = o % nr, my = (o / nr) % nr, mz = o / (nr * nr);
   const double rm[3] = {mx * A.dx, my * A.dx, mz * A.dx};
-  const int io = near ? c_pair_obs[pair] : c_kop_obs[pair];
-  const int is = near ? c_pair_src[pair] : c_kop_src[pair];
   double2 acc[3];
-  kop_pair_sum(A, w, u, v, Np, io, is, rm, threadIdx.x, blockDim.x, acc);
+  kop_pair_sum(P, Q, w, Np, A.ko, rm, threadIdx.x, blockDim.x, acc);
   __shared__ double2 ws[3][32];
   for (int c = 0; c < 3; ++c) {
     const double2 r = warp_sum2(acc[c]);
@@ -823,8 +825,11 @@ static int assemble_toeplitz_k(int L, int M, int N, double dx, double ko, double
     DBuf I;
     MARIE_TRY(I.alloc((size_t)nO * npairs * 3 * sizeof(double2), st));
     dim3 grid(nO, npairs);
-    k_kop_region<<<grid, 256, 3 * R.Np * sizeof(double), st>>>(A, R.w.as<double>(), R.u.as<double>(),
-                                                              R.v.as<double>(), R.Np, nr, near, I.as<double2>());
+    const size_t smem = 9 * R.Np * sizeof(double);  // w, u, v and the two faces' points
+    if (smem > 48 * 1024)
+      MARIE_CUDA_TRY(cudaFuncSetAttribute(k_kop_region, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_kop_region<<<grid, 256, smem, st>>>(A, R.w.as<double>(), R.u.as<double>(), R.v.as<double>(), R.Np, nr, near,
+                                          I.as<double2>());
     count_launch();
     MARIE_CUDA_TRY(cudaGetLastError());
     k_kop_finish<<<(nO + 127) / 128, 128, 0, st>>>(A, I.as<double2>(), nr, near, K);
