@@ -296,6 +296,11 @@ int marie_mv_AN_cufft(marie_plan* plan, const double* JIn0, const double* Mr, co
  * forward, z multiply, y inverse, x inverse) over the matvecs run since the
  * previous call, then resets and switches recording on or off. */
 int64_t marie_launch_count(void);
+/* Per-call device buffers come from a library-owned memory pool per device
+ * that keeps freed blocks for the next call (no reference counterpart).  This
+ * returns the cached blocks to the device (after synchronising it); plans and
+ * their operators are unaffected. */
+int marie_release_cached_memory(void);
 /* Schedule autotuner (no counterpart in the reference): times the plan's FP32
  * matvec for every candidate schedule (fuse: fused x+y cluster passes or the
  * five-pass form; fvar: default or narrow radix schedule of the fused x/y

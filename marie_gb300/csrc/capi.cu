@@ -783,6 +783,21 @@ int marie_plan_set_inner_restart(marie_plan* p, int restart) {
   return MARIE_OK;
 }
 
+int marie_release_cached_memory(void) {
+  // blocks freed by finished calls go back to the device; blocks in use stay
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  for (auto& kv : g_pools) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaSetDevice(kv.first);
+    cudaDeviceSynchronize();
+    const cudaError_t e = cudaMemPoolTrimTo(kv.second, 0);
+    cudaSetDevice(dev);
+    if (e != cudaSuccess) return set_error(MARIE_ECUDA, "trimming the memory pool failed: %s", cudaGetErrorString(e));
+  }
+  return MARIE_OK;
+}
+
 int64_t marie_launch_count(void) { return g_launches.load(); }
 
 void marie_inject_alloc_failure(int64_t nth) { g_fail_alloc_in.store(nth > 0 ? nth : 0); }

@@ -102,6 +102,11 @@ def _out(shape, like_cuda: bool, dtype=np.complex128):
     return C.c_void_p(arr.ctypes.data), arr
 
 
+def release_cached_memory():
+    """Returns the device memory cached by the library's pool between calls."""
+    check(_lib.load().marie_release_cached_memory())
+
+
 def _sync():
     if torch is not None and torch.cuda.is_available():
         torch.cuda.current_stream().synchronize()

@@ -105,3 +105,26 @@ def test_other_solvers_flags_zero_rhs_and_allocation_failures(solver, precision)
             lib.marie_inject_alloc_failure(0)
     out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8, solver=solver)
     assert out[1] == 0 and out[2] <= 1e-8
+
+
+def test_release_cached_memory(cuda):
+    """The pool's cached blocks go back to the device and later calls still work."""
+    import torch
+
+    import marie_gb300 as mg
+
+    L, dx = 16, 5e-3
+    r = vo.grid(L, L, L, dx)
+    er = np.ones((L, L, L), complex)
+    er[np.sum(r * r, axis=3) < 0.035**2] = 50 - 30j
+    er = np.asfortranarray(er)
+    em = vo.EMconstants(298e6)
+    E, _ = vo.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
+    op = mg.Operator.assemble(L, L, L, dx, 298e6, precision="mixed")
+    J1 = mg.JVIE_Solver(np.asfortranarray(E), er, r, 298e6, op, tol=1e-6, solver="G")[0]
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    mg.release_cached_memory()
+    assert torch.cuda.mem_get_info()[0] >= free0
+    J2 = mg.JVIE_Solver(np.asfortranarray(E), er, r, 298e6, op, tol=1e-6, solver="G")[0]
+    assert np.array_equal(J1, J2)
