@@ -10,10 +10,11 @@ from .vie import (EMconstants, E_field_Nop, JVIE_Solver, JVIE_Solver_batch, JVIE
                   pgmres, pgmresDR, singular_integrals, fVIEsolver_Assembly, jvie2solver, supported_size,
                   release_cached_memory)
 from .bodies import Import_RHBM  # noqa: F401
+from .opcache import OperatorCache, ScheduleCache  # noqa: F401
 
 __all__ = ["EMconstants", "E_field_Nop", "JVIE_Solver", "JVIE_Solver_batch", "Operator", "PlaneWave_Excitation",
            "Scat_Solver",
            "Dipole_Excitation", "H_field_Kop", "bicgstab", "getOPERATORS", "mv_AN", "mv_K", "mv_L", "mv_N", "pgmres", "pgmresDR",
            "singular_integrals", "fVIEsolver_Assembly", "jvie2solver", "supported_size", "Import_RHBM",
-           "release_cached_memory",
+           "release_cached_memory", "OperatorCache", "ScheduleCache",
            "MarieError", "load"]

@@ -914,6 +914,7 @@ int marie_get_operators(const double* r, int64_t L, int64_t M, int64_t N, double
   if (op != 'N' && op != 'K') return set_error(MARIE_EINVAL, "op must be 'N' or 'K'");
   if (type != 'F' && type != 'C' && type != 'T') return set_error(MARIE_EINVAL, "type must be 'F', 'C' or 'T'");
   if (L < 2) return set_error(MARIE_EINVAL, "L must be >= 2 to read dx from r");
+  MARIE_TRACE("getOPERATORS");
   if (type != 'T' && (!fft_length_supported((int)(2 * L)) || !fft_length_supported((int)(2 * M)) ||
                       !fft_length_supported((int)(2 * N))))
     return set_error(MARIE_EUNSUPPORTED, "padded FFT length not supported");
@@ -941,6 +942,7 @@ int marie_get_operators(const double* r, int64_t L, int64_t M, int64_t N, double
 int marie_plan_assemble(marie_plan* p, double dx, double freq, char singular, const double* singular_values) {
   if (!p) return set_error(MARIE_EINVAL, "NULL plan");
   if (!(dx > 0) || !(freq > 0)) return set_error(MARIE_EINVAL, "dx and freq must be positive");
+  MARIE_TRACE("getOPERATORS N");
   DBuf F;
   MARIE_TRY(F.alloc((size_t)48 * p->d.V * sizeof(double2), p->stream));
   MARIE_TRY(assemble_operator_device(p->d.L, p->d.M, p->d.N, dx, freq, singular, singular_values, 'F',
@@ -951,6 +953,7 @@ int marie_plan_assemble(marie_plan* p, double dx, double freq, char singular, co
 int marie_plan_assemble_k(marie_plan* p, double dx, double freq) {
   if (!p) return set_error(MARIE_EINVAL, "NULL plan");
   if (!(dx > 0) || !(freq > 0)) return set_error(MARIE_EINVAL, "dx and freq must be positive");
+  MARIE_TRACE("getOPERATORS K");
   DBuf F;
   MARIE_TRY(F.alloc((size_t)24 * p->d.V * sizeof(double2), p->stream));
   MARIE_TRY(assemble_k_device(p->d.L, p->d.M, p->d.N, dx, freq, 'F', F.as<double2>(), p->stream));

@@ -217,6 +217,7 @@ bool finite(cd v) { return std::isfinite(v.real()) && std::isfinite(v.imag()); }
 int bicgstab(marie_plan* p, const DevOp& A, const DevOp* M1, const DevOp* M2, const double2* b, long long n,
              double tol, int maxit, const double2* x0, double2* x, BicgResult& out) {
   if (maxit < 0) return set_error(MARIE_EINVAL, "maxit must be >= 0");
+  MARIE_TRACE("bicgstab");
   cudaStream_t st = p->stream;
   const bool precond = M1 || M2;
   BiWork W;

@@ -304,6 +304,7 @@ int gmres_dr(marie_plan* p, const DevOp& A, const DevOp* L1, const DevOp* L2, co
              double2* x, GmresResult& out) {
   if (restart < 2) return set_error(MARIE_EINVAL, "pgmresDR needs restart >= 2");
   if (maxit < 0) return set_error(MARIE_EINVAL, "maxit must be >= 0");
+  MARIE_TRACE("pgmresDR");
   // pgmresDR.m:55-60
   if (ritz < 1)
     ritz = std::min(10, (int)std::floor(restart / 2.0 + 0.5));

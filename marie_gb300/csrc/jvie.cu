@@ -413,6 +413,7 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
         }
       }
       if (!any) break;
+      MARIE_TRACE("refinement step");
       std::vector<GmresResult> ri;
       const int m_in = p->inner_restart > 0 ? p->inner_restart : inner_it;
       MARIE_TRY(gmres_batch(p, A32, L1m, R1m, Rr, n, n, S_exc, m_in, inner_tol, outer_it, D, n, ri, true, &act,
@@ -696,6 +697,7 @@ int marie_scat_solver(marie_plan* p, const double* Einc, const double* Hinc, dou
                       double* Sout, double* Eout, double* Bout, double* Gsar, double* Pabs) {
   if (!p || !Einc || !eps_r || !sigma_e || !rho || !Jout) return set_error(MARIE_EINVAL, "NULL argument");
   if (!(dx > 0) || !(freq > 0)) return set_error(MARIE_EINVAL, "dx and freq must be positive");
+  MARIE_TRACE("Scat_Solver");
   cudaStream_t st = p->stream;
   const long long V = p->d.V;
   const double Gram = dx * dx * dx;
@@ -783,6 +785,7 @@ int marie_jvie_solve(marie_plan* p, const double* Einc, const double* e_r, doubl
   if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator");
   if (!(dx > 0) || !(freq > 0)) return set_error(MARIE_EINVAL, "dx and freq must be positive");
   MARIE_TRY(clamp_args(tol, form, precond, inner_it, outer_it));
+  MARIE_TRACE("JVIE_Solver");
   SolverArgs sa;
   sa.solver = solver;
   sa.max_it = max_it;
@@ -829,6 +832,7 @@ int marie_jvie2solver(marie_plan* p, const int64_t* idx, int64_t n_idx, const do
   if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator");
   if (!(tol > 0)) return set_error(MARIE_EINVAL, "tol must be positive");
   if (max_it < 1) return set_error(MARIE_EINVAL, "max_it must be >= 1");
+  MARIE_TRACE("jvie2solver");
   const auto t0 = std::chrono::steady_clock::now();
   cudaStream_t st = p->stream;
   const long long V = p->d.V, n = n_idx;

@@ -442,6 +442,7 @@ extern "C" int marie_pgmres(marie_plan* p, marie_op_fn A, void* A_ctx, const dou
                             int* flag, double* relres, int* iter, double* resvec, int64_t resvec_cap,
                             int64_t* resvec_len) {
   if (!p || !b || !x || n < 1) return set_error(MARIE_EINVAL, "NULL argument or n < 1");
+  MARIE_TRACE("pgmres");
   // User operators run outside the plan's stream: finish the plan's work
   // before handing them x; they return with y complete.
   auto wrap = [p](marie_op_fn f, void* ctx, long long nn) -> DevOp {

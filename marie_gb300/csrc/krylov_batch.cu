@@ -689,6 +689,7 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
       any = any || active[s];
     }
     if (!any) break;
+    MARIE_TRACE("pgmres restart cycle");
     MARIE_CUDA_TRY(cudaMemcpyAsync(W.stop.p, stop.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
     if (use_graph && cycles >= 1) {
       if (!W.exec) {

@@ -8,6 +8,7 @@
 
 #include "common.cuh"
 #include "matvec_kernels.cuh"
+#include "trace.h"
 
 struct marie_plan {
   marie::Dims d{};

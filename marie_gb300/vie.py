@@ -43,7 +43,7 @@ from typing import Callable, Optional
 
 import numpy as np
 
-from . import _lib
+from . import _lib, solvelog
 from ._lib import MARIE_FP32, MARIE_FP64, MARIE_MIXED, check
 
 try:  # torch is only needed for device-resident arrays
@@ -537,7 +537,7 @@ def bicgstab(A, b, tol=1e-6, maxit=None, M1=None, M2=None, x0=None):
 # JVIE_Solver
 # ---------------------------------------------------------------------------
 def JVIE_Solver(Einc, e_r, r, freq, fN, tol=None, form=None, solver=None, precond=None, max_it=None, inner_it=None,
-                outer_it=None, ritz=None, gpu_flag=1, logfile=None, precision=None):
+                outer_it=None, ritz=None, gpu_flag=1, logfile=None, precision=None, runlog=None):
     """JVIE_Solver.m on the device: solver 'G' (pgmres), 'D' (pgmresDR) or,
     as in the reference, anything else (the default) 'B' (bicgstab).
 
@@ -545,7 +545,12 @@ def JVIE_Solver(Einc, e_r, r, freq, fN, tol=None, form=None, solver=None, precon
     reference arithmetic), 'fp32', or 'mixed' (FP32 circulant matvec inside FP64
     Krylov iterations with FP64 iterative refinement); defaults to the
     Operator's.  Returns (Je, flag, relres, iter, resvec, solvert): iter is
-    [inner, outer] for 'G' and 'D' and the half-step count for 'B'."""
+    [inner, outer] for 'G' and 'D' and the half-step count for 'B'.
+
+    logfile: the reference's solve summary is appended to this path (1:
+    standard output; None: not written).  runlog: a .jsonl path that receives
+    one JSON record of the solve."""
+    tstart = time.perf_counter()
     tol = 1e-3 if tol is None else tol
     form = 2 if form is None else form
     solver = solver if solver in ("G", "D") else "B"
@@ -579,10 +584,35 @@ def JVIE_Solver(Einc, e_r, r, freq, fN, tol=None, form=None, solver=None, precon
                                        C.byref(relres), it, resvec.ctypes.data_as(_lib._dp), cap, C.byref(rlen),
                                        C.byref(solvert)))
         iters = it[0] if solver == "B" else [int(it[0]), int(it[1])]
-        return Je, flag.value, relres.value, iters, resvec[:min(rlen.value, cap)], solvert.value
+        resvec = resvec[:min(rlen.value, cap)]
+        if logfile is not None or runlog is not None:
+            _log_solve(logfile, runlog, e_r, dx, freq, solver, pc, opr, tol, max_it, inner_it, outer_it, ritz,
+                       flag.value, relres.value, iters, resvec, solvert.value, time.perf_counter() - tstart)
+        return Je, flag.value, relres.value, iters, resvec, solvert.value
     finally:
         if tmp:
             opr.close()
+
+
+def _n_scatterer(e_r) -> int:
+    """length(idxS): voxels with |e_r - 1| > 1e-12 (JVIE_Solver.m:135)."""
+    if _is_cuda(e_r):
+        return int(((e_r - 1).abs() > 1e-12).sum().item())
+    return int(np.count_nonzero(np.abs(np.asarray(e_r) - 1) > 1e-12))
+
+
+def _log_solve(logfile, runlog, e_r, dx, freq, solver, pc, opr, tol, max_it, inner_it, outer_it, ritz, flag, relres,
+               iters, resvec, solvert, elapsed):
+    L, M, N = e_r.shape
+    ns = _n_scatterer(e_r)
+    precond = pc.decode().strip("\0")
+    solvelog.write_solve_log(logfile, L=L, M=M, N=N, dx=dx, n_scat=ns, freq=freq, fN_bytes=8 * L * M * N * 6 * 16,
+                             solver=solver, precond=precond, inner_it=inner_it, ritz=ritz, solvert=solvert,
+                             resvec=resvec, flag=flag, relres=relres, elapsed=elapsed)
+    prec = {MARIE_FP64: "fp64", MARIE_FP32: "fp32", MARIE_MIXED: "mixed"}.get(opr.precision, str(opr.precision))
+    solvelog.write_run_record(runlog, solvelog.run_record(L, M, N, dx, ns, freq, solver, precond, prec, tol,
+                                                          inner_it, outer_it, max_it, flag, relres, iters, resvec,
+                                                          solvert, elapsed))
 
 
 def Scat_Solver(Einc, Hinc, freq, r, epsilon_r, sigma_e, rho, tol=None, fN=None, fK=None, form=None, solver=None,
@@ -591,7 +621,10 @@ def Scat_Solver(Einc, Hinc, freq, r, epsilon_r, sigma_e, rho, tol=None, fN=None,
     """Scat_Solver.m on the device: the J-VIE current, SAR, total E, B = mu0 H,
     global SAR and absorbed power.  fN / fK: an Operator holding them (N and
     K on one plan), or None to assemble both.  Returns (Jout, Sout, Eout, Bout,
-    Gsar, Pabs, op) where op is the Operator that holds fN and fK."""
+    Gsar, Pabs, op) where op is the Operator that holds fN and fK.  logfile:
+    the closing lines with the overall time are appended to it (1: standard
+    output)."""
+    tstart = time.perf_counter()
     tol = 1e-3 if tol is None else tol
     form = 2 if form is None else form
     solver = solver if solver in ("G", "D") else "B"
@@ -627,6 +660,7 @@ def Scat_Solver(Einc, Hinc, freq, r, epsilon_r, sigma_e, rho, tol=None, fN=None,
     check(opr.lib.marie_scat_solver(opr.plan, ep, hp, dx, float(freq), epsp, sp_, rp_, float(tol), int(form),
                                     solver.encode(), pc, int(max_it), int(inner_it), int(outer_it), int(ritz), jp, spo,
                                     eo, bo, C.byref(gsar), C.byref(pabs)))
+    solvelog.write_overall_log(logfile, time.perf_counter() - tstart)
     return Jout, Sout, Eout, Bout, gsar.value, pabs.value, opr
 
 
