@@ -219,3 +219,30 @@ def test_autotuner_candidates_all_match_oracle(shape):
         out = mg.mv_AN(J, op, Mr, Mc, 0.2, "notransp", idx, precision="fp32")
         assert relerr(out, ref) < TOL["fp32"], (f, fv, z)
     op.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_transpose_is_Mc_similarity_on_device(precision):
+    """N is complex symmetric, so A^T = Gram*Mr - N*Mc = Mc^-1 A Mc: the
+    'transp' flag (A^T x = conj(A^H conj(x))) against 'notransp' on Mc x, for
+    a random parity-symmetric circulant and for the device-assembled operator.
+    Two products and a division by Mc (|Mc| >= 0.08 here): FP32 bar 1e-4."""
+    import marie_gb300 as mg
+
+    L, M, N, dx = 12, 20, 16, 5e-3  # FFT lengths 24, 40, 32
+    rng = np.random.default_rng(11)
+    Mr = np.asfortranarray(5 + 40 * rng.random((L, M, N)) - 20j * rng.random((L, M, N)))
+    Mc = np.asfortranarray((Mr - 1) / Mr)
+    V = L * M * N
+    idxS = np.flatnonzero(rng.random(V) < 0.6) + 1
+    idx = np.concatenate([idxS, V + idxS, 2 * V + idxS]).astype(np.int64)
+    x = rng.standard_normal(idx.size) + 1j * rng.standard_normal(idx.size)
+    mc = Mc.reshape(-1, order="F")[(idx - 1) % V]
+    fN = problem(L, M, N, seed=4, physical=True)[0]
+    tol = {"fp64": 1e-12, "fp32": 1e-4}[precision]
+    for op, gram in ((mg.Operator.from_array(fN, precision="mixed"), 0.4),
+                     (mg.Operator.assemble(L, M, N, dx, 298e6, precision="mixed"), dx**3)):
+        ATx = np.conj(mg.mv_AN(np.conj(x), op, Mr, Mc, gram, "transp", idx, precision=precision))
+        sim = mg.mv_AN(mc * x, op, Mr, Mc, gram, "notransp", idx, precision=precision) / mc
+        assert relerr(sim, ATx) < tol
+        op.close()

@@ -129,6 +129,24 @@ def test_mv_AN_transp_is_hermitian_adjoint():
     assert abs(lhs - rhs) < 1e-12 * abs(lhs)
 
 
+def test_mv_AN_transpose_is_Mc_similarity():
+    """A = Gram*Mr - Mc*N with N complex symmetric (a physical circulant), so
+    A^T = Gram*Mr - N*Mc = Mc^-1 A Mc; A^T x = conj(A^H conj(x)) through the
+    'transp' flag."""
+    L, M, N = 4, 5, 3
+    _, Mr, Mc, idx, x = _random_problem(L, M, N, seed=2)
+    rng = np.random.default_rng(7)
+    G = rng.standard_normal((L, M, N, 6)) + 1j * rng.standard_normal((L, M, N, 6))
+    G[0, :, :, [1, 2]] = 0
+    G[:, 0, :, [1, 4]] = 0
+    G[:, :, 0, [2, 4]] = 0
+    fN = vo.fft_operator(vo.circulant_nop(G))
+    mc = Mc.reshape(-1, order="F")[(idx - 1) % (L * M * N)]
+    ATx = np.conj(vo.mv_AN(np.conj(x), fN, Mr, Mc, 0.4, "transp", idx))
+    sim = vo.mv_AN(mc * x, fN, Mr, Mc, 0.4, "notransp", idx) / mc
+    assert np.max(np.abs(ATx - sim)) < 1e-12 * np.max(np.abs(ATx))
+
+
 def test_pgmres_dense_system_matches_solve():
     rng = np.random.default_rng(3)
     n = 40
