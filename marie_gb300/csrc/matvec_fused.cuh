@@ -76,14 +76,23 @@ k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Pro
   cg::cluster_group cluster = cg::this_cluster();
   const int q = (int)cluster.block_rank();
   const int plane = blockIdx.x / CS;  // z + N*c
-  const IO* Jr = J + blockIdx.y * js;
   constexpr int EX = FX::E, R0X = FX::R0;
   const int tx = threadIdx.x % FX::T, sx = threadIdx.x / FX::T;
+  // the twiddles are staged before the wait for the previous pass; the index
+  // map, the skip mask, the prologue factors and J are read after it (the
+  // kernel just before may have written any of them)
+  for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
+  pdl_wait();
+  if (rhs_skipped(d, blockIdx.y)) return;  // uniform over the cluster, before any cluster barrier
+  const int* invw = after_wait(inv);
+  const IO* Jr = after_wait(J) + blockIdx.y * js;
+  Prologue prw = pro;
+  prw.pre = after_wait(pro.pre);
   // DOF indices of one sweep of rows (the zero half of each row is skipped)
   auto load_idx = [&](int* kk, int row0) {
     const int yl = row0 + sx;
     const bool valid = yl < C::RY;
-    const int* invr = inv + (long long)L * (q * C::RY + yl + (long long)M * plane);
+    const int* invr = invw + (long long)L * (q * C::RY + yl + (long long)M * plane);
 #pragma unroll
     for (int b = 0; b < EX / R0X; ++b)
 #pragma unroll
@@ -92,12 +101,6 @@ k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Pro
         kk[b * R0X + r] = (valid && r < R0X / 2 && p < L) ? invr[p] : -1;
       }
   };
-  // the twiddles are staged before the wait for the previous pass; the index
-  // map, the skip mask and J are read after it (a caller may have built the
-  // map in the kernel just before)
-  for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
-  pdl_wait();
-  if (rhs_skipped(d, blockIdx.y)) return;  // uniform over the cluster, before any cluster barrier
   int kk[EX];
   load_idx(kk, 0);
   __syncthreads();  // x twiddles staged
@@ -114,7 +117,7 @@ k_xyfwd(const IO* __restrict__ J, long long js, const int* __restrict__ inv, Pro
       V reg[E];
       if (row0 > 0) load_idx(kk, row0);
 #pragma unroll
-      for (int i = 0; i < E; ++i) reg[i] = kk[i] >= 0 ? cvt<V>(prologue_in(Jr, pro, kk[i])) : mk<V>(0, 0);
+      for (int i = 0; i < E; ++i) reg[i] = kk[i] >= 0 ? cvt<V>(prologue_in(Jr, prw, kk[i])) : mk<V>(0, 0);
       FX::run_half(reg, xb + s * C::ROWP, SAddr(1, true), t, twx_s);
       if (row0 == 0) cluster_wait();  // every CTA of the cluster runs before remote stores
       if (valid) {
@@ -194,7 +197,13 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const IO* __restrict__ J, l
   {
     constexpr int E = FYI::E, R0 = FYI::R0, RL = FYI::RL;
     const int s = threadIdx.x % C::SY, t = threadIdx.x / C::SY;
-    const V* Bp = B + blockIdx.y * bs + (long long)plane * NM * NL + q * C::CW;
+    // twiddles staged before the wait for the spectrum of the previous pass;
+    // the spectrum is read after it, through L2 (the z pass writes it while
+    // this kernel's first CTAs are already resident)
+    for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
+    for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
+    pdl_wait();
+    const V* Bp = after_wait(B) + blockIdx.y * bs + (long long)plane * NM * NL + q * C::CW;
     auto load_cols = [&](V* reg, int c0) {
       const int col = c0 + s;
       const bool valid = col < C::CW;
@@ -202,12 +211,8 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const IO* __restrict__ J, l
       for (int b = 0; b < E / R0; ++b)
 #pragma unroll
         for (int r = 0; r < R0; ++r)
-          reg[b * R0 + r] = valid ? Bp[(long long)FYI::in_pos(t, b, r) * NL + col] : mk<V>(0, 0);
+          reg[b * R0 + r] = valid ? __ldcg(Bp + (long long)FYI::in_pos(t, b, r) * NL + col) : mk<V>(0, 0);
     };
-    // twiddles staged before the wait for the spectrum of the previous pass
-    for (int i = threadIdx.x; i < NL; i += blockDim.x) twx_s[i] = twx[i];
-    for (int i = threadIdx.x; i < NM; i += blockDim.x) twy_s[i] = twy[i];
-    pdl_wait();
     V reg[E];
     load_cols(reg, 0);
     __syncthreads();  // twiddles staged

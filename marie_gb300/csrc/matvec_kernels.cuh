@@ -44,6 +44,20 @@ __device__ __forceinline__ bool rhs_skipped(const Dims& d, int rhs) { return d.s
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// A pointer to data that the previous kernel writes, taken again after
+// pdl_wait through an opaque move.  A kernel parameter declared
+// `const T* __restrict__` tells the compiler that its data is fixed for the
+// kernel's lifetime, so it may schedule those loads before the wait or serve
+// them from the non-coherent read-only path; under programmatic dependent
+// launch the data changes during this kernel's lifetime.  Loads through the
+// returned pointer depend on the move (they cannot start before the wait)
+// and the pointer carries no __restrict__.
+template <typename P> __device__ __forceinline__ P* after_wait(P* p) {
+  unsigned long long v = reinterpret_cast<unsigned long long>(p);
+  asm volatile("mov.b64 %0, %0;" : "+l"(v)::"memory");
+  return reinterpret_cast<P*>(v);
+}
+
 // Epilogue: out[k] = A_k * J[k] - (conjout ? conj(v) : B_k * v)
 struct Epilogue {
   const double2* a;  // per-DOF, or null -> a_s
@@ -78,7 +92,7 @@ template <> struct EpiIO<float2> {
 };
 // J[k] with the prologue applied, in the precision of IO
 template <typename IO>
-__device__ __forceinline__ IO prologue_in(const IO* __restrict__ J, const Prologue& pro, int k) {
+__device__ __forceinline__ IO prologue_in(const IO* J, const Prologue& pro, int k) {
   IO jv = J[k];
   if (pro.conjin) jv.y = -jv.y;
   if (pro.pre) jv = cmul(cvt<IO>(pro.pre[k]), jv);
@@ -477,13 +491,14 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   }
   stage_twiddles(tw_s, tw, NZ);
   pdl_wait();  // the spectrum B is the previous pass's output
+  Bp = after_wait(Bp);
   V reg[E];
 #pragma unroll
   for (int b = 0; b < E / R0; ++b)
 #pragma unroll
     for (int r = 0; r < R0; ++r) {
       const int p = FF::in_pos(t, b, r);
-      reg[b * R0 + r] = (active && r < R0 / 2 && p < NH) ? Bp[p * plane + s] : mk<V>(0, 0);
+      reg[b * R0 + r] = (active && r < R0 / 2 && p < NH) ? __ldcg(Bp + p * plane + s) : mk<V>(0, 0);
     }
   __syncthreads();  // twiddles staged
   V* my = buf + c * BUF + s;

@@ -104,3 +104,34 @@ def test_solutions_meet_the_tolerance_in_fp64_full_size(c2, solver):
     air = np.ones(3 * L * M * N, bool)
     air[S["idxS3"] - 1] = False
     assert not np.any(Je.reshape(-1, order="F")[air])
+
+
+def test_largest_grid_adjoint_and_precision():
+    """The largest workload's grid, 256 x 192 x 160 voxels (512 x 384 x 320
+    FFT), with a 15 cm sphere (5.3 M DOFs): adjoint identity in FP64 and
+    FP32, and FP32 products within 1e-5 of FP64, repeated.  This grid once
+    showed the fused passes' first clusters, started early by programmatic
+    dependent launch, reading the spectrum before the z pass had written it
+    (wrong leading DOFs in three calls out of four)."""
+    import marie_gb300 as mg
+    from marie_gb300 import phantoms
+
+    Lc, Mc_, Nc = 256, 192, 160
+    r, er = phantoms.sphere(Lc, Mc_, Nc, DX, 0.15, 50.0, 0.5, FREQ)
+    V = Lc * Mc_ * Nc
+    idxS = np.flatnonzero(np.abs(er.reshape(-1, order="F") - 1) > 1e-12) + 1
+    S = {"Mr": np.ones_like(er), "Mc": np.asfortranarray((er - 1) / er), "Gram": DX**3,
+         "idxS3": np.concatenate([idxS, V + idxS, 2 * V + idxS]).astype(np.int64)}
+    op = mg.Operator.assemble(Lc, Mc_, Nc, DX, FREQ, precision="mixed")
+    try:
+        x, y = _vecs(S["idxS3"].size, 5)
+        for precision, tol in (("fp64", 1e-12), ("fp32", 1e-5)):
+            lhs = np.vdot(y, _A(op, S, x, "notransp", precision))
+            rhs = np.vdot(_A(op, S, y, "transp", precision), x)
+            assert abs(lhs - rhs) <= tol * abs(lhs)
+        for flag in ("notransp", "transp"):
+            ref = _A(op, S, x, flag, "fp64")
+            for _ in range(4):
+                assert relerr(_A(op, S, x, flag, "fp32"), ref) < 1e-5, flag
+    finally:
+        op.close()
