@@ -68,17 +68,36 @@ void* marie_plan_stream(marie_plan* plan);
  *   r:       L x M x N x 3 voxel centres (uniform spacing; dx = r[1]-r[0])
  *   type:    'F' FFT of the circulant (2L x 2M x 2N x 6, the default 'FFTofC'),
  *            'C' circulant (2L x 2M x 2N x 6), 'T' Toeplitz (L x M x N x 6)
- *   singular:'D' computes the weakly singular self/edge/vertex integrals on
- *            the device (converged 4-D quadrature); 'U' uses the five values
- *            in singular_values = {ST, EAc, EAo, VAc, VAo} (complex)
+ *   singular:'D' (the reference default 'DIRECTFN', getOPERATORS.m:39-41)
+ *            computes the weakly singular self/edge/vertex integrals on the
+ *            device with DIRECTFN at Np_1D = 20 (assembly_nop.m:16,96-98);
+ *            'C' uses a converged 4-D quadrature instead (not a reference
+ *            method; differs from DIRECTFN@20 by up to 3.4e-5 relative);
+ *            'U' uses the five values in singular_values = {ST, EAc, EAo,
+ *            VAc, VAo} (complex).  'E' ('DEMCEM') is not built: MARIE_EINVAL.
  *   op_out:  complex output, host or device.
  * Component order [xx, xy, xz, yy, yz, zz] as vector_projection.m:15-22. */
 int marie_get_operators(const double* r, int64_t L, int64_t M, int64_t N, double f, char op,
                         char type, char singular, const double* singular_values, double* op_out);
 
-/* The five singular integrals {ST, EAc, EAo, VAc, VAo} for voxel size dx and
- * wavenumber ko (replaces singular_st/ea/va.m with singular='DIRECTFN'). */
+/* The five singular integrals {ST, EAc, EAo, VAc, VAo} (complex, out10 =
+ * 5 x (re, im)) for cubic voxels of edge dx and wavenumber ko: replaces
+ * singular_st.m / singular_ea.m / singular_va.m with method 'DIRECTFN' at
+ * Np_1D = 20, as assembly_nop.m:96-98 calls them. */
 int marie_singular_integrals(double ko, double dx, double* out10);
+/* The same with the method ('D' DIRECTFN, 'C' converged quadrature) and its
+ * order np_1d (0: 20 for 'D', 32 for 'C'; DIRECTFN takes 1..64). */
+int marie_singular_integrals_ex(double ko, double dx, char method, int np_1d, double* out10);
+/* One call of a DIRECTFN core for constant basis functions on a triangle
+ * pair, with the MEX gateway's arguments (vertices: 3 x kind-count doubles):
+ *   kind 'S': mexdirectfn_ws_st_const(r1, r2, r3, ko, Np_1D)
+ *             (mexcubatures/directfn_ws_st_const_mex.cpp:47)
+ *   kind 'E': mexdirectfn_ws_ea_const(r1, r2, r3, r4, ko, Np_1D)
+ *             (directfn_ws_ea_const_mex.cpp:50: second triangle (r4, r2, r1))
+ *   kind 'V': mexdirectfn_ws_va_const(r1, r2, r3, r4, r5, ko, Np_1D)
+ *             (directfn_ws_va_const_mex.cpp:51: second triangle (r4, r5, r1))
+ * out2 = (re, im).  Np_1D in 1..64. */
+int marie_directfn(char kind, const double* vertices, double ko, int np_1d, double* out2);
 
 /* Upload an FFT-of-circulant operator fN (2L x 2M x 2N x 6 complex), as
  * gpuArray(fN) in JVIE_Solver.m:271.  Converted to the plan's precisions. */
@@ -111,9 +130,12 @@ int marie_mv_AN(marie_plan* plan, const double* JIn0, const double* Mr, const do
  * fixed arena, or a loop that must not block in cudaMalloc).  Its scratch is a
  * 64 MiB static device array that every GPU loading this library holds until
  * exit; grids needing more (about 204-252 bytes per voxel in FP32, 396 in FP64)
- * are rejected with MARIE_EINVAL.  Device pointers only.  The first call on a
- * device looks up the array's address; make it before any stream capture.
- * Calls share the array, so calls that overlap on the GPU race. */
+ * are rejected with MARIE_EINVAL.  Device pointers only.  The call runs on the
+ * plan's device and stream (the caller's current device is restored) with the
+ * plan's matvec schedule, and waits on the host for that stream before it
+ * returns.  The first call for a device looks up the array's address; make it
+ * before any stream capture.  Calls share the array, so calls that overlap on
+ * the GPU race. */
 int marie_mv_AN_static(marie_plan* plan, const double* JIn0, const double* Mr,
                        const double* Mc, double Gram, int transp, const int64_t* idx,
                        int64_t n_idx, double* JOut, int precision);

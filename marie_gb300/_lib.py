@@ -43,6 +43,8 @@ SIGNATURES = {
     "marie_get_operators": (C.c_int, [_vp, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_char, C.c_char,
                                       C.c_char, _vp, _vp]),
     "marie_singular_integrals": (C.c_int, [C.c_double, C.c_double, _vp]),
+    "marie_singular_integrals_ex": (C.c_int, [C.c_double, C.c_double, C.c_char, C.c_int, _vp]),
+    "marie_directfn": (C.c_int, [C.c_char, _vp, C.c_double, C.c_int, _vp]),
     "marie_set_operator": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, C.c_int64]),
     "marie_plan_assemble": (C.c_int, [_vp, C.c_double, C.c_double, C.c_char, _vp]),
     "marie_get_plan_operator": (C.c_int, [_vp, _vp]),

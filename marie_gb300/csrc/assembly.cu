@@ -16,13 +16,15 @@
 //   circulant embedding 2L x 2M x 2N with per-axis parities (circulant_nop.m,
 //     gperiodic_coeff_nop.m) and the 3-D FFT of each of the 6 components.
 //
-// The singular integrals are computed here by reducing each square-square
-// integral to relative coordinates (the overlap of two unit intervals is a
-// hat function) and removing the 1/R point singularity at the origin with a
-// Duffy (polar-type) substitution, after which tensor Gauss-Legendre converges
-// to machine precision.  The reference's DIRECTFN quadrature at Np_1D = 20 is
-// accurate to about 3e-5 on the edge-adjacent pairs; callers that need its exact
-// values pass them in with singular = 'U'.
+// The singular integrals come from the reference's own scheme by default:
+// singular = 'D' runs DIRECTFN at Np_1D = 20 (directfn.cu), as
+// assembly_nop.m:16,96-98 does.  singular = 'C' is an opt-in that is not in
+// the reference: each square-square integral reduced to relative coordinates
+// (the overlap of two unit intervals is a hat function) with the 1/R point
+// singularity removed by a Duffy (polar-type) substitution, after which tensor
+// Gauss-Legendre converges to machine precision; it differs from DIRECTFN at
+// Np_1D = 20 by up to 3.4e-5 (the truncation error of DIRECTFN at that order).
+// singular = 'U' takes the five values from the caller.
 #include <cmath>
 #include <vector>
 
@@ -34,7 +36,7 @@ namespace marie {
 // --------------------------------------------------------------------------
 // Gauss-Legendre nodes on [-1, 1] (ascending), Newton on P_n in long double.
 // --------------------------------------------------------------------------
-static void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
   x.assign(n, 0.0);
   w.assign(n, 0.0);
   for (int i = 0; i < n; ++i) {
@@ -386,7 +388,8 @@ static cudaError_t rows_full(int NL, double2* data, long long rows, const double
 }
 
 // --------------------------------------------------------------------------
-// singular integrals by relative coordinates + Duffy substitution
+// converged singular integrals (singular = 'C'): relative coordinates + Duffy
+// substitution; not a reference method
 // --------------------------------------------------------------------------
 struct SingArgs {
   double ko, a;
@@ -472,8 +475,7 @@ __global__ void k_singular(SingArgs S, const double* __restrict__ x01, const dou
   }
 }
 
-static int singular_integrals(double ko, double dx, double2 out[5], cudaStream_t st) {
-  const int n = 32;
+static int converged_integrals(double ko, double dx, int n, double2 out[5], cudaStream_t st) {
   std::vector<double> x, w;
   gauss_legendre(n, x, w);
   for (int i = 0; i < n; ++i) {
@@ -859,14 +861,35 @@ int assemble_k_device(int L, int M, int N, double dx, double freq, char type, do
   return fft_operator(out, 2 * L, 2 * M, 2 * N, st, 3);
 }
 
-static int get_sing(char singular, const double* user, double ko, double dx, double2 s[5], cudaStream_t st) {
-  if (singular == 'U' || singular == 'u') {
-    if (!user) return set_error(MARIE_EINVAL, "singular = 'U' needs the five singular values");
-    for (int i = 0; i < 5; ++i) s[i] = mk<double2>(user[2 * i], user[2 * i + 1]);
-    return MARIE_OK;
+// The reference's Np_1D for the singular integrals (Np_DEMCEM, assembly_nop.m:16).
+constexpr int kNpSingular = 20;
+// Gauss order of the converged quadrature of singular = 'C'.
+constexpr int kNpConverged = 32;
+
+// singular: 'D' DIRECTFN at order np (0: the reference's 20), 'C' the converged
+// quadrature at order np (0: 32), 'U' the caller's five values.  The
+// reference's other method, DEMCEM, is not built.
+static int singular_values(char singular, int np, const double* user, double ko, double dx, double2 s[5],
+                           cudaStream_t st) {
+  switch (singular) {
+    case 'U': case 'u':
+      if (!user) return set_error(MARIE_EINVAL, "singular = 'U' needs the five singular values");
+      for (int i = 0; i < 5; ++i) s[i] = mk<double2>(user[2 * i], user[2 * i + 1]);
+      return MARIE_OK;
+    case 'D': case 'd':
+      return directfn_integrals(ko, dx, np ? np : kNpSingular, s, st);
+    case 'C': case 'c':
+      if (np < 0 || np > 128) return set_error(MARIE_EINVAL, "order of the converged quadrature out of range");
+      return converged_integrals(ko, dx, np ? np : kNpConverged, s, st);
+    case 'E': case 'e':
+      return set_error(MARIE_EINVAL, "singular = DEMCEM is not built; use 'D' (DIRECTFN, the reference default)");
+    default:
+      return set_error(MARIE_EINVAL, "singular must be 'D', 'C' or 'U'");
   }
-  if (singular != 'D' && singular != 'd') return set_error(MARIE_EINVAL, "singular must be 'D' or 'U'");
-  return singular_integrals(ko, dx, s, st);
+}
+
+static int get_sing(char singular, const double* user, double ko, double dx, double2 s[5], cudaStream_t st) {
+  return singular_values(singular, 0, user, ko, dx, s, st);
 }
 
 int assemble_operator_device(int L, int M, int N, double dx, double freq, char singular, const double* user_sing,
@@ -897,15 +920,20 @@ using namespace marie;
 
 extern "C" {
 
-int marie_singular_integrals(double ko, double dx, double* out10) {
+int marie_singular_integrals_ex(double ko, double dx, char method, int np_1d, double* out10) {
   if (!out10 || !(dx > 0)) return set_error(MARIE_EINVAL, "bad argument");
+  if (method == 'U' || method == 'u') return set_error(MARIE_EINVAL, "method must be 'D' or 'C'");
   double2 s[5];
-  MARIE_TRY(singular_integrals(ko, dx, s, 0));
+  MARIE_TRY(singular_values(method, np_1d, nullptr, ko, dx, s, 0));
   for (int i = 0; i < 5; ++i) {
     out10[2 * i] = s[i].x;
     out10[2 * i + 1] = s[i].y;
   }
   return MARIE_OK;
+}
+
+int marie_singular_integrals(double ko, double dx, double* out10) {
+  return marie_singular_integrals_ex(ko, dx, 'D', 0, out10);
 }
 
 int marie_get_operators(const double* r, int64_t L, int64_t M, int64_t N, double f, char op, char type,

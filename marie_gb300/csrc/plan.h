@@ -199,6 +199,17 @@ int gmres_dr(marie_plan* p, const DevOp& A, const DevOp* L1, const DevOp* L2, co
              const double2* b, long long n, int restart, double tol, int maxit, int ritz, const double2* x0,
              double2* x, GmresResult& res);
 
+// Gauss-Legendre rule of order n on [-1, 1], ascending nodes (assembly.cu).
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w);
+
+// DIRECTFN singular integrals {ST, EAc, EAo, VAc, VAo} for cubic voxels of
+// edge dx at Np_1D = n (directfn.cu); one triangle-pair call of a DIRECTFN
+// core with a MEX gateway's argument order (kind 'S', 'E' or 'V').
+constexpr int kDirectfnMaxOrder = 64;
+bool directfn_order_ok(int n);
+int directfn_integrals(double ko, double dx, int n, double2 out[5], cudaStream_t st);
+int directfn_single(char kind, const double* r, double ko, int n, double2* out, cudaStream_t st);
+
 // pgmres semantics (pgmres.m:70-181) on device vectors.
 int gmres(marie_plan* p, const DevOp& A, const DevOp* L1, const DevOp* L2, const DevOp* R1, const DevOp* R2,
           const double2* b, long long n, int restart, double tol, int maxit, const double2* x0, double2* x,

@@ -237,14 +237,22 @@ class Operator:
             pass
 
 
+_SINGULAR = {"DIRECTFN": b"D", "D": b"D", "CONVERGED": b"C", "C": b"C"}
+
+
 def _singular_arg(singular, values):
+    """singular: 'DIRECTFN' (the reference default, Np_1D = 20) or
+    'CONVERGED' (a converged quadrature, not a reference method).  The
+    reference's 'DEMCEM' is not built and raises."""
     if values is not None:
         v = np.asarray(values, dtype=np.complex128).reshape(5)
         arr = np.ascontiguousarray(v)
         return (b"U", C.c_void_p(arr.ctypes.data)), arr
-    if singular not in ("DIRECTFN", "D", "DEMCEM"):
-        raise ValueError("singular must be 'DIRECTFN' (or pass singular_values)")
-    return (b"D", None), None
+    if singular == "DEMCEM":
+        raise ValueError("singular='DEMCEM' is not built; use 'DIRECTFN' (the reference default)")
+    if singular not in _SINGULAR:
+        raise ValueError("singular must be 'DIRECTFN' or 'CONVERGED' (or pass singular_values)")
+    return (_SINGULAR[singular], None), None
 
 
 def _operator_for(fN, precision):
@@ -260,9 +268,11 @@ def getOPERATORS(r, f, op="N", type="FFTofC", singular="DIRECTFN", singular_valu
     """getOPERATORS.m:1-127 for op 'N' (6 components) and 'K' (3 components).
     type 'FFTofC' (default), 'C' or 'T'.
 
-    singular='DIRECTFN' evaluates the weakly singular self/edge/vertex integrals
-    of N with a converged device quadrature; singular_values = [ST, EAc, EAo,
-    VAc, VAo] overrides them (e.g. with the reference's own DIRECTFN values)."""
+    singular='DIRECTFN' (the default, as getOPERATORS.m:39-41) evaluates the
+    weakly singular self/edge/vertex integrals of N with DIRECTFN at
+    Np_1D = 20 on the device (assembly_nop.m:16,96-98); 'CONVERGED' uses a
+    converged quadrature instead (not a reference method); singular_values =
+    [ST, EAc, EAo, VAc, VAo] overrides both."""
     lib = _lib.load()
     if op not in ("N", "K"):
         raise ValueError("op must be 'N' or 'K'")
@@ -277,12 +287,33 @@ def getOPERATORS(r, f, op="N", type="FFTofC", singular="DIRECTFN", singular_valu
     return out
 
 
-def singular_integrals(ko, dx):
-    """[ST, EAc, EAo, VAc, VAo] (complex) for wavenumber ko and voxel edge dx."""
+def singular_integrals(ko, dx, method="DIRECTFN", np_1d=0):
+    """[ST, EAc, EAo, VAc, VAo] (complex) for wavenumber ko and voxel edge dx:
+    singular_st/ea/va.m with 'DIRECTFN' at Np_1D = np_1d (0: the reference's
+    20), or the converged quadrature ('CONVERGED')."""
     lib = _lib.load()
     out = np.zeros(10)
-    check(lib.marie_singular_integrals(float(ko), float(dx), C.c_void_p(out.ctypes.data)))
+    if method == "DEMCEM":
+        raise ValueError("method='DEMCEM' is not built")
+    code = _SINGULAR.get(method)
+    if code is None:
+        raise ValueError("method must be 'DIRECTFN' or 'CONVERGED'")
+    check(lib.marie_singular_integrals_ex(float(ko), float(dx), code, int(np_1d), C.c_void_p(out.ctypes.data)))
     return out[0::2] + 1j * out[1::2]
+
+
+def directfn(kind, vertices, ko, np_1d=20):
+    """One DIRECTFN core call with its MEX gateway's arguments:
+    'st' mexdirectfn_ws_st_const(r1, r2, r3, ko, Np_1D), 'ea' (r1..r4), 'va'
+    (r1..r5).  Returns the complex integral."""
+    lib = _lib.load()
+    code = {"st": b"S", "ea": b"E", "va": b"V"}[kind]
+    v = np.ascontiguousarray(np.asarray(vertices, dtype=np.float64).reshape(-1))
+    if v.size != {"st": 9, "ea": 12, "va": 15}[kind]:
+        raise ValueError("wrong number of vertices")
+    out = np.zeros(2)
+    check(lib.marie_directfn(code, C.c_void_p(v.ctypes.data), float(ko), int(np_1d), C.c_void_p(out.ctypes.data)))
+    return out[0] + 1j * out[1]
 
 
 # ---------------------------------------------------------------------------

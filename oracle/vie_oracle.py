@@ -6,6 +6,8 @@ Arrays follow the reference's MATLAB layout: numpy arrays of shape
 """
 from __future__ import annotations
 
+import functools
+
 import numpy as np
 import scipy.fft
 import scipy.special as sp
@@ -705,11 +707,33 @@ def nearby_correct(m, I_non, sing):
     return J
 
 
-def singular_integrals(ko, a, n=32):
+@functools.lru_cache(maxsize=64)
+def _directfn_cached(ko, dx, n):
+    from . import directfn
+
+    return directfn.singular_integrals(ko, dx, n)
+
+
+def singular_integrals(ko, dx, method="DIRECTFN", n=None):
+    """{ST, EAc, EAo, VAc, VAo} for cubic voxels of edge dx.  'DIRECTFN' (the
+    reference default, getOPERATORS.m:39-41) restates singular_st/ea/va.m at
+    Np_1D = n (default 20, assembly_nop.m:16) in oracle/directfn.py;
+    'CONVERGED' is the converged quadrature of singular_integrals_converged
+    (not a reference method)."""
+    if method == "DIRECTFN":
+        return _directfn_cached(float(ko), float(dx), int(n or 20)).copy()
+    if method == "CONVERGED":
+        return singular_integrals_converged(ko, dx, n or 32)
+    raise ValueError("method must be 'DIRECTFN' or 'CONVERGED'")
+
+
+def singular_integrals_converged(ko, a, n=32):
     """Weakly singular square-square integrals {ST, EAc, EAo, VAc, VAo} of
-    exp(-j ko R)/R for voxel edge a, replacing singular_st/ea/va.m.  Relative
-    coordinates turn each into an integral of f(|u|) times hat-function weights;
-    a Duffy substitution removes the 1/R point singularity at the origin."""
+    exp(-j ko R)/R for voxel edge a, converged to machine precision (not the
+    reference's DIRECTFN, which carries a truncation error of up to 3.4e-5 at
+    Np_1D = 20).  Relative coordinates turn each into an integral of f(|u|)
+    times hat-function weights; a Duffy substitution removes the 1/R point
+    singularity at the origin."""
     x, w = np.polynomial.legendre.leggauss(n)
     x = (x + 1) / 2
     w = w / 2
@@ -950,7 +974,8 @@ def fft_operator(A, workers=None):
 
 def getOPERATORS(r, f, op="N", typ="FFTofC", sing=None):
     """getOPERATORS.m:36-127 for op 'N' and 'K'.  sing = the five singular
-    integrals of N (defaults to the converged quadrature of singular_integrals)."""
+    integrals of N (default: DIRECTFN at Np_1D = 20, as the reference's
+    default singular = 'DIRECTFN' computes them, assembly_nop.m:96-98)."""
     dx = r[1, 0, 0, 0] - r[0, 0, 0, 0]
     ko = 2 * np.pi / 299792458 * f
     L, M, N, _ = r.shape

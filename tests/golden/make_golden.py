@@ -1,7 +1,7 @@
 """Generate tests/golden/reference_golden.json from the reference checkout.
 
 Run in a container that has the reference sources (read-only) and g++:
-    python tests/golden/make_golden.py /path/to/reference
+    python tests/golden/make_golden.py <path of the reference checkout>
 
 It records, as small JSON fixtures:
   gauss_1d      the tabulated Gauss-Legendre rules of orders 4, 10, 20
@@ -12,7 +12,10 @@ It records, as small JSON fixtures:
                 (mexcubatures/cubature_nop.cpp) at several offsets
   directfn      the five singular integrals from the reference DIRECTFN C++
                 cores (directfn_ws_{st,ea,va}_const.cpp) with the geometry of
-                singular_st/ea/va.m, at Np_1D = 20 (the reference default) and 64
+                singular_st/ea/va.m, at Np_1D = 20 (the reference default) and
+                64, and at Np_1D = 20 for further frequencies
+  directfn_tri  single calls of the three cores through the MEX gateways'
+                vertex order, on seeded random triangles, Np_1D 8/12/20
 
 The reference C++ is compiled from its own sources by oracle/Makefile into
 oracle/_ref/ (outside the repository history).
@@ -167,6 +170,26 @@ def directfn_values(ko, dx, Np):
     return {"re": [x.real for x in v], "im": [x.imag for x in v]}
 
 
+def directfn_tri_cases():
+    """Single calls of the three DIRECTFN cores on seeded random vertices
+    (gateway argument order: st r1..r3, ea r1..r4, va r1..r5)."""
+    R = str(ROOT / "oracle/_ref/")
+    libs = {"st": (ctypes.CDLL(R + "/libref_directfn_st.so").ref_directfn_st, 3),
+            "ea": (ctypes.CDLL(R + "/libref_directfn_ea.so").ref_directfn_ea, 4),
+            "va": (ctypes.CDLL(R + "/libref_directfn_va.so").ref_directfn_va, 5)}
+    rng = np.random.default_rng(20240)
+    cases = []
+    for kind, (fn, nv) in libs.items():
+        for Np in (8, 12, 20):
+            for _ in range(3):
+                r = rng.uniform(-1.0, 1.0, size=(nv, 3)) * rng.choice([1e-3, 5e-3, 0.3])
+                ko = float(rng.uniform(0.5, 40.0))
+                o = np.zeros(2)
+                fn(*[_ptr(v) for v in r], ctypes.c_double(ko), ctypes.c_int(Np), _ptr(o))
+                cases.append({"kind": kind, "Np": Np, "ko": ko, "r": r.tolist(), "re": o[0], "im": o[1]})
+    return cases
+
+
 def main(ref: Path):
     build_ref(ref)
     ko = 2 * np.pi * FREQ / C0
@@ -174,6 +197,9 @@ def main(ref: Path):
     for dx in (5e-3, 2e-3, 3e-3, 1e-2):
         direct.append({"ko": ko, "dx": dx, "Np": 20, **directfn_values(ko, dx, 20)})
     direct.append({"ko": ko, "dx": 5e-3, "Np": 64, **directfn_values(ko, 5e-3, 64)})
+    for f in (64e6, 128e6, 447e6, 3e9):
+        k = 2 * np.pi * f / C0
+        direct.append({"ko": k, "dx": 5e-3, "Np": 20, **directfn_values(k, 5e-3, 20)})
     data = {
         "freq": FREQ,
         "gauss_1d": parse_gauss(ref),
@@ -182,10 +208,13 @@ def main(ref: Path):
         "nearby_kop_st": parse_nearby_kop(ref),
         "cubature_kop": cubature_kop_cases(),
         "directfn": direct,
+        "directfn_tri": directfn_tri_cases(),
     }
     OUT.write_text(json.dumps(data, indent=1))
     print(f"wrote {OUT}")
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the reference checkout>")
+    main(Path(sys.argv[1]))
