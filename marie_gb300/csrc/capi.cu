@@ -19,6 +19,17 @@ static std::atomic<long long> g_launches{0};
 
 void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+int sm_count() {
+  static std::atomic<int> cache[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) return 152;
+  cache[dev].store(v, std::memory_order_relaxed);
+  return v;
+}
+
 static std::mutex g_smem_mu;
 static std::map<std::pair<const void*, int>, size_t> g_smem_set;  // (kernel, device) -> bytes
 
@@ -219,12 +230,7 @@ __global__ void k_coefficients(const int64_t* idx, long long n, long long V, con
   }
 }
 
-static inline int grid_for(long long n, int threads = 256) {
-  long long g = (n + threads - 1) / threads;
-  if (g > 152 * 16) g = 152 * 16;
-  if (g < 1) g = 1;
-  return (int)g;
-}
+static inline int grid_for(long long n, int threads = 256) { return grid_stride_blocks(n, 16, threads); }
 
 // autotuner input: J = a smooth pattern, the identity DOF map over the grid
 __global__ void k_tune_fill(double2* __restrict__ J, int* __restrict__ inv, long long n) {

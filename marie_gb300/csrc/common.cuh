@@ -43,6 +43,18 @@ int set_error(int code, const char* fmt, ...);
 // Counts kernel launches issued by this library (marie_launch_count).
 void count_launch(long long n = 1);
 
+// Streaming multiprocessors of the current device (queried once per device).
+int sm_count();
+
+// Blocks for a grid-stride loop over n elements: ceil(n / threads), at most
+// per_sm blocks per streaming multiprocessor of the current device, at least 1.
+inline int grid_stride_blocks(long long n, int per_sm, int threads = 256) {
+  long long g = (n + threads - 1) / threads;
+  const long long cap = (long long)sm_count() * per_sm;
+  if (g > cap) g = cap;
+  return g < 1 ? 1 : (int)g;
+}
+
 #define MARIE_CUDA_TRY(expr)                                                          \
   do {                                                                                \
     cudaError_t _e = (expr);                                                          \

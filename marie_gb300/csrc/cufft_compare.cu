@@ -91,11 +91,7 @@ struct CufftState {
 std::mutex g_cf_mu;
 std::map<const marie_plan*, CufftState*> g_cf;
 
-inline int grid_cf(long long n) {
-  long long g = (n + 255) / 256;
-  if (g > 152 * 16) g = 152 * 16;
-  return g < 1 ? 1 : (int)g;
-}
+inline int grid_cf(long long n) { return grid_stride_blocks(n, 16); }
 
 int cufft_state(marie_plan* p, CufftState** out) {
   std::lock_guard<std::mutex> lock(g_cf_mu);

@@ -13,11 +13,7 @@ static constexpr double MU0 = 4e-7 * M_PI;
 static constexpr double C0 = 299792458.0;
 static inline double eps0() { return 1.0 / (C0 * C0 * MU0); }
 
-static inline int grid_n(long long n) {
-  long long g = (n + 255) / 256;
-  if (g > 152 * 8) g = 152 * 8;
-  return g < 1 ? 1 : (int)g;
-}
+static inline int grid_n(long long n) { return grid_stride_blocks(n, 8); }
 
 __global__ void k_identity_index(int* __restrict__ inv, long long n) {
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)

@@ -43,11 +43,7 @@ constexpr int DR_BLOCKS = 304;  // the reduction grid of krylov.cu
 constexpr int DR_THREADS = 256;
 constexpr int DR_MAXCOLS = 128;  // k_combine / k_update_norm stage this many coefficients
 
-inline int grid_n(long long n) {
-  long long g = (n + 255) / 256;
-  if (g > 152 * 8) g = 152 * 8;
-  return g < 1 ? 1 : (int)g;
-}
+inline int grid_n(long long n) { return grid_stride_blocks(n, 8); }
 
 struct DrWork {
   marie_plan* p = nullptr;

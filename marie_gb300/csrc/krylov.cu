@@ -159,11 +159,7 @@ __global__ void k_combine(const double2* __restrict__ Vb, long long ld, int ncol
   }
 }
 
-static inline int grid_n(long long n) {
-  long long g = (n + 255) / 256;
-  if (g > 152 * 8) g = 152 * 8;
-  return g < 1 ? 1 : (int)g;
-}
+static inline int grid_n(long long n) { return grid_stride_blocks(n, 8); }
 
 int dev_norm2(marie_plan* p, const double2* x, long long n, double* out_host) {
   DBuf part, res;

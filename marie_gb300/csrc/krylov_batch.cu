@@ -30,7 +30,10 @@
 
 namespace marie {
 
-static constexpr int BG = 152 * 2;  // row blocks per system for the reductions
+// Row blocks per system of the reductions: a fixed count (2 per SM of a GB300),
+// so that the two-stage sums, and with them the results, do not depend on the
+// device the solve runs on.
+static constexpr int BG = 152 * 2;
 // row blocks of the dots and the update with an FP32 basis: these stream the
 // basis at HBM speed rather than at the FP64 rate, so they want more loads in
 // flight (four blocks per SM)
@@ -474,11 +477,7 @@ __global__ void kb_sub_from(const double2* __restrict__ b, long long bs, double2
     c[i] = csub(a[i], c[i]);
 }
 
-static inline int gx(long long n) {
-  long long g = (n + 255) / 256;
-  if (g > 152 * 4) g = 152 * 4;
-  return g < 1 ? 1 : (int)g;
-}
+static inline int gx(long long n) { return grid_stride_blocks(n, 4); }
 
 struct BatchWork {
   int S = 0, m = 0;

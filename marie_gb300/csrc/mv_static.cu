@@ -13,12 +13,17 @@
 // library holds until the process exits.  Inputs and outputs stay the caller's
 // device buffers; the plan (operator and twiddles) is created beforehand.
 //
-// Set-up: the first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (that device current) and caches it; make that first
-// call before any stream capture.  Every call shares the one array and it keeps
-// the previous call's contents, so each call resets what must start clean (the
-// error flag and the index map); two calls that overlap on the GPU (other
-// streams, other threads, other plans on the same device) race on it.
+// Set-up: the first call for a device looks up the array's device address with
+// cudaGetSymbolAddress, with that device (the plan's) current, and caches it;
+// make that first call before any stream capture.  A call runs on the plan's
+// device and stream whatever device is current, and restores the caller's
+// current device before it returns.  Each call waits for its stream on the host
+// (it reads the status of the index check, then finishes the product) before
+// returning.  Every call shares the one array and it keeps the previous call's
+// contents, so each call resets what must start clean (the error flag and the
+// index map); two calls that overlap on the GPU (other streams, other threads,
+// other plans on the same device) race on it.  The passes run with the plan's
+// schedule (marie_plan_autotune / marie_plan_set_schedule), as marie_mv_AN's do.
 #include <map>
 #include <mutex>
 
@@ -46,9 +51,8 @@ static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBy
 static std::mutex g_scratch_mu;
 static std::map<int, unsigned char*> g_scratch_addr;
 
-static int scratch_address(unsigned char** out) {
-  int dev = 0;
-  MARIE_CUDA_TRY(cudaGetDevice(&dev));
+// dev must be the current device
+static int scratch_address(int dev, unsigned char** out) {
   std::lock_guard<std::mutex> lock(g_scratch_mu);
   auto it = g_scratch_addr.find(dev);
   if (it != g_scratch_addr.end()) {
@@ -94,7 +98,7 @@ static int static_matvec(marie_plan* p, const double2* J, const double2* Mr, con
                      "its static array; use marie_mv_AN",
                      off, kStaticScratchBytes);
   cudaStream_t st = p->stream;
-  const int g = 152 * 8;
+  const int g = sm_count() * 8;
   // the array keeps the previous call's contents: reset the flag and the map
   MARIE_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
   k_fill_int<<<g, 256, 0, st>>>(inv, V3, -1);
@@ -128,15 +132,15 @@ static int static_matvec(marie_plan* p, const double2* J, const double2* Mr, con
   V* const* tw = sizeof(T) == 4 ? reinterpret_cast<V* const*>(p->tw32) : reinterpret_cast<V* const*>(p->tw64);
   const long long sA = p->elems_A(), sB = p->elems_B();
   if (fused) {
-    MARIE_CUDA_TRY(ML::xyfwd(J, n, inv, pro, B, sB, d, tw[0], tw[1], 1, st));
-    MARIE_CUDA_TRY(ML::zmul(B, sB, fN, p->oct, d, tw[2], 1, st));
-    MARIE_CUDA_TRY(ML::yxinv(B, sB, J, n, inv, ep, out, n, d, tw[0], tw[1], 1, st));
+    MARIE_CUDA_TRY(ML::xyfwd(J, n, inv, pro, B, sB, d, tw[0], tw[1], 1, st, p->fvar));
+    MARIE_CUDA_TRY(ML::zmul(B, sB, fN, p->oct, d, tw[2], 1, st, 0, p->zvar));
+    MARIE_CUDA_TRY(ML::yxinv(B, sB, J, n, inv, ep, out, n, d, tw[0], tw[1], 1, st, p->fvar));
     count_launch(3);
   } else {
     MARIE_CUDA_TRY(ML::xfwd(J, n, inv, pro, A, sA, d, tw[0], 1, st));
     MARIE_CUDA_TRY(ML::cols(false, d.Mp, A, (long long)d.Lp * d.M, sA, d.M, B, (long long)d.Lp * d.Mp, sB, d.Mp,
                             d.Lp, 3 * d.N, tw[1], 1, st));
-    MARIE_CUDA_TRY(ML::zmul(B, sB, fN, p->oct, d, tw[2], 1, st));
+    MARIE_CUDA_TRY(ML::zmul(B, sB, fN, p->oct, d, tw[2], 1, st, 0, p->zvar));
     MARIE_CUDA_TRY(ML::cols(true, d.Mp, B, (long long)d.Lp * d.Mp, sB, d.Mp, A, (long long)d.Lp * d.M, sA, d.M,
                             d.Lp, 3 * d.N, tw[1], 1, st));
     MARIE_CUDA_TRY(ML::xinv(A, sA, J, n, inv, ep, out, n, d, tw[0], 1, st));
@@ -146,9 +150,38 @@ static int static_matvec(marie_plan* p, const double2* J, const double2* Mr, con
   return MARIE_OK;
 }
 
+namespace {
+// makes the plan's device current for one call and restores the caller's
+struct DeviceScope {
+  int prev = -1;
+  bool switched = false;
+  int enter(int dev) {
+    MARIE_CUDA_TRY(cudaGetDevice(&prev));
+    if (prev != dev) {
+      MARIE_CUDA_TRY(cudaSetDevice(dev));
+      switched = true;
+    }
+    return MARIE_OK;
+  }
+  ~DeviceScope() {
+    if (switched) cudaSetDevice(prev);
+  }
+};
+}  // namespace
+
+static int mv_static_on_device(marie_plan* p, const double* JIn0, const double* Mr, const double* Mc, double Gram,
+                               int transp, const int64_t* idx, int64_t n_idx, double* JOut, int precision);
+
 extern "C" int marie_mv_AN_static(marie_plan* p, const double* JIn0, const double* Mr, const double* Mc, double Gram,
                                   int transp, const int64_t* idx, int64_t n_idx, double* JOut, int precision) {
   if (!p || !JIn0 || !Mr || !Mc || !JOut || (!idx && n_idx > 0)) return set_error(MARIE_EINVAL, "NULL argument");
+  DeviceScope scope;
+  MARIE_TRY(scope.enter(p->device));
+  return mv_static_on_device(p, JIn0, Mr, Mc, Gram, transp, idx, n_idx, JOut, precision);
+}
+
+static int mv_static_on_device(marie_plan* p, const double* JIn0, const double* Mr, const double* Mc, double Gram,
+                               int transp, const int64_t* idx, int64_t n_idx, double* JOut, int precision) {
   if (transp != 0 && transp != 1) return set_error(MARIE_EINVAL, "transp must be 0 ('notransp') or 1 ('transp')");
   if (!p->has_op) return set_error(MARIE_ENOOP, "plan has no operator");
   if (precision == MARIE_FP32 ? !p->fN32 : (precision == MARIE_FP64 ? !p->fN64 : true))
@@ -159,7 +192,7 @@ extern "C" int marie_mv_AN_static(marie_plan* p, const double* JIn0, const doubl
       (n_idx > 0 && !is_device_ptr(idx)))
     return set_error(MARIE_EINVAL, "marie_mv_AN_static takes device pointers only");
   unsigned char* scratch = nullptr;
-  MARIE_TRY(scratch_address(&scratch));
+  MARIE_TRY(scratch_address(p->device, &scratch));
   if (precision == MARIE_FP32)
     return static_matvec<float>(p, (const double2*)JIn0, (const double2*)Mr, (const double2*)Mc, Gram, transp, idx,
                                 n_idx, (double2*)JOut, scratch);

@@ -1,7 +1,9 @@
 """marie_mv_AN_static, the matvec that allocates nothing (its scratch is a
 static device array), against marie_mv_AN through the C ABI.  Two calls in a
 row on each grid: the second reuses the array the first left behind, with a
-different DOF set and flag.  Bar: FP64 within 1e-12 and FP32 within 1e-5 of
+different DOF set and flag.  Every static call runs with the library's
+allocation-failure injector armed, so any device allocation inside it would
+return MARIE_ENOMEM.  Bar: FP64 within 1e-12 and FP32 within 1e-5 of
 max|out|, as for the matvec parity tests.  Collected last, so it runs both
 after the other GPU tests and alone."""
 import ctypes as C
@@ -46,6 +48,15 @@ def call(fn, plan, c, transp, prec, out, gram=0.37):
               gram, transp, C.c_void_p(c["idx"].data_ptr()), c["n"], C.c_void_p(out.data_ptr()), *prec)
 
 
+def call_static_no_alloc(lib, plan, c, transp, prec, out):
+    """The static entry point with the first device allocation set to fail."""
+    lib.marie_inject_alloc_failure(1)
+    try:
+        return call(lib.marie_mv_AN_static, plan, c, transp, (prec,), out)
+    finally:
+        lib.marie_inject_alloc_failure(0)
+
+
 @pytest.mark.parametrize("shape", [(16, 12, 20), (32, 32, 4), (40, 8, 24)])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_static_matvec_matches_mv_AN_on_two_calls(shape, precision, cuda):
@@ -62,7 +73,7 @@ def test_static_matvec_matches_mv_AN_on_two_calls(shape, precision, cuda):
         ref = torch.zeros(c["n"], dtype=torch.complex128, device=cuda)
         out = torch.full((c["n"],), complex("nan"), dtype=torch.complex128, device=cuda)
         _lib.check(call(lib.marie_mv_AN, op.plan, c, transp, (1, p), ref))
-        _lib.check(call(lib.marie_mv_AN_static, op.plan, c, transp, (p,), out))
+        _lib.check(call_static_no_alloc(lib, op.plan, c, transp, p, out))
         torch.cuda.synchronize()
         r, o = ref.cpu().numpy(), out.cpu().numpy()
         assert np.all(np.isfinite(o))
@@ -93,3 +104,29 @@ def test_static_matvec_rejects_oversize_grids_and_host_pointers(cuda):
     assert st == _lib.MARIE_EINVAL
     assert b"device pointers" in lib.marie_last_error()
     small.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_static_matvec_follows_the_tuned_schedule(precision, cuda):
+    """After marie_plan_set_schedule picks the non-default x/y and z-pass
+    variants, the static entry point still matches marie_mv_AN (which runs
+    them), with the allocation injector armed."""
+    import torch
+
+    import marie_gb300 as mg
+    from marie_gb300 import _lib
+
+    lib = _lib.load()
+    p = _lib.MARIE_FP64 if precision == "fp64" else _lib.MARIE_FP32
+    shape = (32, 32, 16)
+    op = mg.Operator.from_array(operator(*shape, seed=7), precision="mixed")
+    op.set_schedule(1, 1, 1)
+    c = case(*shape, 8, 0.6, cuda)
+    ref = torch.zeros(c["n"], dtype=torch.complex128, device=cuda)
+    out = torch.full((c["n"],), complex("nan"), dtype=torch.complex128, device=cuda)
+    _lib.check(call(lib.marie_mv_AN, op.plan, c, 0, (1, p), ref))
+    _lib.check(call_static_no_alloc(lib, op.plan, c, 0, p, out))
+    torch.cuda.synchronize()
+    r, o = ref.cpu().numpy(), out.cpu().numpy()
+    assert np.max(np.abs(o - r)) <= TOL[precision] * np.max(np.abs(r))
+    op.close()
