@@ -9,16 +9,23 @@ the scatter of J back onto the grid (the operator fN is assembled once per
 frequency, outside the timed region, and reported separately).
 
 Arms:
-  default          FP32 circulant matvec inside FP64 GMRES + FP64 refinement
-                   (inputs resident in HBM for `value`; host buffers through the
-                   C ABI for `e2e`); the plain FP64 solve and the matvec times
-                   are measured beside it.
+  default          FP32 circulant matvec inside GMRES with an FP64 Krylov
+                   basis, FP64 residuals and refinement (inputs resident in
+                   HBM for `value`; host buffers through the C ABI for `e2e`);
+                   the plain FP64 solve, the FP32-basis variant and the matvec
+                   times are measured beside it, and the other workloads (c1
+                   Mie sphere, c3 batched dipoles and uneven bodies, c4 64^3
+                   adjoint gradient, c5 256x192x160 body) as extra keys.
   --impl reference the reference's CPU path (the numpy/scipy restatement of
                    mv_AN + pgmres, complex128, scipy.fft on all host cores),
                    one GMRES iteration per step, reported as solves/s.
 
-Multi-GPU: each rank solves its own body (seed = rank); no data-path
-collective ("weak" scaling, replicas of independent objects).
+Multi-GPU (--gpus N): the script re-runs itself as N processes under
+torch.distributed.run when it is not already inside one.  Each rank solves its
+own body (seed = rank) for the headline, and its share of the c3 excitations
+and bodies; NCCL only takes the timing maximum and gathers the per-unit
+results ("weak" scaling, replicas of independent objects, no data-path
+collective).
 """
 from __future__ import annotations
 
@@ -140,14 +147,9 @@ def make_problem(seed):
 
 
 def dist_init():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
+    from marie_gb300 import replicas
 
-        dist.init_process_group("nccl" if os.environ.get("MARIE_BENCH_GLOO") is None else "gloo")
-    return world, rank, local
+    return replicas.init("nccl")
 
 
 def reduce_max(x, world):
@@ -214,6 +216,8 @@ def run_gpu(args, world, rank, local):
     # schedule autotuner (outside the timed region): fused / five-pass x-y
     # passes and their radix schedule, z-pass radix schedule and columns per CTA
     tuned, tune_cands = op.autotune()
+    # the stated precision split: FP32 matvec, Arnoldi in FP64 (the default)
+    op.set_inner_precision("fp64")
 
     # --- timed region: mixed-precision solves, inputs resident in HBM --------
     for _ in range(args.warmup):
@@ -266,15 +270,22 @@ def run_gpu(args, world, rank, local):
         n_it64 = len(resvec64) - 1
         field_err = float((torch.linalg.norm(Jm - J64) / torch.linalg.norm(J64)).item())
 
-        # --- the same mixed solve with an FP64 Krylov basis in the inner solves
-        op.set_inner_precision("fp64")
-        t0 = time.perf_counter()
-        Ji, fi, ri, iti, resi, _ = solve(op, Ed, erd, r)
-        torch.cuda.synchronize()
-        inner64 = {"flag": fi, "relres": ri, "iter": iti, "matvecs": len(resi) - 1,
-                   "seconds": round(time.perf_counter() - t0, 4),
-                   "field_rel_err_vs_fp64": float((torch.linalg.norm(Ji - J64) / torch.linalg.norm(J64)).item())}
+        # --- the same mixed solve with an FP32 Krylov basis in the inner solves
+        # (an opt-in that departs from the stated split), CUDA events
         op.set_inner_precision("fp32")
+        solve(op, Ed, erd, r)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n32 = max(1, min(args.steps, 3))
+        e0.record(stream)
+        for _ in range(n32):
+            Ji, fi, ri, iti, resi, _ = solve(op, Ed, erd, r)
+        e1.record(stream)
+        e1.synchronize()
+        t32 = e0.elapsed_time(e1) / 1e3 / n32
+        inner32 = {"flag": fi, "relres": ri, "iter": iti, "matvecs": len(resi) - 1, "seconds": round(t32, 4),
+                   "solves_per_s": round(1 / t32, 4), "speedup_vs_fp64": round(t64 / t32, 3),
+                   "field_rel_err_vs_fp64": float((torch.linalg.norm(Ji - J64) / torch.linalg.norm(J64)).item())}
+        op.set_inner_precision("fp64")
         del Ji
 
         # --- the other solvers of JVIE_Solver, mixed precision, one solve each
@@ -301,14 +312,15 @@ def run_gpu(args, world, rank, local):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64 matvec + inner krylov / c128 refinement",
             "data": "synthetic (seeded ellipsoid phantom, plane wave)",
             "config": headline_config(er, world),
-            "method": "mixed precision: inner GMRES(50) with the FP32 matvec on FP32 vectors and an FP32 "
-                      "Krylov basis, FP64 residuals and refinement (GMRES-IR)",
+            "method": "mixed precision: inner GMRES(50) with the FP32 matvec and an FP64 Krylov basis "
+                      "(Arnoldi, Givens and residual estimates in FP64), FP64 true residuals and refinement "
+                      "(GMRES-IR)",
             "solve": {"mixed": {"flag": flag_m, "relres": relres_m, "iter": iter_m,
                                 "matvecs": len(resvec_m) - 1, "solves_per_s": round(value / world, 4)},
                       "fp64": {"flag": flag64, "relres": relres64, "iter": it64, "iterations": n_it64,
                                "seconds": round(t64, 4), "solves_per_s": round(1 / t64, 4)},
                       "speedup_mixed_vs_fp64": round(t64 / (ms_per_step / 1e3), 3),
-                      "field_rel_err_mixed_vs_fp64": field_err, "mixed_inner_fp64_basis": inner64,
+                      "field_rel_err_mixed_vs_fp64": field_err, "mixed_inner_fp32_basis": inner32,
                       "mixed_other_solvers": variants},
             "matvec_ms": {"fp32": mv["fp32_ms"], "fp64": mv["fp64_ms"], "fp32_passes_ms": mv["fp32_passes"],
                           "fp64_passes_ms": mv["fp64_passes"], "fp32_cufft_comparison": mv["fp32_cufft_ms"]},
@@ -478,7 +490,8 @@ def run_reference(args, world, rank):
 
 
 # ---------------------------------------------------------------------------
-# the other workloads (reported beside the headline; not the default line)
+# the other workloads: extra keys of the main line (world 1), or their own line
+# with --config cX
 # ---------------------------------------------------------------------------
 def _timed(fn, steps, warmup):
     import torch
@@ -494,81 +507,153 @@ def _timed(fn, steps, warmup):
     return (time.perf_counter() - t0) / steps, out
 
 
-def run_extra(args):
-    """c1: Mie sphere; c3: 16 dipoles on one 128^3 body + 3 uneven bodies;
-    c4: 64^3 adjoint gradient; c5: 256x192x160, 8 dipoles + gradient."""
+def config_c1(steps, warmup):
+    """32^3 Mie sphere (r 7.5 cm, eps_r 50, sigma 0.5 S/m, 5 mm), plane wave,
+    GMRES(50) to 1e-6: FP64 and mixed solves (the Mie comparison itself is a
+    test against the analytic series)."""
+    import marie_gb300 as mg
+    from marie_gb300 import phantoms
+
+    em = mg.EMconstants(FREQ)
+    Lc, dx, R = 32, 5e-3, 0.075
+    r, er = phantoms.sphere(Lc, Lc, Lc, dx, R, 50.0, 0.5, FREQ)
+    E, _ = mg.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
+    res = {"workload": "32^3 sphere r 7.5 cm, eps_r 50, sigma 0.5 S/m, 5 mm, plane wave, GMRES(50), tol 1e-6"}
+    for prec in ("fp64", "mixed"):
+        op = mg.Operator.assemble(Lc, Lc, Lc, dx, FREQ, precision=prec)
+        t, out = _timed(lambda: mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-6, solver="G"), steps, warmup)
+        res[prec] = {"seconds": round(t, 5), "iter": out[3], "relres": out[2], "matvecs": len(out[4]) - 1}
+        op.close()
+    return res
+
+
+def config_c3(steps, warmup, world=1, rank=0):
+    """16 z-directed dipoles on a 0.15 m cylinder around the 128^3 body, one
+    lockstep batch per rank (its share of the 16); three uneven bodies 48^3,
+    64^3, 96^3 (seeds 1-3) with 4 dipoles each, its share of the bodies
+    solved concurrently.  Throughput = all units / max time over ranks."""
+    import torch
+
+    import marie_gb300 as mg
+    from marie_gb300 import phantoms, replicas
+
+    em = mg.EMconstants(FREQ)
+    res = {"workload": "16 dipoles (4 azimuths x z in {-5,0,5,10} cm, rho 0.15 m) on the 128^3 body; "
+                       "bodies 48^3/64^3/96^3 (seeds 1-3) x 4 dipoles"}
+    r, er = make_problem(0)
+    pos = phantoms.dipole_ring(0.15, [-0.05, 0.0, 0.05, 0.10], 4)
+    mine = replicas.shard(len(pos), rank, world)
+    units = []
+    t_b = 0.0
+    if mine:
+        Eb = np.asfortranarray(np.stack([np.asarray(mg.Dipole_Excitation(r, em["ko"], np.array([[0, 0, 1.0]]),
+                                                                         pos[e][None])) for e in mine], axis=4))
+        op = mg.Operator.assemble(L, M, N, DX, FREQ, precision="mixed", nrhs_max=len(mine))
+        t_b, out = _timed(lambda: mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, tol=TOL), steps, warmup)
+        units = [(e, int(out[1][i]), float(out[2][i]), [int(x) for x in out[3][i]]) for i, e in enumerate(mine)]
+        del Eb
+        op.close()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t_max = replicas.max_over_ranks(t_b, world, dev)
+    allu = replicas.gather_results(units, world)
+    res["batch16"] = {"seconds": round(t_max, 4), "excitation_solves_per_s": round(len(pos) / t_max, 4),
+                      "flags": [u[1] for u in allu], "max_relres": max(u[2] for u in allu),
+                      "iters": [u[3] for u in allu], "units_solved": [u[0] for u in allu]}
+    specs = ((1, 48), (2, 64), (3, 96))
+    mine_b = replicas.shard(len(specs), rank, world)
+    bodies, t_u, ub = [], 0.0, []
+    for i in mine_b:
+        seed, Lb = specs[i]
+        rb, erb, _ = phantoms.ellipsoids(Lb, Lb, Lb, DX, N_ELL, seed, FREQ)
+        pb = phantoms.dipole_ring(0.15, [0.0], 4)
+        Eb = np.asfortranarray(np.stack([np.asarray(mg.Dipole_Excitation(rb, em["ko"], np.array([[0, 0, 1.0]]),
+                                                                         p[None])) for p in pb], axis=4))
+        bodies.append((Eb, erb, rb, mg.Operator.assemble(Lb, Lb, Lb, DX, FREQ, precision="mixed", nrhs_max=4)))
+    if bodies:
+        t_u, out = _timed(lambda: mg.JVIE_Solver_bodies(bodies, FREQ, tol=TOL), steps, warmup)
+        ub = [(specs[i][1], [int(f) for f in o[1]]) for i, o in zip(mine_b, out[0])]
+    t_umax = replicas.max_over_ranks(t_u, world, dev)
+    allb = replicas.gather_results(ub, world)
+    res["bodies_48_64_96x4"] = {"seconds": round(t_umax, 4), "excitation_solves_per_s": round(12 / t_umax, 4),
+                                "flags": [b[1] for b in allb], "bodies_solved": [b[0] for b in allb]}
+    for b in bodies:
+        b[3].close()
+    return res
+
+
+def config_c4(steps, warmup):
+    """64^3 phantom at 3 mm, plane wave: absorbed-power adjoint gradient, FP64
+    and mixed precision, and the difference between the two gradients."""
     import marie_gb300 as mg
     from marie_gb300 import phantoms
     from marie_gb300.autograd import adjoint_gradient
 
     em = mg.EMconstants(FREQ)
-    res = {"config": args.config}
-    if args.config == "c1":
-        from oracle import mie
-
-        Lc, dx, R = 32, 5e-3, 0.075
-        r, er = phantoms.sphere(Lc, Lc, Lc, dx, R, 50.0, 0.5, FREQ)
-        E, _ = mg.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
-        for prec in ("fp64", "mixed"):
-            op = mg.Operator.assemble(Lc, Lc, Lc, dx, FREQ, precision=prec)
-            t, out = _timed(lambda: mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-6, solver="G"), args.steps, args.warmup)
-            res[prec] = {"seconds": t, "iter": out[3], "relres": out[2], "matvecs": len(out[4]) - 1}
-            if prec == "fp64":
-                Et = mg.E_field_Nop(out[0], op, dx**3, FREQ, E)
-                rad = np.sqrt(np.sum(r * r, axis=3))
-                core = rad < R - 0.01
-                Em = mie.MIE_SERIES(r[core][:, None, None, :], R, 50.0, 0.5, FREQ)[:, 0, 0, :]
-                res["mie_rel_l2_error_core"] = float(np.linalg.norm(Et[core] - Em) / np.linalg.norm(Em))
-    elif args.config == "c3":
-        r, er = make_problem(0)
-        pos = phantoms.dipole_ring(0.15, [-0.05, 0.0, 0.05, 0.10], 4)
-        Es = [mg.Dipole_Excitation(r, em["ko"], np.array([[0, 0, 1.0]]), p[None]) for p in pos]
-        Eb = np.asfortranarray(np.stack(Es, axis=4))
-        del Es
-        op = mg.Operator.assemble(L, M, N, DX, FREQ, precision="mixed", nrhs_max=16)
-        t, out = _timed(lambda: mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, tol=TOL), args.steps, args.warmup)
-        res["batch16"] = {"seconds": t, "excitation_solves_per_s": 16 / t, "flags": out[1].tolist(),
-                          "max_relres": float(out[2].max()), "iters": out[3].tolist()}
-        del Eb, op
-        bodies = []
-        for seed, Lb in ((1, 48), (2, 64), (3, 96)):
-            rb, erb, _ = phantoms.ellipsoids(Lb, Lb, Lb, DX, N_ELL, seed, FREQ)
-            pb = phantoms.dipole_ring(0.15, [0.0], 4)
-            Eb = np.asfortranarray(np.stack([mg.Dipole_Excitation(rb, em["ko"], np.array([[0, 0, 1.0]]), p[None])
-                                             for p in pb], axis=4))
-            bodies.append((Eb, erb, rb, mg.Operator.assemble(Lb, Lb, Lb, DX, FREQ, precision="mixed", nrhs_max=4)))
-        t, out = _timed(lambda: mg.JVIE_Solver_bodies(bodies, FREQ, tol=TOL), args.steps, args.warmup)
-        res["bodies_48_64_96x4"] = {"seconds": t, "excitation_solves_per_s": 12 / t,
-                                    "flags": [o[1].tolist() for o in out[0]]}
-    elif args.config == "c4":
-        Lc, dx = 64, 3e-3
-        r, er, _ = phantoms.ellipsoids(Lc, Lc, Lc, dx, N_ELL, 0, FREQ)
-        E, _ = mg.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
-        for prec in ("fp64", "mixed"):
-            op = mg.Operator.assemble(Lc, Lc, Lc, dx, FREQ, precision=prec)
-            t, out = _timed(lambda: adjoint_gradient(op, E, er, dx, FREQ, "power", None, TOL), args.steps,
-                            args.warmup)
-            res[prec] = {"seconds_per_gradient": t, "F": out[0], "flags": out[3], "iters": out[4]}
-            res[prec + "_grad"] = out[1:3]
-        g64, gm = res.pop("fp64_grad"), res.pop("mixed_grad")
-        res["grad_rel_diff_mixed_vs_fp64"] = [float(np.linalg.norm(a - b) / np.linalg.norm(a)) for a, b in
-                                              zip(g64, gm)]
-    elif args.config == "c5":
-        Lc, Mc, Nc = 256, 192, 160
-        r, er, _ = phantoms.ellipsoids(Lc, Mc, Nc, DX, 40, 0, FREQ)
-        pos = phantoms.dipole_ring(0.2, [-0.05, 0.05], 4)
-        Es = [mg.Dipole_Excitation(r, em["ko"], np.array([[0, 0, 1.0]]), p[None]) for p in pos]
-        Eb = np.asfortranarray(np.stack(Es, axis=4))
-        t0 = time.perf_counter()
-        op = mg.Operator.assemble(Lc, Mc, Nc, DX, FREQ, precision="mixed", nrhs_max=8)
-        res["assembly_s"] = time.perf_counter() - t0
-        t, out = _timed(lambda: mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, tol=TOL), 1, 0)
-        res["batch8"] = {"seconds": t, "flags": out[1].tolist(), "max_relres": float(out[2].max()),
-                         "iters": out[3].tolist()}
-        Esum = np.asfortranarray(sum(Es))
-        t, g = _timed(lambda: adjoint_gradient(op, Esum, er, DX, FREQ, "power", None, TOL), 1, 0)
-        res["gradient"] = {"seconds": t, "F": g[0], "flags": g[3], "iters": g[4]}
+    Lc, dx = 64, 3e-3
+    r, er, _ = phantoms.ellipsoids(Lc, Lc, Lc, dx, N_ELL, 0, FREQ)
+    E, _ = mg.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [1, 0, 0])
+    res = {"workload": "64^3 ellipsoid phantom at 3 mm, plane wave, absorbed-power gradient w.r.t. eps_r and sigma"}
+    grads = {}
+    for prec in ("fp64", "mixed"):
+        op = mg.Operator.assemble(Lc, Lc, Lc, dx, FREQ, precision=prec)
+        t, out = _timed(lambda: adjoint_gradient(op, E, er, dx, FREQ, "power", None, TOL), steps, warmup)
+        res[prec] = {"seconds_per_gradient": round(t, 4), "F": out[0], "flags": out[3], "iters": out[4]}
+        grads[prec] = out[1:3]
+        op.close()
+    res["grad_rel_diff_mixed_vs_fp64"] = [float(np.linalg.norm(a - b) / np.linalg.norm(a))
+                                          for a, b in zip(grads["fp64"], grads["mixed"])]
     return res
+
+
+def config_c5():
+    """256x192x160 at 2 mm (512x384x320 FFT), 40 ellipsoids, 8 dipoles on a
+    0.2 m cylinder: assembly, the 8 excitations in one batch, and the
+    absorbed-power gradient of the summed excitation."""
+    import marie_gb300 as mg
+    from marie_gb300 import phantoms
+    from marie_gb300.autograd import adjoint_gradient
+
+    em = mg.EMconstants(FREQ)
+    Lc, Mc, Nc = 256, 192, 160
+    r, er, _ = phantoms.ellipsoids(Lc, Mc, Nc, DX, 40, 0, FREQ)
+    pos = phantoms.dipole_ring(0.2, [-0.05, 0.05], 4)
+    Es = [np.asarray(mg.Dipole_Excitation(r, em["ko"], np.array([[0, 0, 1.0]]), p[None])) for p in pos]
+    Eb = np.asfortranarray(np.stack(Es, axis=4))
+    res = {"workload": "256x192x160 at 2 mm, 40 ellipsoids, 8 dipoles (rho 0.2 m), batch + summed-excitation "
+                       "gradient"}
+    t0 = time.perf_counter()
+    op = mg.Operator.assemble(Lc, Mc, Nc, DX, FREQ, precision="mixed", nrhs_max=8)
+    res["assembly_s"] = round(time.perf_counter() - t0, 3)
+    t, out = _timed(lambda: mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, tol=TOL), 1, 0)
+    res["batch8"] = {"seconds": round(t, 4), "flags": out[1].tolist(), "max_relres": float(out[2].max()),
+                     "iters": out[3].tolist()}
+    del Eb, out
+    Esum = np.asfortranarray(sum(Es))
+    t, g = _timed(lambda: adjoint_gradient(op, Esum, er, DX, FREQ, "power", None, TOL), 1, 0)
+    res["gradient"] = {"seconds": round(t, 4), "F": g[0], "flags": g[3], "iters": g[4]}
+    op.close()
+    return res
+
+
+def run_configs(which, world, rank):
+    """The other workloads as a dict of per-config results; a failure is
+    recorded under its config instead of ending the run."""
+    import torch
+
+    import marie_gb300 as mg
+
+    out = {}
+    for c in which:
+        try:
+            if c == "c3":
+                out[c] = config_c3(1, 1, world, rank)
+            elif rank == 0:
+                out[c] = {"c1": lambda: config_c1(3, 1), "c4": lambda: config_c4(1, 1), "c5": config_c5}[c]()
+        except Exception as exc:  # noqa: BLE001 - reported in the JSON line
+            out[c] = {"error": f"{type(exc).__name__}: {exc}"}
+        torch.cuda.synchronize()
+        mg.release_cached_memory()
+    return out
 
 
 def main():
@@ -580,23 +665,39 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--solve-only", action="store_true", help="run the mixed solves only (for profilers)")
+    ap.add_argument("--configs", default="c1,c3,c4,c5",
+                    help="other workloads reported as extra keys of the main line ('' for none)")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     args = ap.parse_args()
+    from marie_gb300 import replicas
+
+    if args.gpus > 1 and not replicas.under_launcher():
+        sys.exit(replicas.relaunch(args.gpus, __file__, sys.argv[1:]))
     world, rank, local = dist_init()
+    if args.impl == "marie":
+        import torch
+
+        torch.cuda.set_device(local)
     if args.config != "c2":
+        res = run_configs([args.config], world, rank)
         if rank == 0:
-            print(json.dumps(run_extra(args), default=float))
+            print(json.dumps({"config": args.config, "n_gpus": world, **res[args.config]}, default=float))
+        replicas.finish(world)
         return
     if args.impl == "reference":
         out = run_reference(args, world, rank)
     else:
         out = run_gpu(args, world, rank, local)
+        which = [c for c in args.configs.split(",") if c] if not args.solve_only else []
+        if world > 1:
+            which = [c for c in which if c == "c3"]
+        if which:
+            extra = run_configs(which, world, rank)
+            if rank == 0 and out:
+                out["configs"] = extra
     if rank == 0 and out:
-        print(json.dumps(out))
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.destroy_process_group()
+        print(json.dumps(out, default=float))
+    replicas.finish(world)
 
 
 if __name__ == "__main__":

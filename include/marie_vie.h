@@ -336,10 +336,11 @@ int marie_plan_autotune(marie_plan* plan, int* fuse, int* fvar, int* zvar, doubl
 /* Pin a schedule as marie_plan_autotune would choose it. */
 int marie_plan_set_schedule(marie_plan* plan, int fuse, int fvar, int zvar);
 /* Krylov basis precision of the inner solves of a MARIE_MIXED plan's GMRES
- * refinement (no counterpart in the reference): MARIE_FP32 (the default; FP32
- * basis, dots and updates with FP64 reductions, Hessenberg and rotations) or
- * MARIE_FP64.  The outer residuals and the returned solution are FP64 either
- * way. */
+ * refinement (no counterpart in the reference): MARIE_FP64 (the default: the
+ * Arnoldi orthogonalisation in FP64 around the FP32 matvec) or MARIE_FP32 (an
+ * opt-in: FP32 basis, dots and updates with FP64 reductions across threads;
+ * FP64 Hessenberg and rotations).  The outer residuals and the returned
+ * solution are FP64 either way. */
 int marie_plan_set_inner_precision(marie_plan* plan, int precision);
 /* Restart length of those inner GMRES solves (no counterpart in the
  * reference): 0 (the default) uses the caller's inner_it, as the reference's

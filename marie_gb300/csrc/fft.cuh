@@ -83,6 +83,31 @@ template <typename L> struct RFirst;
 template <int R0, int... Rs> struct RFirst<RList<R0, Rs...>> { static constexpr int value = R0; };
 
 // ---------------------------------------------------------------------------
+// Butterfly additions.  An FP32 complex value is a pair of f32 registers, so a
+// complex add or subtract is one packed f32x2 instruction (PTX add/sub.rn.f32x2,
+// sm_100 and later) instead of two; results are bitwise those of two FADDs.
+// Sums that involve a multiply stay scalar so that they contract into FMAs.
+// ---------------------------------------------------------------------------
+template <typename V> __device__ __forceinline__ V badd(V a, V b) { return cadd(a, b); }
+template <typename V> __device__ __forceinline__ V bsub(V a, V b) { return csub(a, b); }
+template <> __device__ __forceinline__ float2 badd<float2>(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+      "add.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+template <> __device__ __forceinline__ float2 bsub<float2>(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+      "sub.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+
+// ---------------------------------------------------------------------------
 // Small DFTs in registers.  Forward uses exp(-2*pi*i/R); INV uses exp(+2*pi*i/R).
 // ---------------------------------------------------------------------------
 template <int R, bool INV> struct DFT;
@@ -90,17 +115,17 @@ template <int R, bool INV> struct DFT;
 template <bool INV> struct DFT<2, INV> {
   template <typename V> __device__ __forceinline__ static void run(V* v) {
     V a = v[0], b = v[1];
-    v[0] = cadd(a, b);
-    v[1] = csub(a, b);
+    v[0] = badd(a, b);
+    v[1] = bsub(a, b);
   }
 };
 
 template <bool INV> struct DFT<4, INV> {
   template <typename V> __device__ __forceinline__ static void run(V* v) {
-    V t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
-    V t2 = cadd(v[1], v[3]), t3 = rot90<INV>(csub(v[1], v[3]));
-    v[0] = cadd(t0, t2);
-    v[2] = csub(t0, t2);
+    V t0 = badd(v[0], v[2]), t1 = bsub(v[0], v[2]);
+    V t2 = badd(v[1], v[3]), t3 = rot90<INV>(bsub(v[1], v[3]));
+    v[0] = badd(t0, t2);
+    v[2] = bsub(t0, t2);
     v[1] = cadd(t1, t3);
     v[3] = csub(t1, t3);
   }
@@ -113,8 +138,8 @@ template <bool INV> struct DFT<8, INV> {
     V a[4], b[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      a[k] = cadd(v[k], v[k + 4]);
-      b[k] = csub(v[k], v[k + 4]);
+      a[k] = badd(v[k], v[k + 4]);
+      b[k] = bsub(v[k], v[k + 4]);
     }
     // b[k] *= exp(-+ i*pi*k/4)
     b[1] = INV ? mk<V>(h * (b[1].x - b[1].y), h * (b[1].x + b[1].y))
@@ -173,8 +198,8 @@ template <bool INV> struct DFT<16, INV> {
     V a[8], b[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-      a[k] = cadd(v[k], v[k + 8]);
-      b[k] = csub(v[k], v[k + 8]);
+      a[k] = badd(v[k], v[k + 8]);
+      b[k] = bsub(v[k], v[k + 8]);
     }
     twiddle16(b);
     DFT<8, INV>::run(a);

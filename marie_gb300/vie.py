@@ -196,7 +196,7 @@ class Operator:
         return self
 
     def set_inner_precision(self, precision):
-        """Krylov basis of the inner solves of a 'mixed' plan: 'fp32' (default) or 'fp64'."""
+        """Krylov basis of the inner solves of a 'mixed' plan: 'fp64' (default) or 'fp32'."""
         check(self.lib.marie_plan_set_inner_precision(self.plan, {"fp32": 32, "fp64": 64}[precision]))
         return self
 

@@ -62,3 +62,29 @@ def test_two_rank_gloo_sharding():
         owners = [r for _, _, r in res]
         assert owners == [0, 0, 0, 0, 1, 1, 1]
         assert t == 2.0
+
+
+def test_launcher_runs_two_gloo_ranks_end_to_end():
+    """The launcher bench.py uses (--gpus 2 outside torchrun re-runs the script
+    as two ranks): every unit solved exactly once, results in unit order, the
+    work split between the two ranks, n_gpus reported as 2."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    drv = Path(__file__).resolve().parent / "replica_driver.py"
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    p = subprocess.run([sys.executable, str(drv), "--gpus", "2"], capture_output=True, text=True, timeout=300,
+                       env=env)
+    assert p.returncode == 0, p.stderr[-2000:]
+    line = [l for l in p.stdout.splitlines() if l.startswith("{")][-1]
+    out = json.loads(line)
+    assert out["n_gpus"] == 2
+    got = [(r["kind"], r["unit"]) for r in out["results"]]
+    want = [("excitation", e) for e in range(16)] + [("body", b) for b in range(3)]
+    assert got == want
+    assert all(r["value"] == (r["unit"] + 1) * 499500 for r in out["results"])
+    owners = [r for _, r in out["owners"]]
+    assert sorted(set(owners)) == [0, 1] and abs(owners.count(0) - owners.count(1)) <= 1
+    assert out["seconds_max"] >= 0
