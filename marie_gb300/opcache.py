@@ -35,8 +35,11 @@ def operator_key(L: int, M: int, N: int, dx: float, freq: float, op: str = "N", 
     edge dx (floats kept exactly, as hexadecimal)."""
     if op not in ("N", "K"):
         raise ValueError("op must be 'N' or 'K'")
+    # "scheme" names what 'DIRECTFN' computes (DIRECTFN at Np_1D = 20); entries
+    # written before the library computed it (a converged quadrature under the
+    # same name) carry no scheme and miss
     return {"op": op, "grid": [int(L), int(M), int(N)], "dx": float(dx).hex(), "freq": float(freq).hex(),
-            "singular": singular if op == "N" else None}
+            "singular": singular if op == "N" else None, "scheme": 2}
 
 
 def _atomic_write(path: str, write) -> None:
