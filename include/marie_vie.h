@@ -343,9 +343,11 @@ int marie_plan_set_schedule(marie_plan* plan, int fuse, int fvar, int zvar);
  * solution are FP64 either way. */
 int marie_plan_set_inner_precision(marie_plan* plan, int precision);
 /* Restart length of those inner GMRES solves (no counterpart in the
- * reference): 0 (the default) uses the caller's inner_it, as the reference's
- * pgmres does; 1..127 overrides it for the inner solves only (the FP32 basis
- * makes long restarts affordable).  Plain FP64 / FP32 solves are unaffected. */
+ * reference): 0 (the default) uses 20 (at most the caller's inner_it) with the
+ * FP64 basis, whose FP64 Gram-Schmidt makes shorter cycles faster, and the
+ * caller's inner_it with the FP32 basis; 1..127 overrides it for the inner
+ * solves only.  Plain FP64 / FP32 solves and the outer semantics (restart of
+ * the caller, tolerance on the FP64 true residual) are unaffected. */
 int marie_plan_set_inner_restart(marie_plan* plan, int restart);
 /* Host-side fault injection for tests (no reference counterpart): the nth
  * device allocation from now on fails with MARIE_ENOMEM (0 switches it off). */

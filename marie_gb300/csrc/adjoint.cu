@@ -126,5 +126,5 @@ extern "C" int marie_jvie_adjoint_grad(marie_plan* p, const double* Einc, const 
   MARIE_TRY(finish_out(dF_deps, ge_d, V * sizeof(double), st));
   MARIE_TRY(finish_out(dF_dsigma, gs_d, V * sizeof(double), st));
   MARIE_CUDA_TRY(cudaStreamSynchronize(st));
-  return MARIE_OK;
+  return check_kernel_status(p);
 }

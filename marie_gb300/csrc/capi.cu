@@ -298,7 +298,8 @@ static int run_matvec_t(marie_plan* p, const IO* J, long long js, IO* out, long 
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[1], p->stream));
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
       }
-      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, oct, d, tw[2], nr, p->stream, kind, kind == 0 ? p->zvar : 0));
+      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, oct, d, tw[2], nr, p->stream, kind, kind == 0 ? p->zvar : 0,
+                                    kind == 0 ? &p->zt : nullptr));
       if (prof) {
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
         MARIE_CUDA_TRY(cudaEventRecord(p->ev[4], p->stream));
@@ -311,7 +312,8 @@ static int run_matvec_t(marie_plan* p, const IO* J, long long js, IO* out, long 
       MARIE_CUDA_TRY(ML::cols(false, d.Mp, A, (long long)d.Lp * d.M, sA, d.M, B, (long long)d.Lp * d.Mp, sB, d.Mp,
                               d.Lp, 3 * d.N, tw[1], nr, p->stream, d.stop, step));
       if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[2], p->stream));
-      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, oct, d, tw[2], nr, p->stream, kind, kind == 0 ? p->zvar : 0));
+      MARIE_CUDA_TRY(ML::zmul(B, sB, fN, oct, d, tw[2], nr, p->stream, kind, kind == 0 ? p->zvar : 0,
+                                    kind == 0 ? &p->zt : nullptr));
       if (prof) MARIE_CUDA_TRY(cudaEventRecord(p->ev[3], p->stream));
       MARIE_CUDA_TRY(ML::cols(true, d.Mp, B, (long long)d.Lp * d.Mp, sB, d.Mp, A, (long long)d.Lp * d.M, sA, d.M,
                               d.Lp, 3 * d.N, tw[1], nr, p->stream, d.stop, step));
@@ -445,6 +447,23 @@ __global__ void k_extract_octant(const double2* __restrict__ f, int L, int M, in
   }
 }
 
+// the N operator full along x, half along y and z: fx[q][oz][oy][kx] =
+// s * f[q][oz][oy][kx] for oy <= M, oz <= N, in FP32 (the z pass's bulk tile
+// source; the full operator already carries the x-reflection signs)
+__global__ void k_extract_fullx(const double2* __restrict__ f, int L, int M, int N, double s, float2* __restrict__ fx) {
+  const long long Lp = 2LL * L, Mp = 2LL * M, Np = 2LL * N, P = Lp * Mp * Np;
+  const long long Mo = M + 1, No = N + 1, X = Lp * Mo * No;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 6 * X; t += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(t / X);
+    long long r = t - q * X;
+    const long long kx = r % Lp;
+    r /= Lp;
+    const long long oy = r % Mo, oz = r / Mo;
+    const double2 v = f[q * P + kx + Lp * (oy + Mp * oz)];
+    fx[t] = mk<float2>((float)(v.x * s), (float)(v.y * s));
+  }
+}
+
 // full operator from the octant (inverse of k_extract_octant), scaled by s
 __global__ void k_expand_octant(const double2* __restrict__ o, int L, int M, int N, int kind, double s,
                                 double2* __restrict__ f) {
@@ -470,6 +489,77 @@ __global__ void k_expand_octant(const double2* __restrict__ o, int L, int M, int
 // has the circulant's parity symmetry to 1e-12 of its maximum (every operator
 // built by getOPERATORS does), the full array otherwise.  Scaled by 1/(8LMN).
 // kind 0: N (6 components, fN64/fN32), 1: K (3 components, fK64/fK32).
+// cuTensorMapEncodeTiled from the driver (looked up once through the runtime;
+// the library links no driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// The z pass's bulk tile source of an FP32 octant N operator: fN32x and one
+// tensor map per box width (8, 4, 2 columns) over (2L, M+1, N+1, 6) 8-byte
+// elements.  Without the driver entry point, or with N + 1 > 256 (beyond the
+// box limit), the plan keeps the per-thread tile copies.
+static int build_zt(marie_plan* p, const double2* fN_dev) {
+  const Dims& d = p->d;
+  cudaFree(p->fN32x);
+  p->fN32x = nullptr;
+  p->zt.ok = 0;
+  p->zt.err = p->kerr;
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc || d.N + 1 > 256) return MARIE_OK;
+  const long long X = (long long)d.Lp * (d.M + 1) * (d.N + 1);
+  MARIE_CUDA_TRY(cudaMalloc(&p->fN32x, 6 * X * sizeof(float2)));
+  const long long P = (long long)d.Lp * d.Mp * d.Np;
+  k_extract_fullx<<<grid_for(6 * X), 256, 0, p->stream>>>(fN_dev, d.L, d.M, d.N, 1.0 / (double)P, p->fN32x);
+  count_launch();
+  MARIE_CUDA_TRY(cudaGetLastError());
+  const cuuint64_t gd[4] = {(cuuint64_t)d.Lp, (cuuint64_t)d.M + 1, (cuuint64_t)d.N + 1, 6};
+  const cuuint64_t gs[3] = {(cuuint64_t)d.Lp * 8, (cuuint64_t)d.Lp * (d.M + 1) * 8,
+                            (cuuint64_t)d.Lp * (d.M + 1) * (d.N + 1) * 8};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  const int widths[3] = {8, 4, 2};
+  for (int i = 0; i < 3; ++i) {
+    const cuuint32_t bd[4] = {(cuuint32_t)widths[i], 1, (cuuint32_t)d.N + 1, 6};
+    const CUresult r = enc(&p->zt.map[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, p->fN32x, gd, gs, bd, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      cudaFree(p->fN32x);
+      p->fN32x = nullptr;
+      return MARIE_OK;
+    }
+  }
+  p->zt.ok = 1;
+  return MARIE_OK;
+}
+
+int check_kernel_status(marie_plan* p) {
+  if (!p || !p->kerr) return MARIE_OK;
+  int h = 0;
+  MARIE_CUDA_TRY(cudaMemcpyAsync(&h, p->kerr, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  if (h) {
+    MARIE_CUDA_TRY(cudaMemsetAsync(p->kerr, 0, sizeof(int), p->stream));
+    MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    return set_error(MARIE_ETIMEOUT, "a z-pass operator tile copy did not arrive within its time limit");
+  }
+  return MARIE_OK;
+}
+
 int install_operator(marie_plan* p, const double2* fN_dev, int kind) {
   const Dims& d = p->d;
   const long long P = (long long)d.Lp * d.Mp * d.Np;
@@ -491,7 +581,12 @@ int install_operator(marie_plan* p, const double2* fN_dev, int kind) {
   memcpy(&mx, &h[1], sizeof(double));
   const int oct = (dev <= 1e-12 * mx) ? 1 : 0;
   const long long n = oct ? NQ * O : NQ * P;
-  if (kind == 0) release_cufft_state(p);  // its full copy of fN is stale now
+  if (kind == 0) {
+    release_cufft_state(p);  // its full copy of fN is stale now
+    cudaFree(p->fN32x);
+    p->fN32x = nullptr;
+    p->zt.ok = 0;
+  }
   double2*& f64 = kind == 0 ? p->fN64 : p->fK64;
   float2*& f32 = kind == 0 ? p->fN32 : p->fK32;
   cudaFree(f64);
@@ -513,6 +608,7 @@ int install_operator(marie_plan* p, const double2* fN_dev, int kind) {
   }
   count_launch();
   MARIE_CUDA_TRY(cudaGetLastError());
+  if (kind == 0 && oct && need32) MARIE_TRY(build_zt(p, fN_dev));
   MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
   if (kind == 0) {
     p->oct = oct;
@@ -602,6 +698,11 @@ int marie_plan_create(int64_t L, int64_t M, int64_t N, int precision, int64_t nr
     }
     p->own_stream = true;
   }
+  if (cudaMalloc(&p->kerr, sizeof(int)) != cudaSuccess || cudaMemset(p->kerr, 0, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    marie_plan_destroy(p);
+    return set_error(MARIE_ENOMEM, "plan status word allocation failed");
+  }
   const int lens[3] = {p->d.Lp, p->d.Mp, p->d.Np};
   for (int a = 0; a < 3; ++a) {
     int s = MARIE_OK;
@@ -663,6 +764,8 @@ int marie_plan_destroy(marie_plan* p) {
   if (p->stream) cudaStreamSynchronize(p->stream);
   cudaFree(p->fN64);
   cudaFree(p->fN32);
+  cudaFree(p->fN32x);
+  cudaFree(p->kerr);
   cudaFree(p->fK64);
   cudaFree(p->fK32);
   for (int a = 0; a < 3; ++a) {
@@ -761,7 +864,7 @@ int marie_plan_autotune(marie_plan* p, int* fuse_out, int* fvar_out, int* zvar_o
     ms_out[4 * i + 3] = cands[i].ms;
   }
   if (count) *count = (int64_t)cands.size();
-  return MARIE_OK;
+  return check_kernel_status(p);
 }
 
 int marie_plan_set_schedule(marie_plan* p, int fuse, int fvar, int zvar) {
@@ -911,7 +1014,7 @@ int marie_mv_AN(marie_plan* p, const double* JIn0, const double* Mr, const doubl
     MARIE_TRY(run_matvec(p, precision, (const double2*)J_d, (double2*)out_d, n, (int)nrhs, inv.as<int>(), pro, ep));
   MARIE_TRY(finish_out(JOut, out_d, n * nrhs * sizeof(double2), p->stream));
   MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
-  return MARIE_OK;
+  return check_kernel_status(p);
 }
 
 int marie_mv_L(marie_plan* p, const double* JIn0, double Gram, const int64_t* idx, int64_t n_idx, double* JOut,
@@ -937,7 +1040,7 @@ int marie_mv_L(marie_plan* p, const double* JIn0, double Gram, const int64_t* id
     MARIE_TRY(run_matvec(p, precision, (const double2*)J_d, (double2*)out_d, n, (int)nrhs, inv.as<int>(), pro, ep));
   MARIE_TRY(finish_out(JOut, out_d, n * nrhs * sizeof(double2), p->stream));
   MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
-  return MARIE_OK;
+  return check_kernel_status(p);
 }
 
 int marie_mv_K(marie_plan* p, const double* JIn0, const int64_t* idx, int64_t n_idx, double* JOut, int64_t nrhs,

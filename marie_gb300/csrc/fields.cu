@@ -128,7 +128,7 @@ int marie_e_field_nop(marie_plan* p, const double* J, double Gram, double freq, 
   MARIE_CUDA_TRY(cudaGetLastError());
   MARIE_TRY(finish_out(Etot, O_d, n * sizeof(double2), st));
   MARIE_CUDA_TRY(cudaStreamSynchronize(st));
-  return MARIE_OK;
+  return check_kernel_status(p);
 }
 
 int marie_h_field_kop(marie_plan* p, const double* J, double Gram, const double* Hinc, double* Htot,

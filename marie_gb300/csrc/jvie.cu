@@ -23,6 +23,15 @@
 
 namespace marie {
 
+// Restart length of the inner GMRES of mixed-precision refinement with an FP64
+// Krylov basis (when the plan sets none).  Its Gram-Schmidt costs ~0.016 ms
+// per basis vector per step at 128^3 on the FP64 pipe, so shorter cycles win
+// although they take more matvecs: measured on the 128^3 phantom, restart
+// 12 / 20 / 30 / 50 gave 224 / 224 / 241 / 262 ms per solve (303 / 273 / 261 /
+// 236 matvecs).  With the FP32 basis the time is flat in the restart and the
+// caller's inner_it is kept.
+constexpr int kInnerRestart64 = 20;
+
 // EMconstants.m:13-20
 static constexpr double MU0 = 4e-7 * M_PI;
 static constexpr double C0 = 299792458.0;
@@ -411,7 +420,12 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
       if (!any) break;
       MARIE_TRACE("refinement step");
       std::vector<GmresResult> ri;
-      const int m_in = p->inner_restart > 0 ? p->inner_restart : inner_it;
+      // restart of the inner solves: the plan's setting, else with an FP64
+      // basis kInnerRestart64 (its Gram-Schmidt is FP64-pipe-bound, so
+      // shorter cycles win despite more matvecs), else the caller's inner_it
+      const int m_in = p->inner_restart > 0 ? p->inner_restart
+                       : p->inner_prec == MARIE_FP64 ? std::min(inner_it, kInnerRestart64)
+                                                     : inner_it;
       MARIE_TRY(gmres_batch(p, A32, L1m, R1m, Rr, n, n, S_exc, m_in, inner_tol, outer_it, D, n, ri, true, &act,
                             false, p->inner_prec == MARIE_FP32));
       MARIE_CUDA_TRY(cudaMemcpyAsync(flags.p, act.data(), S_exc * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -769,7 +783,7 @@ int marie_scat_solver(marie_plan* p, const double* Einc, const double* Hinc, dou
   }
   if (Gsar) *Gsar = ssum * Gram;
   if (Pabs) *Pabs = 0.5 * psum * Gram;
-  return MARIE_OK;
+  return check_kernel_status(p);
 }
 
 
@@ -818,7 +832,7 @@ int marie_jvie_solve(marie_plan* p, const double* Einc, const double* e_r, doubl
   if (resvec)
     for (int64_t i = 0; i < (int64_t)rv.size() && i < resvec_cap; ++i) resvec[i] = rv[i];
   if (solvert) *solvert = std::chrono::duration<double>(t1 - t0).count();
-  return MARIE_OK;
+  return check_kernel_status(p);
 }
 
 int marie_jvie2solver(marie_plan* p, const int64_t* idx, int64_t n_idx, const double* Mr, const double* Mc,
@@ -883,7 +897,7 @@ int marie_jvie2solver(marie_plan* p, const int64_t* idx, int64_t n_idx, const do
   MARIE_TRY(finish_out(Vsol, x_d, n * sizeof(double2), st));
   MARIE_CUDA_TRY(cudaStreamSynchronize(st));
   if (solvert) *solvert = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  return MARIE_OK;
+  return check_kernel_status(p);
 }
 
 int marie_jvie_solve_batch(marie_plan* p, const double* Einc, int64_t nexc, const double* e_r, double dx, double freq,
@@ -920,7 +934,7 @@ int marie_jvie_solve_batch(marie_plan* p, const double* Einc, int64_t nexc, cons
     }
   }
   if (solvert) *solvert = std::chrono::duration<double>(t1 - t0).count();
-  return MARIE_OK;
+  return check_kernel_status(p);
 }
 
 int marie_jvie_solve_bodies(int nbody, marie_plan* const* plans, const double* const* Einc, const int64_t* nexc,

@@ -481,5 +481,5 @@ extern "C" int marie_pgmres(marie_plan* p, marie_op_fn A, void* A_ctx, const dou
   if (resvec_len) *resvec_len = nr;
   if (resvec)
     for (int64_t i = 0; i < nr && i < resvec_cap; ++i) resvec[i] = res.resvec[i];
-  return MARIE_OK;
+  return check_kernel_status(p);
 }

@@ -4,5 +4,5 @@
 namespace marie {
 using V32 = MatvecLaunch<float>::V;
 template cudaError_t MatvecLaunch<float>::zmul(V32*, long long, const V32*, int, const Dims&, const V32*, int,
-                                               cudaStream_t, int, int);
+                                               cudaStream_t, int, int, const ZTile*);
 }  // namespace marie

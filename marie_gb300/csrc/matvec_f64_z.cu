@@ -4,5 +4,5 @@
 namespace marie {
 using V64 = MatvecLaunch<double>::V;
 template cudaError_t MatvecLaunch<double>::zmul(V64*, long long, const V64*, int, const Dims&, const V64*, int,
-                                                cudaStream_t, int, int);
+                                                cudaStream_t, int, int, const ZTile*);
 }  // namespace marie

@@ -1,6 +1,8 @@
 // Definitions of the matvec launchers; included only by the two translation
 // units that instantiate them (matvec_f32.cu, matvec_f64.cu).
 #pragma once
+#include <cstring>
+
 #include "matvec_fused.cuh"
 #include "matvec_launch.cuh"
 
@@ -48,9 +50,16 @@ template <typename T> struct MatvecImpl {
   }
   template <int NZ, int KIND, int VAR>
   static cudaError_t zmul_nk(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                             cudaStream_t st) {
+                             cudaStream_t st, const ZTile* zt) {
     using ZC = ZS<T, NZ, KIND, VAR>;
     constexpr int S = ZC::S;
+    // the bulk-copy tile needs a tensor map whose box is S columns wide
+    const int mi = S == 8 ? 0 : S == 4 ? 1 : S == 2 ? 2 : -1;
+    const int tma = (ZC::TMA && zt && zt->ok && oct && mi >= 0) ? 1 : 0;
+    CUtensorMap none;
+    memset(&none, 0, sizeof(none));
+    const CUtensorMap& tmap = tma ? zt->map[mi] : none;
+    int* err = zt ? zt->err : nullptr;
     const size_t smem = (size_t)ZC::bytes(S);  // S columns, 3 component buffers, operator tile
     cudaError_t e = opt_in_smem(k_zmul<T, NZ, KIND, VAR>, smem);
     if (e != cudaSuccess) return e;
@@ -65,18 +74,18 @@ template <typename T> struct MatvecImpl {
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_zmul<T, NZ, KIND, VAR>, B, bs, fN, oct, d, tw);
+    return cudaLaunchKernelEx(&cfg, k_zmul<T, NZ, KIND, VAR>, B, bs, fN, oct, d, tw, tmap, tma, err);
   }
   template <int NZ>
   static cudaError_t zmul_n(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                            cudaStream_t st, int kind, int var) {
-    if (kind == 1) return zmul_nk<NZ, 1, 0>(B, bs, fN, oct, d, tw, nrhs, st);
+                            cudaStream_t st, int kind, int var, const ZTile* zt) {
+    if (kind == 1) return zmul_nk<NZ, 1, 0>(B, bs, fN, oct, d, tw, nrhs, st, nullptr);
     if constexpr (sizeof(T) == 4) {
       if constexpr (HasWide<NZ>::value)
-        if (var == 1) return zmul_nk<NZ, 0, 1>(B, bs, fN, oct, d, tw, nrhs, st);
-      if (var == 2) return zmul_nk<NZ, 0, 2>(B, bs, fN, oct, d, tw, nrhs, st);
+        if (var == 1) return zmul_nk<NZ, 0, 1>(B, bs, fN, oct, d, tw, nrhs, st, zt);
+      if (var == 2) return zmul_nk<NZ, 0, 2>(B, bs, fN, oct, d, tw, nrhs, st, zt);
     }
-    return zmul_nk<NZ, 0, 0>(B, bs, fN, oct, d, tw, nrhs, st);
+    return zmul_nk<NZ, 0, 0>(B, bs, fN, oct, d, tw, nrhs, st, zt);
   }
 
   template <typename IO>
@@ -120,9 +129,9 @@ template <typename T> struct MatvecImpl {
     return cudaErrorInvalidValue;
   }
   static cudaError_t zmul(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                          cudaStream_t st, int kind, int var) {
+                          cudaStream_t st, int kind, int var, const ZTile* zt) {
     switch (d.Np) {
-#define MARIE_CASE(n_) case n_: return zmul_n<n_>(B, bs, fN, oct, d, tw, nrhs, st, kind, var);
+#define MARIE_CASE(n_) case n_: return zmul_n<n_>(B, bs, fN, oct, d, tw, nrhs, st, kind, var, zt);
       MARIE_FFT_LENGTHS(MARIE_CASE)
 #undef MARIE_CASE
     }
@@ -268,8 +277,8 @@ cudaError_t MatvecLaunch<T>::cols(bool inv, int NC, const V* in, long long in_w,
 }
 template <typename T>
 cudaError_t MatvecLaunch<T>::zmul(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                                  cudaStream_t st, int kind, int var) {
-  return MatvecImpl<T>::zmul(B, bs, fN, oct, d, tw, nrhs, st, kind, var);
+                                  cudaStream_t st, int kind, int var, const ZTile* zt) {
+  return MatvecImpl<T>::zmul(B, bs, fN, oct, d, tw, nrhs, st, kind, var, zt);
 }
 
 }  // namespace marie

@@ -18,6 +18,8 @@
 // fN layout: fN[q][kz][ky][kx], q in [xx,xy,xz,yy,yz,zz], pre-scaled by 1/(8LMN)
 // so that the inverse transforms need no normalisation.
 #pragma once
+#include <cuda.h>  // CUtensorMap (the type only; no driver library is linked)
+
 #include "fft.cuh"
 
 namespace marie {
@@ -321,7 +323,13 @@ template <typename T, int NZ, int KIND = 0, int VAR = 0> struct ZS {
   static constexpr int BUF = NZ * ES + (HALF ? (NZ / 16 + 1) * S : 0);  // one component's exchange buffer
   // octant operator tile of the CTA's columns: NQ components x (N+1) planes x S
   static constexpr int TILE = OpKind<KIND>::NQ * (NZ / 2 + 1) * S;
-  static constexpr long long bytes(int) { return (long long)(NZ + 3 * BUF + TILE) * sizeof(cplx<T>); }
+  // + 128 bytes so that the tile can start on a 128-byte boundary (bulk tensor copies)
+  static constexpr long long bytes(int) { return (long long)(NZ + 3 * BUF + TILE) * sizeof(cplx<T>) + 128; }
+  // The tile arrives by one bulk tensor copy (cp.async.bulk.tensor) from the
+  // FP32 N operator stored full along x: needs FP32 values, the N operator, an
+  // even column count (the box starts on a 16-byte boundary) and at most 256
+  // octant planes (the box limit).
+  static constexpr bool TMA = sizeof(T) == 4 && KIND == 0 && S % 2 == 0 && NZ / 2 + 1 <= 256;
   __device__ static SAddr addr() { return SAddr(ES, false, HALF ? S : 0); }
 };
 
@@ -434,10 +442,21 @@ __device__ __forceinline__ void zrow_k(V* reg, int t, int s, bool active, int oc
 // the forward transforms the three spectra meet in shared memory; group c
 // forms row c of the symmetric product and runs its inverse transform from
 // the registers (the inverse radix order starts where the forward ended).
+//
+// Operator tile (octant operators, oct = 1): with tma = 1 (FP32 N operator)
+// one thread issues a single bulk tensor copy of the S columns x (N+1) planes
+// x 6 components from the copy of the operator stored full along x (x
+// reflections already carry their signs there) and every thread waits on the
+// copy's mbarrier, with a time limit after which err is set and the pass goes
+// on; the y reflection is applied as N -> D N D with D = diag(1, -1, 1) on the
+// y component's spectrum and product row (the symmetric tensor's xy and yz
+// entries are the odd ones in y), the z reflection by the sign of the z-odd
+// entries per position.  Otherwise every thread copies its share of the tile
+// from the octant with cp.async and signs the x and y reflections in place.
 template <typename T, int NZ, int KIND, int VAR>
 __global__ void __launch_bounds__(ZS<T, NZ, KIND, VAR>::THREADS)
 k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN, int oct, Dims d,
-       const cplx<T>* __restrict__ tw) {
+       const cplx<T>* __restrict__ tw, const __grid_constant__ CUtensorMap tmap, int tma, int* err) {
   if (rhs_skipped(d, blockIdx.z)) return;
   using V = cplx<T>;
   using ZC = ZS<T, NZ, KIND, VAR>;
@@ -461,7 +480,9 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   const int rem = threadIdx.x - c * S * FF::T;
   const int s = rem % S, t = rem / S;
   V* Bp = B + blockIdx.z * b_rhs + c * comp + (long long)ky * d.Lp + kx0;
-  V* tile = buf + 3 * BUF;  // octant operator of the CTA's columns, [q][oz][s]
+  V* tile = buf + 3 * BUF;  // operator tile of the CTA's columns, [q][oz][s], 128-byte aligned
+  tile = reinterpret_cast<V*>(reinterpret_cast<char*>(tile) +
+                              ((128u - ((unsigned)__cvta_generic_to_shared(tile) & 127u)) & 127u));
   const bool active = kx0 + s < d.Lp;
   const bool fy = oct && ky > d.M;
   const int oy = fy ? d.Mp - ky : ky;
@@ -472,7 +493,25 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   // row0, row0 + STEP, ... (THREADS is a multiple of S).
   constexpr int ROWS = OK::NQ * NO, STEP = ZC::THREADS / S;
   const int row0 = threadIdx.x / S;
-  if (oct && active) {
+  const bool bulk = ZC::TMA && tma && oct;
+  __shared__ __align__(8) unsigned long long tile_bar;
+  const unsigned bar = (unsigned)__cvta_generic_to_shared(&tile_bar);
+  if (bulk) {
+    if (threadIdx.x == 0) {
+      // box origin (kx0, oy, 0, 0): kx0 is a multiple of the even S, so the
+      // copy starts on a 16-byte boundary; the box (S x 1 x NO x 6) lies
+      // inside the (Lp, M+1, N+1, 6) tensor
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      const unsigned bytes = (unsigned)(OK::NQ * NO * S * sizeof(V));
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+      asm volatile(
+          "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+          "%5}], [%6];" ::"r"((unsigned)__cvta_generic_to_shared(tile)),
+          "l"(reinterpret_cast<unsigned long long>(&tmap)), "r"(kx0), "r"(oy), "r"(0), "r"(0), "r"(bar)
+          : "memory");
+    }
+  } else if (oct && active) {
     // the operator tile streams into shared memory while the forward
     // transforms run (its latency was the z pass's main stall)
     const int kx = kx0 + s;
@@ -503,9 +542,36 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   __syncthreads();  // twiddles staged
   V* my = buf + c * BUF + s;
   FF::run_half(reg, my, ad, t, tw_s);
+  // D N D with D = diag(1, -1, 1) for a y-reflected column (bulk tile only)
+  const bool neg_y = bulk && c == 1 && fy;
+  if (neg_y) {
+#pragma unroll
+    for (int i = 0; i < E; ++i) reg[i] = mk<V>(-reg[i].x, -reg[i].y);
+  }
   __syncthreads();
   FF::store(reg, my, ad, t);
-  if (oct && active) {
+  if (bulk) {
+    // wait for the tile, at most ~2 s of global time; then flag it and go on
+    // (the values are wrong, the status word tells the host)
+    unsigned long long t_start;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
+    for (;;) {
+      unsigned done;
+      asm volatile(
+          "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+          "selp.u32 %0, 1, 0, p;\n\t}"
+          : "=r"(done)
+          : "r"(bar)
+          : "memory");
+      if (done) break;
+      unsigned long long t_now;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_now));
+      if (t_now - t_start > 2000000000ull) {
+        if (err) atomicExch(err, 1);
+        break;
+      }
+    }
+  } else if (oct && active) {
     // each thread signs the tile entries it copied: reflections in x and y
     // flip the components odd along that axis
     cp_async_wait_all();
@@ -551,6 +617,10 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
       zrow_k<1, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, bc, ad);
     else
       zrow_k<2, FF, V, NZ, S>(reg, t, s, active, oct, tile, fp, fq, fplane, bc, ad);
+  }
+  if (neg_y) {
+#pragma unroll
+    for (int i = 0; i < E; ++i) reg[i] = mk<V>(-reg[i].x, -reg[i].y);
   }
   pdl_trigger();
   FI::run(reg, my, ad, t, tw_s);

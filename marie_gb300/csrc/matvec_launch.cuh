@@ -26,6 +26,16 @@ template <typename K> inline cudaError_t opt_in_smem(K kernel, size_t bytes) {
   return e;
 }
 
+// The z pass's operator tile by bulk tensor copy (FP32 N operator): tensor
+// maps over the plan's copy of the operator stored full along x,
+// fN32x[q][oz][oy][kx] (2L x (M+1) x (N+1) x 6), one per box width of 8, 4
+// and 2 columns, and the device word a pass sets when a copy does not arrive.
+struct ZTile {
+  CUtensorMap map[3];
+  int ok = 0;
+  int* err = nullptr;
+};
+
 // IO: the type of the matvec's input and output vectors (double2, or float2
 // for FP32 arithmetic T = float)
 template <typename T> struct MatvecLaunch {
@@ -41,8 +51,9 @@ template <typename T> struct MatvecLaunch {
                           cudaStream_t st, const int* stop = nullptr, int step = 0);
   // kind 0: the symmetric N operator (6 components), 1: the K operator (3);
   // var: the z-pass variant chosen by the autotuner (FP32, N operator)
+  // zt: the bulk-copy tile source of an FP32 N operator (null: per-thread copies)
   static cudaError_t zmul(V* B, long long bs, const V* fN, int oct, const Dims& d, const V* tw, int nrhs,
-                          cudaStream_t st, int kind = 0, int var = 0);
+                          cudaStream_t st, int kind = 0, int var = 0, const ZTile* zt = nullptr);
   // fused x+y passes (thread-block clusters); fused() says whether this grid has them
   static bool fused(const Dims& d);
   // fvar: 0 the default x/y radix schedules, 1 the narrow (radix-8) ones

@@ -7,7 +7,7 @@
 #include <vector>
 
 #include "common.cuh"
-#include "matvec_kernels.cuh"
+#include "matvec_launch.cuh"
 #include "trace.h"
 
 struct marie_plan {
@@ -28,6 +28,16 @@ struct marie_plan {
   int inner_prec = MARIE_FP64;  // Krylov basis of the mixed-precision inner solves
   int inner_restart = 0;        // their restart length (0: the caller's inner_it)
   int oct = 0;  // 1: fN64/fN32 hold the (L+1)(M+1)(N+1) octant, 0: the full array
+
+  // The FP32 N operator stored full along x for the z pass's bulk tile copy
+  // (fN32x[q][oz][oy][kx], 2L x (M+1) x (N+1) x 6, x reflections signed in),
+  // with its tensor maps; built beside the octant when the operator has the
+  // circulant parity symmetry and N + 1 <= 256.
+  float2* fN32x = nullptr;
+  marie::ZTile zt{};
+  // Device status word of the kernels' bounded waits (1: a tile copy did not
+  // arrive in time); read and cleared by check_kernel_status.
+  int* kerr = nullptr;
 
   // K operator (mv_K, H_field_Kop), same scaling and layouts with 3 components.
   double2* fK64 = nullptr;
@@ -136,6 +146,11 @@ int run_matvec32(marie_plan* p, const float2* J, long long js, float2* out, long
 // Scale fN by 1/(8LMN) into the plan's FP64/FP32 copies (fN_dev: full layout).
 // kind 0: the N operator (6 components), 1: the K operator (3 components).
 int install_operator(marie_plan* p, const double2* fN_dev, int kind = 0);
+
+// Reads the plan's kernel status word after the plan's stream has finished
+// (a synchronising copy), clears it and returns MARIE_ETIMEOUT if a kernel's
+// bounded wait ran out.
+int check_kernel_status(marie_plan* p);
 
 // Per-DOF coefficient arrays for mv_AN: (a, b) or (pre, a) for the adjoint.
 // mode 0: a = Gram*Mr, b = Mc      mode 1: pre = Mc, a = Gram*conj(Mr)
