@@ -473,7 +473,11 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   V* tw_s = reinterpret_cast<V*>(smem_raw);
   V* buf = tw_s + NZ;  // 3 exchange buffers of BUF elements
   const int kx0 = blockIdx.x * S;
-  const int ky = blockIdx.y;
+  // grid rows in the order 0, M, 1, 2M-1, 2, 2M-2, ...: the two rows that
+  // read the same operator tile (ky and its y reflection 2M - ky) run one
+  // grid row apart, so the second copy finds the tile in L2
+  const int gy = blockIdx.y;
+  const int ky = gy == 0 ? 0 : gy == 1 ? d.M : (gy & 1) ? d.Mp - (gy >> 1) : (gy >> 1);
   const long long plane = (long long)d.Lp * d.Mp;  // one z-plane of B
   const long long comp = plane * NH;                // one component of B
   const int c = threadIdx.x / (S * FF::T);
