@@ -352,6 +352,12 @@ int marie_plan_set_inner_restart(marie_plan* plan, int restart);
 /* Host-side fault injection for tests (no reference counterpart): the nth
  * device allocation from now on fails with MARIE_ENOMEM (0 switches it off). */
 void marie_inject_alloc_failure(int64_t nth);
+/* Test of the bounded waits (no reference counterpart): the next n z passes
+ * that load their operator tile by bulk copy arm its barrier for 16 bytes more
+ * than the copy delivers and wait 5 ms instead of 2 s; the pass then finishes
+ * with a wrong product and the entry point returns MARIE_ETIMEOUT (the plan
+ * stays usable).  Nothing faults or hangs: the copy itself completes. */
+void marie_inject_tile_timeout(int64_t n);
 int marie_plan_profile(marie_plan* plan, int enable, double* pass_ms, int64_t* count);
 
 #ifdef __cplusplus

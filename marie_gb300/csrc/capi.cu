@@ -19,6 +19,14 @@ static std::atomic<long long> g_launches{0};
 
 void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+static std::atomic<long long> g_tile_timeouts{0};
+bool take_tile_timeout_injection() {
+  long long left = g_tile_timeouts.load();
+  while (left > 0 && !g_tile_timeouts.compare_exchange_weak(left, left - 1)) {
+  }
+  return left > 0;
+}
+
 int sm_count() {
   static std::atomic<int> cache[64] = {};
   int dev = 0;
@@ -910,6 +918,8 @@ int marie_release_cached_memory(void) {
 int64_t marie_launch_count(void) { return g_launches.load(); }
 
 void marie_inject_alloc_failure(int64_t nth) { g_fail_alloc_in.store(nth > 0 ? nth : 0); }
+
+void marie_inject_tile_timeout(int64_t n) { g_tile_timeouts.store(n > 0 ? n : 0); }
 
 int marie_plan_profile(marie_plan* p, int enable, double* pass_ms, int64_t* count) {
   if (!p) return set_error(MARIE_EINVAL, "NULL plan");

@@ -43,6 +43,10 @@ int set_error(int code, const char* fmt, ...);
 // Counts kernel launches issued by this library (marie_launch_count).
 void count_launch(long long n = 1);
 
+// Test injection (marie_inject_tile_timeout): true once for each z-pass launch
+// that should arm its tile barrier for more bytes than the copy delivers.
+bool take_tile_timeout_injection();
+
 // Streaming multiprocessors of the current device (queried once per device).
 int sm_count();
 

@@ -55,7 +55,8 @@ template <typename T> struct MatvecImpl {
     constexpr int S = ZC::S;
     // the bulk-copy tile needs a tensor map whose box is S columns wide
     const int mi = S == 8 ? 0 : S == 4 ? 1 : S == 2 ? 2 : -1;
-    const int tma = (ZC::TMA && zt && zt->ok && oct && mi >= 0) ? 1 : 0;
+    int tma = (ZC::TMA && zt && zt->ok && oct && mi >= 0) ? 1 : 0;
+    if (tma && take_tile_timeout_injection()) tma = 2;  // test: a wait that runs out
     CUtensorMap none;
     memset(&none, 0, sizeof(none));
     const CUtensorMap& tmap = tma ? zt->map[mi] : none;

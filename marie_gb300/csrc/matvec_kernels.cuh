@@ -448,7 +448,8 @@ __device__ __forceinline__ void zrow_k(V* reg, int t, int s, bool active, int oc
 // x 6 components from the copy of the operator stored full along x (x
 // reflections already carry their signs there) and every thread waits on the
 // copy's mbarrier, with a time limit after which err is set and the pass goes
-// on; the y reflection is applied as N -> D N D with D = diag(1, -1, 1) on the
+// on (tma = 2: a test of that path, the barrier armed for more bytes than the
+// copy delivers); the y reflection is applied as N -> D N D with D = diag(1, -1, 1) on the
 // y component's spectrum and product row (the symmetric tensor's xy and yz
 // entries are the odd ones in y), the z reflection by the sign of the z-odd
 // entries per position.  Otherwise every thread copies its share of the tile
@@ -507,7 +508,9 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
       // inside the (Lp, M+1, N+1, 6) tensor
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      const unsigned bytes = (unsigned)(OK::NQ * NO * S * sizeof(V));
+      // tma == 2 (a test of the bounded wait): armed for 16 bytes more than
+      // the copy delivers, so the barrier never completes
+      const unsigned bytes = (unsigned)(OK::NQ * NO * S * sizeof(V)) + (tma == 2 ? 16u : 0u);
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
       asm volatile(
           "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
@@ -555,8 +558,10 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
   __syncthreads();
   FF::store(reg, my, ad, t);
   if (bulk) {
-    // wait for the tile, at most ~2 s of global time; then flag it and go on
-    // (the values are wrong, the status word tells the host)
+    // wait for the tile, at most ~2 s of global time (5 ms in the test of
+    // this path); then flag it and go on (the values are wrong, the status
+    // word tells the host)
+    const unsigned long long limit = tma == 2 ? 5000000ull : 2000000000ull;
     unsigned long long t_start;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
     for (;;) {
@@ -570,7 +575,7 @@ k_zmul(cplx<T>* __restrict__ B, long long b_rhs, const cplx<T>* __restrict__ fN,
       if (done) break;
       unsigned long long t_now;
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_now));
-      if (t_now - t_start > 2000000000ull) {
+      if (t_now - t_start > limit) {
         if (err) atomicExch(err, 1);
         break;
       }

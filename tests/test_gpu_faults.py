@@ -1,7 +1,8 @@
 """Failure handling on the device path, with every failure made on the host
 (no kernel is made to fault, trap or hang): non-convergence is a flag,
-non-finite inputs and allocation failures are error statuses, and the
-library stays usable afterwards."""
+non-finite inputs and allocation failures are error statuses, a bounded
+device wait that runs out is a status, and the library stays usable
+afterwards."""
 import numpy as np
 import pytest
 
@@ -105,6 +106,35 @@ def test_other_solvers_flags_zero_rhs_and_allocation_failures(solver, precision)
             lib.marie_inject_alloc_failure(0)
     out = mg.JVIE_Solver(E, er, r, FREQ, op, tol=1e-8, solver=solver)
     assert out[1] == 0 and out[2] <= 1e-8
+
+
+def test_bounded_tile_wait_that_runs_out_is_a_status():
+    """The z pass waits for its bulk tile copy with a time limit.  Armed (on
+    the host) for more bytes than the copy delivers, the wait runs out after
+    5 ms, the pass sets the plan's status word and finishes, mv_AN returns
+    MARIE_ETIMEOUT, and the next product is right again."""
+    import marie_gb300 as mg
+
+    L = 16
+    r, er, E = sphere(L=L, dx=2.5e-3, R=0.012)
+    S = vo.jvie_setup(E, er, r, FREQ, 2)
+    op = mg.Operator.assemble(L, L, L, 2.5e-3, FREQ, precision="mixed")
+    rng = np.random.default_rng(5)
+    n = S["idxS3"].size
+    J = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    args = (S["Mr"], S["Mc"], S["Gram"], "notransp", S["idxS3"])
+    ref = mg.mv_AN(J, op, *args, precision="fp32")
+    lib = mg.load()
+    lib.marie_inject_tile_timeout(1)
+    try:
+        with pytest.raises(mg.MarieError) as ei:
+            mg.mv_AN(J, op, *args, precision="fp32")
+        assert ei.value.code == -6
+    finally:
+        lib.marie_inject_tile_timeout(0)
+    again = mg.mv_AN(J, op, *args, precision="fp32")
+    assert np.array_equal(again, ref)
+    op.close()
 
 
 def test_release_cached_memory(cuda):
