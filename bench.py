@@ -241,11 +241,27 @@ def run_gpu(args, world, rank, local):
     ms_per_step = elapsed_max / args.steps * 1e3
     value = world * args.steps / elapsed_max
 
-    # --- e2e: the same solves through the public API with host buffers (the
-    # excitation and e_r copied in, Je copied out every solve), right after the
-    # device-resident timing so that both see the same GPU state
+    # --- e2e: the same solves through the reference-facing C ABI
+    # (marie_jvie_solve, the call a MEX gateway makes) with host buffers: the
+    # excitation and e_r copied in and Je copied out by the library every
+    # solve, into a host output allocated per solve as a gateway allocates its
+    # mxArray; right after the device-resident timing so that both see the
+    # same GPU state
     Eh, erh = np.asfortranarray(E), np.asfortranarray(er)
-    solve(op, Eh, erh, r)
+    rv_cap = 1 + RESTART * 201 * 4
+    rv = np.zeros(rv_cap)
+
+    def solve_cabi():
+        Jh = np.empty((L, M, N, 3), dtype=np.complex128, order="F")
+        flag, relres, rlen, st = C.c_int(), C.c_double(), C.c_int64(), C.c_double()
+        it = (C.c_double * 2)()
+        _lib.check(lib.marie_jvie_solve(op.plan, C.c_void_p(Eh.ctypes.data), C.c_void_p(erh.ctypes.data), DX, FREQ,
+                                        TOL, 2, b"G", b"\0", 1000, RESTART, 200, 5, C.c_void_p(Jh.ctypes.data),
+                                        C.byref(flag), C.byref(relres), it, rv.ctypes.data_as(_lib._dp), rv_cap,
+                                        C.byref(rlen), C.byref(st)))
+        return Jh, flag.value, relres.value, st.value
+
+    solve_cabi()
     barrier(world)
     torch.cuda.synchronize()
     ne2e = max(1, args.steps)
@@ -254,12 +270,13 @@ def run_gpu(args, world, rank, local):
         t0 = time.perf_counter()
         for _ in range(ne2e):
             t1 = time.perf_counter()
-            res_h = solve(op, Eh, erh, r)
+            Jh, fh, rh, lib_s = solve_cabi()
             e2e_ms.append(round(1e3 * (time.perf_counter() - t1), 2))
-            e2e_lib_ms.append(round(1e3 * res_h[5], 2))  # inside marie_jvie_solve, staging included
+            e2e_lib_ms.append(round(1e3 * lib_s, 2))  # inside marie_jvie_solve, staging included
+            assert fh == 0 and rh <= TOL, (fh, rh)
+            del Jh
         t_e2e = (time.perf_counter() - t0) / ne2e
     t_e2e = reduce_max(t_e2e, world)
-    del res_h
 
     out = {}
     if rank == 0:
