@@ -406,6 +406,7 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
       out.r[e].resvec.push_back(out.r[e].relres);
     }
     const int max_refine = 20;
+    std::vector<double> inner_tols(S_exc, 0.5);
     for (int it = 0; it < max_refine; ++it) {
       bool any = false;
       double inner_tol = 0.5;
@@ -413,8 +414,10 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
         act[e] = out.r[e].relres > tol ? 1 : 0;
         if (act[e]) {
           any = true;
-          // half of what is still missing, not below the FP32 floor
-          inner_tol = std::min(inner_tol, std::max(0.5 * tol * bn[e] / rn[e], 1e-5));
+          // half of what is still missing, not below the FP32 floor; each
+          // system of a batch stops its inner solve at its own tolerance
+          inner_tols[e] = std::min(0.5, std::max(0.5 * tol * bn[e] / rn[e], 1e-5));
+          inner_tol = std::min(inner_tol, inner_tols[e]);
         }
       }
       if (!any) break;
@@ -427,7 +430,7 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
                        : p->inner_prec == MARIE_FP64 ? std::min(inner_it, kInnerRestart64)
                                                      : inner_it;
       MARIE_TRY(gmres_batch(p, A32, L1m, R1m, Rr, n, n, S_exc, m_in, inner_tol, outer_it, D, n, ri, true, &act,
-                            false, p->inner_prec == MARIE_FP32));
+                            false, p->inner_prec == MARIE_FP32, &inner_tols));
       MARIE_CUDA_TRY(cudaMemcpyAsync(flags.p, act.data(), S_exc * sizeof(int), cudaMemcpyHostToDevice, st));
       k_add_b<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(D, X, n, flags.as<int>());
       count_launch();

@@ -628,8 +628,11 @@ static int cycle(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L
 int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const double2* B,
                 long long bs, long long n, int S, int restart, double tol, int maxit, double2* X, long long xs,
                 std::vector<GmresResult>& out, bool use_graph, const std::vector<int>* active_in,
-                bool true_residual, bool fp32_basis) {
+                bool true_residual, bool fp32_basis, const std::vector<double>* tol_s) {
   if (restart < 1 || restart > 127) return set_error(MARIE_EINVAL, "restart must be in [1, 127]");
+  if (tol_s && (int)tol_s->size() < S) return set_error(MARIE_EINVAL, "one tolerance per system");
+  // the relative tolerance of system s
+  auto tol_of = [&](int s) { return tol_s ? (*tol_s)[s] : tol; };
   if (S < 1) return set_error(MARIE_EINVAL, "need at least one system");
   cudaStream_t st = p->stream;
   BatchWork W;
@@ -673,10 +676,10 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
       return set_error(MARIE_EBREAKDOWN, "non-finite right-hand side (system %d)", s);
     // b = 0 has the exact solution x = 0 (the reference's pgmres errors out)
     out[s].resvec.push_back(bnorm[s] > 0 ? rn[s] / bnorm[s] : 0.0);
-    active[s] = (out[s].resvec.back() > tol && maxit > 0 && wanted) ? 1 : 0;
+    active[s] = (out[s].resvec.back() > tol_of(s) && maxit > 0 && wanted) ? 1 : 0;
   }
   std::vector<double> tolabs(S);
-  for (int s = 0; s < S; ++s) tolabs[s] = tol * bnorm[s];
+  for (int s = 0; s < S; ++s) tolabs[s] = tol_of(s) * bnorm[s];
   MARIE_CUDA_TRY(cudaMemcpyAsync(W.tol.p, tolabs.data(), S * sizeof(double), cudaMemcpyHostToDevice, st));
   std::vector<int> stop(S);
   std::vector<double> resv((size_t)S * restart);
@@ -721,7 +724,7 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
       for (int j = 0; j < stop[s]; ++j) out[s].resvec.push_back(resv[(size_t)s * restart + j] / bnorm[s]);
       if (!std::isfinite(out[s].resvec.back()))
         return set_error(MARIE_EBREAKDOWN, "non-finite GMRES residual (system %d, cycle %d)", s, outit[s]);
-      active[s] = (out[s].resvec.back() > tol && outit[s] < maxit) ? 1 : 0;
+      active[s] = (out[s].resvec.back() > tol_of(s) && outit[s] < maxit) ? 1 : 0;
     }
   }
   for (int s = 0; s < S; ++s) {
@@ -731,7 +734,7 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
   if (!true_residual) {
     for (int s = 0; s < S; ++s) {
       out[s].relres = out[s].resvec.back();
-      out[s].flag = out[s].relres <= tol ? 0 : 1;
+      out[s].flag = out[s].relres <= tol_of(s) ? 0 : 1;
     }
     return MARIE_OK;
   }
@@ -750,7 +753,7 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
     out[s].iter[0] = pk[s];
     out[s].iter[1] = outit[s];
     out[s].relres = bn[s] > 0 ? tr[s] / bn[s] : 0.0;
-    out[s].flag = out[s].relres <= tol ? 0 : 1;
+    out[s].flag = out[s].relres <= tol_of(s) ? 0 : 1;
   }
   return MARIE_OK;
 }

@@ -191,11 +191,12 @@ struct BatchOp {
 // pgmres semantics for S systems sharing one operator, device-driven (one
 // graph launch per restart cycle when use_graph).  x0 = 0.  active_in (may be
 // null) selects the systems to solve (others return x = 0); true_residual
-// adds the final ||b - A x|| / ||b|| (pgmres.m:175).
+// adds the final ||b - A x|| / ||b|| (pgmres.m:175); tol_s (may be null)
+// gives each system its own relative tolerance in place of tol.
 int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const double2* B,
                 long long bs, long long n, int S, int restart, double tol, int maxit, double2* X, long long xs,
                 std::vector<GmresResult>& out, bool use_graph, const std::vector<int>* active_in,
-                bool true_residual, bool fp32_basis = false);
+                bool true_residual, bool fp32_basis = false, const std::vector<double>* tol_s = nullptr);
 
 // MATLAB bicgstab semantics (the solver 'B' of JVIE_Solver.m:451-499) on
 // device vectors: iter in half steps, resvec absolute (bicgstab.cu).
