@@ -318,6 +318,11 @@ int marie_mv_AN_cufft(marie_plan* plan, const double* JIn0, const double* Mr, co
  * forward, z multiply, y inverse, x inverse) over the matvecs run since the
  * previous call, then resets and switches recording on or off. */
 int64_t marie_launch_count(void);
+/* Number of device-driven GMRES calls (the solvers' restart cycles) whose
+ * cycles after the first ran as one graph launch: a conditional WHILE node
+ * repeating one cycle and its device-side close (no counterpart in the
+ * reference; a diagnostic like marie_launch_count). */
+int64_t marie_graph_loops(void);
 /* Per-call device buffers come from a library-owned memory pool per device
  * that keeps freed blocks for the next call (no reference counterpart).  This
  * returns the cached blocks to the device (after synchronising it); plans and

@@ -81,6 +81,7 @@ SIGNATURES = {
     "marie_e_field_nop": (C.c_int, [_vp, _vp, C.c_double, C.c_double, _vp, _vp, C.c_int]),
     "marie_plane_wave": (C.c_int, [_vp, C.c_int64, C.c_int64, C.c_int64, _vp, _vp, _vp]),
     "marie_launch_count": (C.c_int64, []),
+    "marie_graph_loops": (C.c_int64, []),
     "marie_release_cached_memory": (C.c_int, []),
     "marie_plan_autotune": (C.c_int, [_vp, _ip, _ip, _ip, _dp, C.c_int64, _i64p]),
     "marie_plan_set_schedule": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),

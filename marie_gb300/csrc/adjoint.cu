@@ -24,12 +24,6 @@
 
 namespace marie {
 
-static constexpr double MU0_ = 4e-7 * M_PI;
-static constexpr double C0_ = 299792458.0;
-static inline double eps0_() { return 1.0 / (C0_ * C0_ * MU0_); }
-
-static inline int gridn(long long n) { return grid_stride_blocks(n, 8); }
-
 // E_k = J_k / (j omega eps0 chi_v) on body DOFs; w_k = dF/dE_k; per-block F partials
 __global__ void k_adj_fields(const double2* __restrict__ J, const int64_t* __restrict__ idx3, long long n,
                              long long V, const double2* __restrict__ er, double omega_eps0, int objective,

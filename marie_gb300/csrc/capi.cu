@@ -20,6 +20,8 @@ static std::atomic<long long> g_launches{0};
 void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 static std::atomic<long long> g_tile_timeouts{0};
+static std::atomic<long long> g_graph_loops{0};
+void count_graph_loop() { g_graph_loops.fetch_add(1, std::memory_order_relaxed); }
 bool take_tile_timeout_injection() {
   long long left = g_tile_timeouts.load();
   while (left > 0 && !g_tile_timeouts.compare_exchange_weak(left, left - 1)) {
@@ -125,15 +127,7 @@ int DBuf::alloc(size_t bytes, cudaStream_t st) {
   return MARIE_OK;
 }
 
-bool is_device_ptr(const void* ptr) {
-  if (!ptr) return false;
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
-}
+bool is_device_ptr(const void* ptr) { return ptr && host_kind(ptr) == HostKind::Device; }
 
 int stage_in(const void* user, size_t bytes, cudaStream_t st, DBuf& tmp, const void** dev) {
   if (is_device_ptr(user)) {
@@ -141,7 +135,7 @@ int stage_in(const void* user, size_t bytes, cudaStream_t st, DBuf& tmp, const v
     return MARIE_OK;
   }
   MARIE_TRY(tmp.alloc(bytes, st));
-  MARIE_CUDA_TRY(cudaMemcpyAsync(tmp.p, user, bytes, cudaMemcpyHostToDevice, st));
+  MARIE_TRY(copy_to_device(tmp.p, user, bytes, st));
   *dev = tmp.p;
   return MARIE_OK;
 }
@@ -157,10 +151,7 @@ int stage_out(void* user, size_t bytes, cudaStream_t st, DBuf& tmp, void** dev) 
 }
 
 int finish_out(void* user, const void* dev, size_t bytes, cudaStream_t st) {
-  if (user != dev) {
-    MARIE_CUDA_TRY(cudaMemcpyAsync(user, dev, bytes, cudaMemcpyDeviceToHost, st));
-    MARIE_CUDA_TRY(cudaStreamSynchronize(st));
-  }
+  if (user != dev) MARIE_TRY(copy_to_host(user, dev, bytes, st));
   return MARIE_OK;
 }
 
@@ -916,6 +907,8 @@ int marie_release_cached_memory(void) {
 }
 
 int64_t marie_launch_count(void) { return g_launches.load(); }
+
+int64_t marie_graph_loops(void) { return g_graph_loops.load(); }
 
 void marie_inject_alloc_failure(int64_t nth) { g_fail_alloc_in.store(nth > 0 ? nth : 0); }
 

@@ -47,6 +47,10 @@ void count_launch(long long n = 1);
 // that should arm its tile barrier for more bytes than the copy delivers.
 bool take_tile_timeout_injection();
 
+// Counts GMRES calls whose restart cycles ran in one conditional-graph launch
+// (marie_graph_loops).
+void count_graph_loop();
+
 // Streaming multiprocessors of the current device (queried once per device).
 int sm_count();
 

@@ -479,6 +479,51 @@ __global__ void kb_sub_from(const double2* __restrict__ b, long long bs, double2
 
 static inline int gx(long long n) { return grid_stride_blocks(n, 4); }
 
+// Closes one restart cycle on the device, as the host loop of gmres_batch does
+// between cycles: per active system the outer count, the last step, the
+// residual estimates appended to its history, its next activity (above its
+// tolerance and below maxit) and its stop mark for the next cycle; a
+// non-finite residual ends the loop with err = system + 1.  Sets the loop
+// condition of the conditional graph node: another cycle while any system is
+// active, never more than maxit cycles.
+__global__ void kb_cycle_close(int S, int m, int maxit, const double* __restrict__ resv,
+                               const double* __restrict__ bnorm, const double* __restrict__ tolr, int* __restrict__ stop,
+                               int* __restrict__ act, int* __restrict__ outit, int* __restrict__ pk,
+                               double* __restrict__ hist, int* __restrict__ hlen, long long cap, int* __restrict__ err,
+                               int* __restrict__ ncycles, cudaGraphConditionalHandle cond) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    if (!act[s]) continue;
+    outit[s] += 1;
+    const int k = stop[s];
+    pk[s] = k;
+    double last = 0;
+    int len = hlen[s];
+    for (int j = 0; j < k; ++j) {
+      last = resv[(long long)s * m + j] / bnorm[s];
+      if (len < cap) hist[(long long)s * cap + len++] = last;
+    }
+    hlen[s] = len;
+    bool a;
+    if (!isfinite(last)) {
+      atomicCAS(err, 0, s + 1);
+      a = false;
+    } else {
+      a = last > tolr[s] && outit[s] < maxit;
+    }
+    act[s] = a ? 1 : 0;
+    stop[s] = a ? m : 0;
+    if (a) atomicOr(&any, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int c = ++*ncycles;
+    cudaGraphSetConditional(cond, (any && *err == 0 && c < maxit) ? 1u : 0u);
+  }
+}
+
 struct BatchWork {
   int S = 0, m = 0;
   long long n = 0, ld = 0;  // rows; column stride of the basis
@@ -625,6 +670,101 @@ static int cycle(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L
   return MARIE_OK;
 }
 
+// Runs the remaining restart cycles of gmres_batch in one launch of a graph
+// whose conditional WHILE node repeats {one cycle, kb_cycle_close}; the
+// state the host loop keeps between cycles (activity, outer counts, last
+// steps, residual histories) lives on the device and is copied back once.
+// *ran = false (and nothing run) when the graph cannot be built here, e.g.
+// a driver without conditional nodes, or a history longer than 4 M entries.
+template <typename CycleFn, typename TolOf>
+static int cycles_in_one_launch(marie_plan* p, BatchWork& W, CycleFn& one_cycle, int S, int m, int maxit,
+                                std::vector<int>& active, std::vector<int>& outit, std::vector<int>& pk,
+                                const std::vector<double>& bnorm, TolOf& tol_of, std::vector<GmresResult>& out,
+                                bool* ran) {
+  *ran = false;
+  const long long cap = (long long)m * maxit;
+  if (cap <= 0 || cap * S > (4LL << 20)) return MARIE_OK;
+  cudaStream_t st = p->stream;
+  DBuf d_act, d_outit, d_pk, d_hist, d_hlen, d_bn, d_tol, d_err, d_nc;
+  MARIE_TRY(d_act.alloc(S * sizeof(int), st));
+  MARIE_TRY(d_outit.alloc(S * sizeof(int), st));
+  MARIE_TRY(d_pk.alloc(S * sizeof(int), st));
+  MARIE_TRY(d_hist.alloc((size_t)S * cap * sizeof(double), st));
+  MARIE_TRY(d_hlen.alloc(S * sizeof(int), st));
+  MARIE_TRY(d_bn.alloc(S * sizeof(double), st));
+  MARIE_TRY(d_tol.alloc(S * sizeof(double), st));
+  MARIE_TRY(d_err.alloc(2 * sizeof(int), st));
+  std::vector<double> tolr(S);
+  for (int s = 0; s < S; ++s) tolr[s] = tol_of(s);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(d_act.p, active.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(d_outit.p, outit.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(d_pk.p, pk.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+  MARIE_CUDA_TRY(cudaMemsetAsync(d_hlen.p, 0, S * sizeof(int), st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(d_bn.p, bnorm.data(), S * sizeof(double), cudaMemcpyHostToDevice, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(d_tol.p, tolr.data(), S * sizeof(double), cudaMemcpyHostToDevice, st));
+  MARIE_CUDA_TRY(cudaMemsetAsync(d_err.p, 0, 2 * sizeof(int), st));
+  int* err = d_err.as<int>();
+  int* ncyc = err + 1;
+  // build: graph -> WHILE node (condition 1 at every launch) -> body captured
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  size_t body_nodes = 0;
+  auto fail = [&]() {
+    cudaGetLastError();
+    if (exec) cudaGraphExecDestroy(exec);
+    if (g) cudaGraphDestroy(g);
+    return MARIE_OK;  // *ran stays false: the caller runs the per-cycle graphs
+  };
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return fail();
+  cudaGraphConditionalHandle cond;
+  if (cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) return fail();
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = cond;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) != cudaSuccess) return fail();
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  if (cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return fail();
+  const int s1 = one_cycle();
+  kb_cycle_close<<<1, 128, 0, st>>>(S, m, maxit, W.resv.as<double>(), d_bn.as<double>(), d_tol.as<double>(),
+                                    W.stop.as<int>(), d_act.as<int>(), d_outit.as<int>(), d_pk.as<int>(),
+                                    d_hist.as<double>(), d_hlen.as<int>(), cap, err, ncyc, cond);
+  cudaGraph_t captured = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(st, &captured);
+  if (s1 != MARIE_OK || ec != cudaSuccess) return fail();
+  cudaGraphGetNodes(body, nullptr, &body_nodes);
+  if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) return fail();
+  if (cudaGraphLaunch(exec, st) != cudaSuccess) return fail();
+  *ran = true;
+  count_graph_loop();
+  int hc[2];
+  std::vector<int> hlen(S), act2(S), outit2(S), pk2(S);
+  std::vector<double> hist((size_t)S * cap);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hc, err, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hlen.data(), d_hlen.p, S * sizeof(int), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(act2.data(), d_act.p, S * sizeof(int), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(outit2.data(), d_outit.p, S * sizeof(int), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(pk2.data(), d_pk.p, S * sizeof(int), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hist.data(), d_hist.p, hist.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  const cudaError_t es = cudaStreamSynchronize(st);
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(g);
+  MARIE_CUDA_TRY(es);
+  count_launch((long long)hc[1] * (long long)body_nodes);
+  for (int s = 0; s < S; ++s) {
+    for (int j = 0; j < hlen[s]; ++j) out[s].resvec.push_back(hist[(size_t)s * cap + j]);
+    active[s] = act2[s];
+    outit[s] = outit2[s];
+    pk[s] = pk2[s];
+  }
+  if (hc[0]) return set_error(MARIE_EBREAKDOWN, "non-finite GMRES residual (system %d, cycle %d)", hc[0] - 1,
+                              outit[hc[0] - 1]);
+  return MARIE_OK;
+}
+
 int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const double2* B,
                 long long bs, long long n, int S, int restart, double tol, int maxit, double2* X, long long xs,
                 std::vector<GmresResult>& out, bool use_graph, const std::vector<int>* active_in,
@@ -684,6 +824,7 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
   std::vector<int> stop(S);
   std::vector<double> resv((size_t)S * restart);
   int cycles = 0;
+  bool loop_tried = false;
   while (true) {
     bool any = false;
     for (int s = 0; s < S; ++s) {
@@ -693,6 +834,17 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
     if (!any) break;
     MARIE_TRACE("pgmres restart cycle");
     MARIE_CUDA_TRY(cudaMemcpyAsync(W.stop.p, stop.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (use_graph && cycles >= 1 && !loop_tried) {
+      // every remaining cycle in one graph launch (a conditional WHILE node
+      // whose body is one cycle and its device-side close); the per-cycle
+      // graphs below when the device or the sizes do not allow it
+      loop_tried = true;
+      bool ran = false;
+      auto one_cycle = [&]() { return run_cycle(X, Rv); };
+      MARIE_TRY(cycles_in_one_launch(p, W, one_cycle, S, restart, maxit, active, outit, pk, bnorm, tol_of, out,
+                                     &ran));
+      if (ran) break;
+    }
     if (use_graph && cycles >= 1) {
       if (!W.exec) {
         cudaGraph_t graph;

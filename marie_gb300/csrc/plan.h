@@ -95,6 +95,14 @@ struct DBuf {
 // True when ptr is device (or managed) memory of the current device.
 bool is_device_ptr(const void* ptr);
 
+enum class HostKind { Device, Pinned, Pageable };
+HostKind host_kind(const void* ptr);
+// Host-to-device copy queued on st; pageable sources of 8 MB and more go
+// through the library's pinned ring (the call returns once the source has
+// been read).  Device-to-host copy that returns once `host` holds the data.
+int copy_to_device(void* dev, const void* host, size_t bytes, cudaStream_t st);
+int copy_to_host(void* host, const void* dev, size_t bytes, cudaStream_t st);
+
 // Input view: device pointer to `bytes` of data, copying from host if needed.
 int stage_in(const void* user, size_t bytes, cudaStream_t st, DBuf& tmp, const void** dev);
 // Output view: device pointer to write to; finish_out copies back to host.

@@ -81,6 +81,25 @@ def test_jvie_solver_matches_oracle(form, precond):
     assert np.max(np.abs(out[0] - ref[0])) < 1e-8 * np.max(np.abs(ref[0]))
 
 
+def test_restart_cycles_run_in_one_graph_launch():
+    """After the first restart cycle, the remaining cycles of a GMRES call run
+    in one graph launch (a conditional WHILE node whose body is one cycle and
+    its device-side close); the solve matches the oracle's as before."""
+    import marie_gb300 as mg
+
+    L, dx = 8, 5e-3
+    r, er, E = sphere_problem(L, dx, 0.018)
+    fN = vo.getOPERATORS(r, FREQ)
+    ref = vo.JVIE_Solver(E, er, r, FREQ, fN, tol=1e-10, inner_it=10, solver="G")
+    lib = mg.load()
+    n0 = lib.marie_graph_loops()
+    out = mg.JVIE_Solver(E, er, r, FREQ, mg.Operator.from_array(fN), tol=1e-10, inner_it=10, solver="G")
+    assert ref[3][1] > 2  # several restart cycles
+    assert lib.marie_graph_loops() > n0
+    assert out[1] == ref[1] == 0 and out[3] == ref[3]
+    np.testing.assert_allclose(out[4], ref[4], rtol=1e-6, atol=1e-13)
+
+
 @pytest.mark.parametrize("precision,precond", [("fp64", 0), ("fp64", "R"), ("mixed", 0)])
 def test_batched_excitations_match_single_solves(precision, precond):
     """Several excitations of one body in one lockstep batch give the same
