@@ -354,6 +354,12 @@ int marie_plan_set_inner_precision(marie_plan* plan, int precision);
  * solves only.  Plain FP64 / FP32 solves and the outer semantics (restart of
  * the caller, tolerance on the FP64 true residual) are unaffected. */
 int marie_plan_set_inner_restart(marie_plan* plan, int restart);
+/* Batched GMRES schedule (no counterpart in the reference): 2 (the default)
+ * splits the excitations of a batch into two groups on two streams whose
+ * matvecs alternate, so that one group's FP64 Gram-Schmidt can run beside the
+ * other group's FP32 matvec; 1 steps all excitations together.  Per system the
+ * arithmetic is the same either way: the results are identical. */
+int marie_plan_set_batch_groups(marie_plan* plan, int groups);
 /* Host-side fault injection for tests (no reference counterpart): the nth
  * device allocation from now on fails with MARIE_ENOMEM (0 switches it off). */
 void marie_inject_alloc_failure(int64_t nth);

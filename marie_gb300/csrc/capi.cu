@@ -891,6 +891,13 @@ int marie_plan_set_inner_restart(marie_plan* p, int restart) {
   return MARIE_OK;
 }
 
+int marie_plan_set_batch_groups(marie_plan* p, int groups) {
+  if (!p) return set_error(MARIE_EINVAL, "NULL plan");
+  if (groups != 1 && groups != 2) return set_error(MARIE_EINVAL, "batch groups must be 1 or 2");
+  p->batch_groups = groups;
+  return MARIE_OK;
+}
+
 int marie_release_cached_memory(void) {
   // blocks freed by finished calls go back to the device; blocks in use stay
   std::lock_guard<std::mutex> lock(g_pool_mu);

@@ -534,8 +534,24 @@ struct BatchWork {
   GState gs{};
   cudaGraphExec_t exec = nullptr;
   long long graph_nodes = 0;
+  // Two groups (Sa > 0): systems [0, Sa) step on the plan's stream, [Sa, S)
+  // on st2; ev_a / ev_b order the groups' matvecs, ev_fork / ev_join bracket
+  // the steps of a cycle.
+  int Sa = 0;
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_fork = nullptr, ev_join = nullptr;
   ~BatchWork() {
     if (exec) cudaGraphExecDestroy(exec);
+    for (cudaEvent_t e : {ev_a, ev_b, ev_fork, ev_join})
+      if (e) cudaEventDestroy(e);
+    if (st2) cudaStreamDestroy(st2);
+  }
+  int init_groups() {
+    Sa = (S + 1) / 2;
+    MARIE_CUDA_TRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&ev_a, &ev_b, &ev_fork, &ev_join})
+      MARIE_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    return MARIE_OK;
   }
   int init(cudaStream_t st, int S_, int m_, long long n_, bool f32_) {
     S = S_;
@@ -594,40 +610,114 @@ static int bnorms(marie_plan* p, BatchWork& W, const double2* X, long long xs, s
   return MARIE_OK;
 }
 
-// dst = L1 A R1 src for basis columns (stride vs), FP64 or FP32 vectors
+// dst = L1 A R1 src for the basis columns (stride vs) of systems g0 ..
+// g0 + Sg - 1 (src, dst point at system g0), FP64 or FP32 vectors
 static int basis_matvec(BatchWork& W, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const double2* src,
-                        double2* dst, int k) {
-  const int S = W.S;
+                        double2* dst, int k, int g0, int Sg) {
   const long long n = W.n, vs = W.vs();
-  const int* stop = W.stop.as<int>();
+  const int* stop = W.stop.as<int>() + g0;
+  double2* t1 = W.t1.as<double2>() + g0 * n;
+  double2* t2 = W.t2.as<double2>() + g0 * n;
   long long ss = vs;
   if (R1) {
-    MARIE_TRY(R1->apply(src, ss, W.t1.as<double2>(), n, S, stop, k));
-    src = W.t1.as<double2>();
+    MARIE_TRY(R1->apply(src, ss, t1, n, Sg, stop, k));
+    src = t1;
     ss = n;
   }
   if (L1) {
-    MARIE_TRY(A.apply(src, ss, W.t2.as<double2>(), n, S, stop, k));
-    return L1->apply(W.t2.as<double2>(), n, dst, vs, S, stop, k);
+    MARIE_TRY(A.apply(src, ss, t2, n, Sg, stop, k));
+    return L1->apply(t2, n, dst, vs, Sg, stop, k);
   }
-  return A.apply(src, ss, dst, vs, S, stop, k);
+  return A.apply(src, ss, dst, vs, Sg, stop, k);
 }
 static int basis_matvec(BatchWork& W, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const float2* src,
-                        float2* dst, int k) {
-  const int S = W.S;
+                        float2* dst, int k, int g0, int Sg) {
   const long long n = W.n, vs = W.vs();
-  const int* stop = W.stop.as<int>();
+  const int* stop = W.stop.as<int>() + g0;
+  float2* t1 = W.t1f.as<float2>() + g0 * n;
+  float2* t2 = W.t2f.as<float2>() + g0 * n;
   long long ss = vs;
   if (R1) {
-    MARIE_TRY(R1->apply32(src, ss, W.t1f.as<float2>(), n, S, stop, k));
-    src = W.t1f.as<float2>();
+    MARIE_TRY(R1->apply32(src, ss, t1, n, Sg, stop, k));
+    src = t1;
     ss = n;
   }
   if (L1) {
-    MARIE_TRY(A.apply32(src, ss, W.t2f.as<float2>(), n, S, stop, k));
-    return L1->apply32(W.t2f.as<float2>(), n, dst, vs, S, stop, k);
+    MARIE_TRY(A.apply32(src, ss, t2, n, Sg, stop, k));
+    return L1->apply32(t2, n, dst, vs, Sg, stop, k);
   }
-  return A.apply32(src, ss, dst, vs, S, stop, k);
+  return A.apply32(src, ss, dst, vs, Sg, stop, k);
+}
+
+// Gram-Schmidt step k of systems g0 .. g0 + Sg - 1 on stream sm: dots,
+// update (its last block runs the Givens step) and scale
+template <typename VB>
+static void group_gs(BatchWork& W, int g0, int Sg, int k, cudaStream_t sm) {
+  const int S = W.S, m = W.m;
+  const long long vs = W.vs(), ld = W.ld;
+  VB* V = W.V.as<VB>() + g0 * vs;
+  const int* stop = W.stop.as<int>() + g0;
+  unsigned* cnt = W.cnt.as<unsigned>();
+  double2* h = W.h.as<double2>() + (long long)g0 * (m + 1);
+  GState gs = W.gs;
+  gs.H += (long long)g0 * (m + 1) * m;
+  gs.R += (long long)g0 * (m + 1) * m;
+  gs.g += (long long)g0 * (m + 1);
+  gs.cs += (long long)g0 * m;
+  gs.sn += (long long)g0 * m;
+  gs.y += (long long)g0 * m;
+  gs.res += (long long)g0 * (m + 1);
+  gs.resv += (long long)g0 * m;
+  gs.beta += g0;
+  gs.tolabs += g0;
+  gs.hn += g0;
+  gs.stop += g0;
+  kb_dots<VB><<<dim3(W.bg, Sg), BT, 0, sm>>>(V, vs, ld, k, stop, W.part_d.as<double2>() + (long long)g0 * 128 * W.bg,
+                                             cnt + g0, h, m + 1);
+  kb_update<VB><<<dim3(W.bg, Sg), BT, 0, sm>>>(V, vs, ld, k, h, m + 1, stop,
+                                               W.part_n.as<double>() + (long long)g0 * W.bg, cnt + S + g0, gs, m);
+  kb_scale<VB><<<dim3(gx(ld / BUnit<VB>::W), Sg), 256, 0, sm>>>(V, vs, ld, k, W.hn.as<double>() + g0, stop);
+  count_launch(3);
+}
+
+// The m steps of a cycle in two groups: group a's matvec, then group b's
+// matvec on the second stream while group a's Gram-Schmidt runs, then group
+// a's next matvec while group b's Gram-Schmidt runs, and so on.  The matvecs
+// alternate (they share the plan's workspace); each group's Gram-Schmidt
+// overlaps the other group's matvec.
+template <typename VB>
+static int steps_in_two_groups(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L1, const BatchOp* R1) {
+  const int Sa = W.Sa, Sb = W.S - W.Sa, m = W.m;
+  const long long ld = W.ld, vs = W.vs();
+  VB* Va = W.V.as<VB>();
+  VB* Vb = Va + Sa * vs;
+  cudaStream_t sa = p->stream, sb = W.st2;
+  MARIE_CUDA_TRY(cudaEventRecord(W.ev_fork, sa));
+  MARIE_CUDA_TRY(cudaStreamWaitEvent(sb, W.ev_fork, 0));
+  int rc = MARIE_OK;
+  cudaError_t ce = cudaSuccess;
+  for (int k = 1; k <= m; ++k) {
+    if (k > 1 && (ce = cudaStreamWaitEvent(sa, W.ev_b, 0)) != cudaSuccess) break;
+    if ((rc = basis_matvec(W, A, L1, R1, Va + (k - 1) * ld, Va + k * ld, k, 0, Sa)) != MARIE_OK) break;
+    if ((ce = cudaEventRecord(W.ev_a, sa)) != cudaSuccess) break;
+    group_gs<VB>(W, 0, Sa, k, sa);
+    if ((ce = cudaStreamWaitEvent(sb, W.ev_a, 0)) != cudaSuccess) break;
+    p->stream = sb;  // the operators launch on the plan's stream
+    rc = basis_matvec(W, A, L1, R1, Vb + (k - 1) * ld, Vb + k * ld, k, Sa, Sb);
+    p->stream = sa;
+    if (rc != MARIE_OK) break;
+    if ((ce = cudaEventRecord(W.ev_b, sb)) != cudaSuccess) break;
+    group_gs<VB>(W, Sa, Sb, k, sb);
+  }
+  p->stream = sa;
+  // join the second stream back, also after an error (a capture in progress
+  // cannot end with a stream left out)
+  const cudaError_t e1 = cudaEventRecord(W.ev_join, sb);
+  const cudaError_t e2 = cudaStreamWaitEvent(sa, W.ev_join, 0);
+  if (rc != MARIE_OK) return rc;
+  if (ce == cudaSuccess) ce = (e1 != cudaSuccess) ? e1 : e2;
+  if (ce != cudaSuccess) return set_error(MARIE_ECUDA, "two-group GMRES steps: %s", cudaGetErrorString(ce));
+  return MARIE_OK;
 }
 
 // one restart cycle for all systems with stop[s] = m (others stop[s] = 0)
@@ -643,16 +733,14 @@ static int cycle(marie_plan* p, BatchWork& W, const BatchOp& A, const BatchOp* L
   kb_norm_fin<<<S, 32, 0, st>>>(W.part_n.as<double>(), BG, stop, 1, W.beta.as<double>());
   kb_cycle_init<VB><<<dim3(gx(ld), S), 256, 0, st>>>(Rv, rs, V, vs, n, ld, W.beta.as<double>(), stop);
   count_launch(3);
-  for (int k = 1; k <= m; ++k) {
-    // V(:,k) = L1 A R1 V(:,k-1), in the basis precision
-    MARIE_TRY(basis_matvec(W, A, L1, R1, V + (long long)(k - 1) * ld, V + (long long)k * ld, k));
-    unsigned* cnt = W.cnt.as<unsigned>();
-    kb_dots<VB><<<dim3(W.bg, S), BT, 0, st>>>(V, vs, ld, k, stop, W.part_d.as<double2>(), cnt, W.h.as<double2>(),
-                                              m + 1);
-    kb_update<VB><<<dim3(W.bg, S), BT, 0, st>>>(V, vs, ld, k, W.h.as<double2>(), m + 1, stop,
-                                                W.part_n.as<double>(), cnt + S, W.gs, m);
-    kb_scale<VB><<<dim3(gx(ld / BUnit<VB>::W), S), 256, 0, st>>>(V, vs, ld, k, W.hn.as<double>(), stop);
-    count_launch(3);
+  if (W.Sa > 0) {
+    MARIE_TRY(steps_in_two_groups<VB>(p, W, A, L1, R1));
+  } else {
+    for (int k = 1; k <= m; ++k) {
+      // V(:,k) = L1 A R1 V(:,k-1), in the basis precision
+      MARIE_TRY(basis_matvec(W, A, L1, R1, V + (long long)(k - 1) * ld, V + (long long)k * ld, k, 0, S));
+      group_gs<VB>(W, 0, S, k, st);
+    }
   }
   // x += R1(V y) ; r = V(:,1:k+1) res
   kb_combine<VB><<<dim3(gx(n), S), 256, 0, st>>>(V, vs, n, ld, W.y.as<double2>(), m, stop, 0, W.t1.as<double2>(), n,
@@ -779,6 +867,7 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
   if (fp32_basis && (!A.apply32 || (L1 && !L1->apply32) || (R1 && !R1->apply32)))
     return set_error(MARIE_EINVAL, "an FP32 Krylov basis needs operators on FP32 vectors");
   MARIE_TRY(W.init(st, S, restart, n, fp32_basis));
+  if (p->batch_groups == 2 && S >= 2) MARIE_TRY(W.init_groups());
   auto run_cycle = [&](double2* Xc, double2* Rc) {
     return W.f32 ? cycle<float2>(p, W, A, L1, R1, Xc, xs, Rc, n) : cycle<double2>(p, W, A, L1, R1, Xc, xs, Rc, n);
   };

@@ -27,6 +27,7 @@ struct marie_plan {
   int zvar = 0;      // z-pass variant of the FP32 N matvec (set by marie_plan_autotune)
   int inner_prec = MARIE_FP64;  // Krylov basis of the mixed-precision inner solves
   int inner_restart = 0;        // their restart length (0: the caller's inner_it)
+  int batch_groups = 2;         // batched GMRES: systems split into this many groups on their own streams
   int oct = 0;  // 1: fN64/fN32 hold the (L+1)(M+1)(N+1) octant, 0: the full array
 
   // The FP32 N operator stored full along x for the z pass's bulk tile copy

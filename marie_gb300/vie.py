@@ -219,6 +219,12 @@ class Operator:
         check(self.lib.marie_plan_set_inner_restart(self.plan, int(restart)))
         return self
 
+    def set_batch_groups(self, groups):
+        """Batched GMRES schedule: 2 (default: two groups on two streams, one
+        group's Gram-Schmidt beside the other's matvec) or 1 (all in lockstep)."""
+        check(self.lib.marie_plan_set_batch_groups(self.plan, int(groups)))
+        return self
+
     def to_array(self):
         """The FP64 operator as a 2L x 2M x 2N x 6 numpy array."""
         ptr, arr = _out((2 * self.L, 2 * self.M, 2 * self.N, 6), False)

@@ -136,6 +136,41 @@ def test_batched_excitations_match_single_solves(precision, precond):
             assert np.max(np.abs(Jb[..., e] - ref[0])) < 1e-7 * np.max(np.abs(ref[0]))
 
 
+@pytest.mark.parametrize("precision,precond", [("fp64", 0), ("fp64", "R"), ("mixed", 0), ("mixed", "L")])
+def test_batch_in_two_groups_gives_the_same_bits(precision, precond):
+    """Two groups of excitations on two streams (one group's Gram-Schmidt
+    beside the other's matvec) give bit for bit the fields, iteration counts
+    and residual histories of the one-group lockstep batch, with an uneven
+    split (3 excitations: 2 + 1) and restart cycles in the conditional graph."""
+    import marie_gb300 as mg
+
+    L, dx = 12, 5e-3
+    r, er, E1 = sphere_problem(L, dx, 0.025)
+    em = vo.EMconstants(FREQ)
+    E2, _ = vo.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [0, 1, 0])
+    E3 = vo.Dipole_Excitation(r, em["ko"], np.array([[0, 0, 1.0]]), np.array([[0.06, 0.0, 0.01]]))
+    Eb = np.asfortranarray(np.stack([E1, E2, E3], axis=4))
+    op = mg.Operator.assemble(L, L, L, dx, FREQ, precision=precision, nrhs_max=3)
+    kw = dict(tol=1e-9, precond=precond, inner_it=8)
+    op.set_batch_groups(1)
+    one = mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, **kw)
+    lib = mg.load()
+    n0 = lib.marie_graph_loops()
+    op.set_batch_groups(2)
+    two = mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, **kw)
+    assert lib.marie_graph_loops() > n0
+    np.testing.assert_array_equal(two[0], one[0])
+    assert list(map(list, two[3])) == list(map(list, one[3]))
+    np.testing.assert_array_equal(two[2], one[2])
+    assert np.all(np.asarray(two[1]) == 0)
+    op.set_batch_groups(1)
+    again = mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, **kw)
+    np.testing.assert_array_equal(again[0], one[0])
+    with pytest.raises(mg.MarieError):
+        op.set_batch_groups(3)
+    op.close()
+
+
 def test_uneven_bodies_solved_concurrently():
     """Three bodies of different grid sizes with two dipole excitations each
     (c3 structure at test sizes) give the same fields as separate solves."""
