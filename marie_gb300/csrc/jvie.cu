@@ -291,8 +291,13 @@ static BatchOp make_bop(marie_plan* p, int prec, const JvieState& S, const doubl
       return run_matvec32(p, in, is, out, os, n, ns, inv, pro, ep, stop, step);
     };
   }
-  op.apply = [p, prec, n, inv, a, b, diag_only](const double2* in, long long is, double2* out, long long os, int ns,
-                                                const int* stop, int step) -> int {
+  // the FP32 operator on FP64 vectors (an FP64 Krylov basis) runs its
+  // epilogue in FP32 with the coefficient copies af, bf, when given
+  const float2* af_epi = prec == MARIE_FP32 ? af : nullptr;
+  const float2* bf_epi = prec == MARIE_FP32 ? bf : nullptr;
+  op.apply = [p, prec, n, inv, a, b, af_epi, bf_epi, diag_only](const double2* in, long long is, double2* out,
+                                                                long long os, int ns, const int* stop,
+                                                                int step) -> int {
     if (diag_only) {
       k_diag_b<<<dim3(grid_n(n), ns), 256, 0, p->stream>>>(a, in, is, out, os, n, stop, step);
       count_launch();
@@ -303,6 +308,8 @@ static BatchOp make_bop(marie_plan* p, int prec, const JvieState& S, const doubl
     Epilogue ep{};
     ep.a = a;
     ep.b = b;
+    ep.af = af_epi;
+    ep.bf = bf_epi;
     return run_matvec(p, prec, in, is, out, os, n, ns, inv, pro, ep, stop, step);
   };
   return op;

@@ -277,21 +277,46 @@ k_yxinv(const cplx<T>* __restrict__ B, long long bs, const IO* __restrict__ J, l
           // index loads (above), then the per-DOF loads, then the epilogue arithmetic
           // per-DOF loads in groups of EPI (bounded registers)
           constexpr int EPI = 2;
+          // FP64 vectors with FP32 coefficient copies (the matvec of the
+          // mixed-precision inner solves): the whole epilogue in FP32, the
+          // transforms' precision, with one conversion in and one out
+          constexpr bool MIX = std::is_same<IO, double2>::value && std::is_same<V, float2>::value;
+          const bool f32epi = MIX && ep.af != nullptr;
 #pragma unroll
           for (int i0 = 0; i0 < E; i0 += EPI) {
             IO jv[EPI], ak[EPI], bk[EPI];
+            float2 af[EPI], bf[EPI];
 #pragma unroll
             for (int j = 0; j < EPI; ++j) {
               const int k = kk[i0 + j];
               if (k < 0) continue;
               jv[j] = Jr[k];
-              ak[j] = EpiIO<IO>::a(ep, k);
-              bk[j] = EpiIO<IO>::b(ep, k);
+              if (f32epi) {
+                af[j] = ep.af[k];
+                bf[j] = ep.bf[k];
+              } else {
+                ak[j] = EpiIO<IO>::a(ep, k);
+                bk[j] = EpiIO<IO>::b(ep, k);
+              }
             }
 #pragma unroll
             for (int j = 0; j < EPI; ++j) {
               const int k = kk[i0 + j];
               if (k < 0) continue;
+              if constexpr (MIX) {
+                if (f32epi) {
+                  const float2 v = reg[i0 + j];
+                  float2 r32 = cmul(af[j], cvt<float2>(jv[j]));
+                  if (ep.conjout) {
+                    r32.x -= v.x;
+                    r32.y += v.y;
+                  } else {
+                    r32 = csub(r32, cmul(bf[j], v));
+                  }
+                  outr[k] = cvt<IO>(r32);
+                  continue;
+                }
+              }
               // the diagonal Gram*Mr*J term in the vectors' precision; the
               // circulant term in the transform's precision
               IO res = cmul(ak[j], jv[j]);
