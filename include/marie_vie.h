@@ -360,6 +360,13 @@ int marie_plan_set_inner_restart(marie_plan* plan, int restart);
  * other group's FP32 matvec; 1 steps all excitations together.  Per system the
  * arithmetic is the same either way: the results are identical. */
 int marie_plan_set_batch_groups(marie_plan* plan, int groups);
+/* Control of the mixed-precision refinement (no counterpart in the
+ * reference): 1 (the default) runs a MARIE_MIXED plan's GMRES solve -- every
+ * refinement step with its inner restart cycles, FP64 residuals and
+ * tolerance updates -- as one launch of a CUDA graph with nested conditional
+ * WHILE nodes, the device deciding every step; 0 drives the refinement steps
+ * from the host.  The arithmetic and the results are the same. */
+int marie_plan_set_graph_refinement(marie_plan* plan, int on);
 /* Host-side fault injection for tests (no reference counterpart): the nth
  * device allocation from now on fails with MARIE_ENOMEM (0 switches it off). */
 void marie_inject_alloc_failure(int64_t nth);

@@ -898,6 +898,13 @@ int marie_plan_set_batch_groups(marie_plan* p, int groups) {
   return MARIE_OK;
 }
 
+int marie_plan_set_graph_refinement(marie_plan* p, int on) {
+  if (!p) return set_error(MARIE_EINVAL, "NULL plan");
+  if (on != 0 && on != 1) return set_error(MARIE_EINVAL, "graph refinement must be 0 or 1");
+  p->graph_refine = on != 0;
+  return MARIE_OK;
+}
+
 int marie_release_cached_memory(void) {
   // blocks freed by finished calls go back to the device; blocks in use stay
   std::lock_guard<std::mutex> lock(g_pool_mu);

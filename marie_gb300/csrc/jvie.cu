@@ -396,24 +396,61 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
                            S.pbf.as<float2>());
     const BatchOp* L1m = precond == 'L' ? &P32 : nullptr;
     const BatchOp* R1m = precond == 'R' ? &P32 : nullptr;
-    DBuf rb, db, flags;
+    const int max_refine = 20;
+    // restart of the inner solves: the plan's setting, else with an FP64
+    // basis kInnerRestart64 (its Gram-Schmidt is FP64-pipe-bound, so
+    // shorter cycles win despite more matvecs), else the caller's inner_it
+    const int m_in = p->inner_restart > 0 ? p->inner_restart
+                     : p->inner_prec == MARIE_FP64 ? std::min(inner_it, kInnerRestart64)
+                                                   : inner_it;
+    if (p->graph_refine) {
+      // the whole refinement in one graph launch; the host-driven loop below
+      // when the graph cannot be built
+      RefineOps ops;
+      ops.add = [p, n, S_exc](const double2* D, double2* Xv, const int* fl) -> int {
+        k_add_b<<<dim3(grid_n(n), S_exc), 256, 0, p->stream>>>(D, Xv, n, fl);
+        count_launch();
+        MARIE_CUDA_TRY(cudaGetLastError());
+        return MARIE_OK;
+      };
+      ops.residual = [p, n, S_exc, &A64, Bv](const double2* Xv, double2* R, const int* fl) -> int {
+        MARIE_TRY(A64.apply(Xv, n, R, n, S_exc, fl, 1));
+        k_sub_b<<<dim3(grid_n(n), S_exc), 256, 0, p->stream>>>(Bv, R, n, fl);
+        count_launch();
+        MARIE_CUDA_TRY(cudaGetLastError());
+        return MARIE_OK;
+      };
+      bool ran = false;
+      MARIE_TRY(refine_batch_graph(p, A32, L1m, R1m, ops, Bv, n, S_exc, m_in, tol, outer_it, max_refine,
+                                   p->inner_prec == MARIE_FP32, X, out.r, &ran));
+      if (ran) return MARIE_OK;
+    }
+    DBuf rb, db, flags, nrm;
     MARIE_TRY(rb.alloc((size_t)S_exc * n * sizeof(double2), st));
     MARIE_TRY(db.alloc((size_t)S_exc * n * sizeof(double2), st));
     MARIE_TRY(flags.alloc(S_exc * sizeof(int), st));
+    MARIE_TRY(nrm.alloc((S_exc + batch_norm_scratch(S_exc)) * sizeof(double), st));
     double2* Rr = rb.as<double2>();
     double2* D = db.as<double2>();
     MARIE_CUDA_TRY(cudaMemsetAsync(X, 0, (size_t)S_exc * n * sizeof(double2), st));
     MARIE_CUDA_TRY(cudaMemcpyAsync(Rr, Bv, (size_t)S_exc * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     std::vector<double> bn(S_exc), rn(S_exc);
-    for (int e = 0; e < S_exc; ++e) MARIE_TRY(dev_norm2(p, Bv + e * n, n, &bn[e]));
+    // the norms of the graph-launched refinement (same kernels, same bits)
+    double* nrm_d = nrm.as<double>();
+    auto norms = [&](const double2* V, const int* mask, std::vector<double>& h) -> int {
+      MARIE_TRY(batch_norms_dev(p, V, n, n, S_exc, mask, nrm_d + S_exc, nrm_d));
+      MARIE_CUDA_TRY(cudaMemcpyAsync(h.data(), nrm_d, S_exc * sizeof(double), cudaMemcpyDeviceToHost, st));
+      MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+      return MARIE_OK;
+    };
+    MARIE_TRY(norms(Bv, nullptr, bn));
     rn = bn;
     std::vector<int> act(S_exc), inner_total(S_exc, 0), last_p(S_exc, 0);
     for (int e = 0; e < S_exc; ++e) {
       out.r[e].relres = rn[e] / bn[e];
       out.r[e].resvec.push_back(out.r[e].relres);
     }
-    const int max_refine = 20;
-    std::vector<double> inner_tols(S_exc, 0.5);
+    std::vector<double> inner_tols(S_exc, 0.5), rn_new(S_exc);
     for (int it = 0; it < max_refine; ++it) {
       bool any = false;
       double inner_tol = 0.5;
@@ -430,12 +467,6 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
       if (!any) break;
       MARIE_TRACE("refinement step");
       std::vector<GmresResult> ri;
-      // restart of the inner solves: the plan's setting, else with an FP64
-      // basis kInnerRestart64 (its Gram-Schmidt is FP64-pipe-bound, so
-      // shorter cycles win despite more matvecs), else the caller's inner_it
-      const int m_in = p->inner_restart > 0 ? p->inner_restart
-                       : p->inner_prec == MARIE_FP64 ? std::min(inner_it, kInnerRestart64)
-                                                     : inner_it;
       MARIE_TRY(gmres_batch(p, A32, L1m, R1m, Rr, n, n, S_exc, m_in, inner_tol, outer_it, D, n, ri, true, &act,
                             false, p->inner_prec == MARIE_FP32, &inner_tols));
       MARIE_CUDA_TRY(cudaMemcpyAsync(flags.p, act.data(), S_exc * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -446,12 +477,13 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
       k_sub_b<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(Bv, Rr, n, flags.as<int>());
       count_launch();
       MARIE_CUDA_TRY(cudaGetLastError());
+      MARIE_TRY(norms(Rr, flags.as<int>(), rn_new));
       for (int e = 0; e < S_exc; ++e) {
         if (!act[e]) continue;
         for (size_t i = 1; i < ri[e].resvec.size(); ++i) out.r[e].resvec.push_back(ri[e].resvec[i] * rn[e] / bn[e]);
         inner_total[e] += ri[e].iter[1];
         last_p[e] = ri[e].iter[0];
-        MARIE_TRY(dev_norm2(p, Rr + e * n, n, &rn[e]));
+        rn[e] = rn_new[e];
         out.r[e].relres = rn[e] / bn[e];
         out.r[e].resvec.push_back(out.r[e].relres);
       }

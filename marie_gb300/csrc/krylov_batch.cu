@@ -24,6 +24,7 @@
 // norms, the iterate and the restart residual stay FP64.
 #include <cmath>
 #include <type_traits>
+#include <algorithm>
 #include <vector>
 
 #include "plan.h"
@@ -995,6 +996,349 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
     out[s].iter[1] = outit[s];
     out[s].relres = bn[s] > 0 ? tr[s] / bn[s] : 0.0;
     out[s].flag = out[s].relres <= tol_of(s) ? 0 : 1;
+  }
+  return MARIE_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Mixed-precision refinement in one graph launch
+// ---------------------------------------------------------------------------
+size_t batch_norm_scratch(int S) { return (size_t)S * BG; }
+
+int batch_norms_dev(marie_plan* p, const double2* X, long long xs, long long n, int S, const int* mask, double* part,
+                    double* out) {
+  kb_norm_part<<<dim3(BG, S), BT, 0, p->stream>>>(X, xs, n, mask, 1, part);
+  kb_norm_fin<<<S, 32, 0, p->stream>>>(part, BG, mask, 1, out);
+  count_launch(2);
+  MARIE_CUDA_TRY(cudaGetLastError());
+  return MARIE_OK;
+}
+
+// rn = bn, relres = rn / bn: the state before the first refinement step
+__global__ void kr_start(int S, const double* __restrict__ bn, double* __restrict__ rn, double* __restrict__ relres) {
+  for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    rn[s] = bn[s];
+    relres[s] = rn[s] / bn[s];
+  }
+}
+
+// Opens a refinement step: act = relres > tol and, for the active systems,
+// the inner tolerance min(0.5, max(0.5 tol ||b|| / ||r||, 1e-5)) (the
+// comparisons of std::min / std::max, so that NaN propagates alike)
+__global__ void kr_open(int S, double tol, const double* __restrict__ relres, const double* __restrict__ bn,
+                        const double* __restrict__ rn, int* __restrict__ act, double* __restrict__ itol) {
+  for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    const bool a = relres[s] > tol;
+    act[s] = a ? 1 : 0;
+    if (a) {
+      double v = 0.5 * tol * bn[s] / rn[s];
+      v = (v < 1e-5) ? 1e-5 : v;
+      itol[s] = (v < 0.5) ? v : 0.5;
+    }
+  }
+}
+
+// Opens the inner GMRES of a step (x0 = 0, r = the step's residual): its
+// active systems, absolute tolerances, first-cycle stop marks and counters,
+// and the condition of the restart-cycle loop.  err: a wanted system with a
+// non-finite right-hand side.
+__global__ void kr_inner_open(int S, int m, int maxit, const int* __restrict__ act, const double* __restrict__ itol,
+                              const double* __restrict__ bnorm, const double* __restrict__ rn0,
+                              double* __restrict__ tolabs, int* __restrict__ stop, int* __restrict__ act_in,
+                              int* __restrict__ outit, int* __restrict__ pk, int* __restrict__ err,
+                              int* __restrict__ ncycles, cudaGraphConditionalHandle cond) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    const bool wanted = act[s] != 0;
+    if (wanted && !isfinite(bnorm[s])) atomicCAS(err, 0, s + 1);
+    const double r0 = bnorm[s] > 0 ? rn0[s] / bnorm[s] : 0.0;
+    const bool a = r0 > itol[s] && maxit > 0 && wanted;
+    act_in[s] = a ? 1 : 0;
+    stop[s] = a ? m : 0;
+    tolabs[s] = itol[s] * bnorm[s];
+    outit[s] = 0;
+    pk[s] = 0;
+    if (a) atomicOr(&any, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *ncycles = 0;
+    cudaGraphSetConditional(cond, (any && *err == 0) ? 1u : 0u);
+  }
+}
+
+// Closes a refinement step for the systems it moved: the step's inner
+// counts, the residual norm before (the scale of the step's inner history)
+// and after, relres, the end of the step's history; another step while any
+// system is above tol, no error occurred and fewer than max_refine ran.
+__global__ void kr_close(int S, int MR, double tol, int max_refine, const int* __restrict__ act,
+                         const int* __restrict__ outit, const int* __restrict__ pk, const double* __restrict__ rn_new,
+                         const double* __restrict__ bn, const int* __restrict__ hlen, double* __restrict__ rn,
+                         double* __restrict__ relres, int* __restrict__ inner_total, int* __restrict__ last_p,
+                         int* __restrict__ step_end, double* __restrict__ step_scale, double* __restrict__ step_relres,
+                         int* __restrict__ step_act, int* __restrict__ nstep, const int* __restrict__ err,
+                         const int* __restrict__ ncycles, int* __restrict__ cycles_total,
+                         cudaGraphConditionalHandle cond) {
+  __shared__ int any, j;
+  if (threadIdx.x == 0) {
+    any = 0;
+    j = *nstep;
+  }
+  __syncthreads();
+  for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    const long long o = (long long)s * MR + j;
+    if (act[s]) {
+      step_scale[o] = rn[s];
+      inner_total[s] += outit[s];
+      last_p[s] = pk[s];
+      rn[s] = rn_new[s];
+      relres[s] = rn[s] / bn[s];
+      step_end[o] = hlen[s];
+      step_relres[o] = relres[s];
+      step_act[o] = 1;
+    } else {
+      step_act[o] = 0;
+    }
+    if (relres[s] > tol) atomicOr(&any, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *nstep = j + 1;
+    *cycles_total += *ncycles;
+    cudaGraphSetConditional(cond, (any && *err == 0 && j + 1 < max_refine) ? 1u : 0u);
+  }
+}
+
+// Leaf nodes (no dependents) of a graph.
+static int graph_leaves(cudaGraph_t g, std::vector<cudaGraphNode_t>& out) {
+  size_t n = 0;
+  MARIE_CUDA_TRY(cudaGraphGetNodes(g, nullptr, &n));
+  std::vector<cudaGraphNode_t> all(n);
+  MARIE_CUDA_TRY(cudaGraphGetNodes(g, all.data(), &n));
+  out.clear();
+  for (cudaGraphNode_t nd : all) {
+    size_t d = 0;
+    MARIE_CUDA_TRY(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &d));
+    if (d == 0) out.push_back(nd);
+  }
+  return MARIE_OK;
+}
+
+// Kernel nodes of a graph (not counting the nodes inside conditional bodies).
+static long long kernel_nodes(cudaGraph_t g) {
+  size_t n = 0;
+  if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return 0;
+  std::vector<cudaGraphNode_t> all(n);
+  if (cudaGraphGetNodes(g, all.data(), &n) != cudaSuccess) return 0;
+  long long k = 0;
+  for (cudaGraphNode_t nd : all) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
+
+int refine_batch_graph(marie_plan* p, const BatchOp& A32, const BatchOp* L1, const BatchOp* R1, const RefineOps& ops,
+                       const double2* Bv, long long n, int S, int m, double tol, int maxit_in, int max_refine,
+                       bool fp32_basis, double2* X, std::vector<GmresResult>& out, bool* ran) {
+  *ran = false;
+  if (S < 1 || m < 1 || m > 127 || max_refine < 1) return MARIE_OK;
+  const int MR = max_refine;
+  const long long cap = (long long)m * (maxit_in > 0 ? maxit_in : 1) * MR;  // inner history entries per system
+  if (cap * S > (16LL << 20)) return MARIE_OK;
+  if (fp32_basis && (!A32.apply32 || (L1 && !L1->apply32) || (R1 && !R1->apply32))) return MARIE_OK;
+  cudaStream_t st = p->stream;
+  // matvec workspaces at their largest, so that nothing is allocated while capturing
+  MARIE_TRY(ensure_workspace(p, MARIE_FP64, S < p->nrhs_max ? S : p->nrhs_max, true));
+  BatchWork W;
+  MARIE_TRY(W.init(st, S, m, n, fp32_basis));
+  if (p->batch_groups == 2 && S >= 2) MARIE_TRY(W.init_groups());
+  DBuf rr, dd, rv, bp, dv, iv, hs, sv;
+  MARIE_TRY(rr.alloc((size_t)S * n * sizeof(double2), st));
+  MARIE_TRY(dd.alloc((size_t)S * n * sizeof(double2), st));
+  MARIE_TRY(rv.alloc((size_t)S * n * sizeof(double2), st));
+  if (L1) MARIE_TRY(bp.alloc((size_t)S * n * sizeof(double2), st));
+  // FP64 per system: bn rn rn_new relres itol bnorm_in rn_in, then the norm scratch
+  const size_t nd = 7 * (size_t)S + batch_norm_scratch(S);
+  MARIE_TRY(dv.alloc(nd * sizeof(double), st));
+  // int per system: act act_in outit pk inner_total last_p hlen allstop, then err ncycles nstep
+  MARIE_TRY(iv.alloc((8 * (size_t)S + 4) * sizeof(int), st));
+  MARIE_TRY(hs.alloc((size_t)S * cap * sizeof(double), st));
+  // per system and step: scale, relres (FP64), end, act (int)
+  MARIE_TRY(sv.alloc((size_t)S * MR * (2 * sizeof(double) + 2 * sizeof(int)), st));
+  double2 *Rr = rr.as<double2>(), *D = dd.as<double2>(), *Rv = rv.as<double2>(), *bpb = bp.as<double2>();
+  double* dp = dv.as<double>();
+  double *bn = dp, *rn = dp + S, *rn_new = dp + 2 * S, *relres = dp + 3 * S, *itol = dp + 4 * S,
+         *bnorm_in = dp + 5 * S, *rn_in = dp + 6 * S, *npart = dp + 7 * S;
+  int* ip = iv.as<int>();
+  int *act = ip, *act_in = ip + S, *outit = ip + 2 * S, *pk = ip + 3 * S, *inner_total = ip + 4 * S,
+      *last_p = ip + 5 * S, *hlen = ip + 6 * S, *allstop = ip + 7 * S, *err = ip + 8 * S, *ncyc = err + 1,
+      *nstep = err + 2, *tcyc = err + 3;
+  double* hist = hs.as<double>();
+  double* step_scale = sv.as<double>();
+  double* step_relres = step_scale + (size_t)S * MR;
+  int* step_end = reinterpret_cast<int*>(step_relres + (size_t)S * MR);
+  int* step_act = step_end + (size_t)S * MR;
+  // eager start: x = 0, r = b, ||b||, relres = 1, counters 0
+  MARIE_CUDA_TRY(cudaMemsetAsync(X, 0, (size_t)S * n * sizeof(double2), st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(Rr, Bv, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  MARIE_TRY(batch_norms_dev(p, Bv, n, n, S, nullptr, npart, bn));
+  kr_start<<<1, 128, 0, st>>>(S, bn, rn, relres);
+  count_launch();
+  MARIE_CUDA_TRY(cudaMemsetAsync(ip, 0, (8 * (size_t)S + 4) * sizeof(int), st));
+  {
+    std::vector<int> big(S, 1 << 30);
+    MARIE_CUDA_TRY(cudaMemcpyAsync(allstop, big.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+  }
+  MARIE_CUDA_TRY(cudaGetLastError());
+  MARIE_CUDA_TRY(cudaStreamSynchronize(st));  // the pageable staging vector above
+
+  // ---- the graph: WHILE(refinement step) { open ; WHILE(restart cycle) { cycle ; close } ; update ; close }
+  const long long launches0 = marie_launch_count();
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool capturing = false;
+  auto fail = [&]() {
+    if (capturing) {
+      cudaGraph_t junk = nullptr;
+      cudaStreamEndCapture(st, &junk);
+      if (junk) cudaGraphDestroy(junk);
+    }
+    cudaGetLastError();
+    if (exec) cudaGraphExecDestroy(exec);
+    if (g) cudaGraphDestroy(g);
+    count_launch(launches0 - marie_launch_count());  // nothing of the captures ran
+    return MARIE_OK;  // *ran stays false: the caller refines from the host
+  };
+  auto begin = [&](cudaGraph_t body, const cudaGraphNode_t* deps, size_t nd_) {
+    if (cudaStreamBeginCaptureToGraph(st, body, deps, nullptr, nd_, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return false;
+    capturing = true;
+    return true;
+  };
+  auto end = [&]() {
+    cudaGraph_t tmp = nullptr;
+    capturing = false;
+    return cudaStreamEndCapture(st, &tmp) == cudaSuccess;
+  };
+  auto run_cycle = [&]() {
+    return W.f32 ? cycle<float2>(p, W, A32, L1, R1, D, n, Rv, n) : cycle<double2>(p, W, A32, L1, R1, D, n, Rv, n);
+  };
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return fail();
+  cudaGraphConditionalHandle h_step, h_cycle;
+  if (cudaGraphConditionalHandleCreate(&h_step, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) return fail();
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h_step;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t n_step;
+  if (cudaGraphAddNode(&n_step, g, nullptr, nullptr, 0, &cp) != cudaSuccess) return fail();
+  cudaGraph_t b_step = cp.conditional.phGraph_out[0];
+  if (cudaGraphConditionalHandleCreate(&h_cycle, b_step, 0, 0) != cudaSuccess) return fail();
+  // step, part 1: open, inner start (x0 = 0, r = the step's residual, left preconditioning), inner open
+  if (!begin(b_step, nullptr, 0)) return fail();
+  {
+    kr_open<<<1, 128, 0, st>>>(S, tol, relres, bn, rn, act, itol);
+    count_launch();
+    int rc = cudaMemsetAsync(D, 0, (size_t)S * n * sizeof(double2), st) == cudaSuccess &&
+                     cudaMemcpyAsync(Rv, Rr, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st) ==
+                         cudaSuccess
+                 ? MARIE_OK
+                 : MARIE_ECUDA;
+    if (rc == MARIE_OK && L1) {
+      rc = L1->apply(Rv, n, W.t1.as<double2>(), n, S, allstop, 1);
+      if (rc == MARIE_OK &&
+          (cudaMemcpyAsync(Rv, W.t1.p, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+           cudaMemcpyAsync(bpb, Rv, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st) != cudaSuccess))
+        rc = MARIE_ECUDA;
+    }
+    if (rc == MARIE_OK) rc = batch_norms_dev(p, L1 ? bpb : Rr, n, n, S, nullptr, npart, bnorm_in);
+    if (rc == MARIE_OK) rc = batch_norms_dev(p, Rv, n, n, S, nullptr, npart, rn_in);
+    kr_inner_open<<<1, 128, 0, st>>>(S, m, maxit_in, act, itol, bnorm_in, rn_in, W.tol.as<double>(),
+                                     W.stop.as<int>(), act_in, outit, pk, err, ncyc, h_cycle);
+    count_launch();
+    if (!end() || rc != MARIE_OK) return fail();
+  }
+  std::vector<cudaGraphNode_t> lv;
+  if (graph_leaves(b_step, lv) != MARIE_OK) return fail();
+  cudaGraphNodeParams ip2 = {};
+  ip2.type = cudaGraphNodeTypeConditional;
+  ip2.conditional.handle = h_cycle;
+  ip2.conditional.type = cudaGraphCondTypeWhile;
+  ip2.conditional.size = 1;
+  cudaGraphNode_t n_cycle;
+  if (cudaGraphAddNode(&n_cycle, b_step, lv.data(), nullptr, lv.size(), &ip2) != cudaSuccess) return fail();
+  cudaGraph_t b_cycle = ip2.conditional.phGraph_out[0];
+  // the restart cycle and its device-side close
+  if (!begin(b_cycle, nullptr, 0)) return fail();
+  {
+    const int rc = run_cycle();
+    kb_cycle_close<<<1, 128, 0, st>>>(S, m, maxit_in, W.resv.as<double>(), bnorm_in, itol, W.stop.as<int>(), act_in,
+                                      outit, pk, hist, hlen, cap, err, ncyc, h_cycle);
+    count_launch();
+    if (!end() || rc != MARIE_OK) return fail();
+  }
+  // step, part 2: x += d, the FP64 residual and its norm, close
+  if (!begin(b_step, &n_cycle, 1)) return fail();
+  {
+    int rc = ops.add(D, X, act);
+    if (rc == MARIE_OK) rc = ops.residual(X, Rr, act);
+    if (rc == MARIE_OK) rc = batch_norms_dev(p, Rr, n, n, S, act, npart, rn_new);
+    kr_close<<<1, 128, 0, st>>>(S, MR, tol, max_refine, act, outit, pk, rn_new, bn, hlen, rn, relres, inner_total,
+                                last_p, step_end, step_scale, step_relres, step_act, nstep, err, ncyc, tcyc, h_step);
+    count_launch();
+    if (!end() || rc != MARIE_OK) return fail();
+  }
+  const long long nodes_step = kernel_nodes(b_step), nodes_cycle = kernel_nodes(b_cycle);
+  if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) return fail();
+  count_launch(launches0 - marie_launch_count());  // the captures ran nothing; counted below
+  if (cudaGraphLaunch(exec, st) != cudaSuccess) return fail();
+  *ran = true;
+  count_graph_loop();
+  // ---- results
+  std::vector<double> hd(nd), hh((size_t)S * cap), hsv((size_t)S * MR * 2);
+  std::vector<int> hi(8 * (size_t)S + 4), hsi((size_t)S * MR * 2);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hd.data(), dp, nd * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hi.data(), ip, hi.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hsv.data(), step_scale, hsv.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hsi.data(), step_end, hsi.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+  const cudaError_t es = cudaStreamSynchronize(st);
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(g);
+  MARIE_CUDA_TRY(es);
+  const int e_code = hi[8 * S], steps = hi[8 * S + 2], cycles = hi[8 * S + 3];
+  count_launch((long long)steps * nodes_step + (long long)cycles * nodes_cycle);
+  if (e_code != 0) return set_error(MARIE_EBREAKDOWN, "non-finite GMRES residual (system %d)", e_code - 1);
+  if (*std::max_element(hi.begin() + 6 * S, hi.begin() + 7 * S) > 0) {
+    MARIE_CUDA_TRY(cudaMemcpyAsync(hh.data(), hist, (size_t)S * cap * sizeof(double), cudaMemcpyDeviceToHost, st));
+    MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  const double* h_bn = hd.data();
+  const double* h_relres = hd.data() + 3 * S;
+  const double* h_scale = hsv.data();
+  const double* h_srel = hsv.data() + (size_t)S * MR;
+  const int* h_end = hsi.data();
+  const int* h_sact = hsi.data() + (size_t)S * MR;
+  out.assign(S, GmresResult());
+  for (int s = 0; s < S; ++s) {
+    GmresResult& r = out[s];
+    r.resvec.push_back(h_bn[s] / h_bn[s]);  // rn / bn before any step (rn = bn)
+    int from = 0;
+    for (int j = 0; j < steps && j < MR; ++j) {
+      const size_t o = (size_t)s * MR + j;
+      if (!h_sact[o]) continue;
+      for (int i = from; i < h_end[o] && i < cap; ++i) r.resvec.push_back(hh[(size_t)s * cap + i] * h_scale[o] / h_bn[s]);
+      from = h_end[o];
+      r.resvec.push_back(h_srel[o]);
+    }
+    r.relres = h_relres[s];
+    r.flag = r.relres <= tol ? 0 : 1;
+    r.iter[0] = hi[5 * S + s];
+    r.iter[1] = hi[4 * S + s];
   }
   return MARIE_OK;
 }

@@ -28,6 +28,7 @@ struct marie_plan {
   int inner_prec = MARIE_FP64;  // Krylov basis of the mixed-precision inner solves
   int inner_restart = 0;        // their restart length (0: the caller's inner_it)
   int batch_groups = 2;         // batched GMRES: systems split into this many groups on their own streams
+  bool graph_refine = true;     // mixed-precision refinement in one graph launch (host-driven when false)
   int oct = 0;  // 1: fN64/fN32 hold the (L+1)(M+1)(N+1) octant, 0: the full array
 
   // The FP32 N operator stored full along x for the z pass's bulk tile copy
@@ -202,6 +203,32 @@ struct BatchOp {
 // null) selects the systems to solve (others return x = 0); true_residual
 // adds the final ||b - A x|| / ||b|| (pgmres.m:175); tol_s (may be null)
 // gives each system its own relative tolerance in place of tol.
+// The FP64 side of mixed-precision refinement, on device vectors of S systems
+// (stride n), for the systems whose flag is set: X += D, and R = B - A64 X.
+struct RefineOps {
+  std::function<int(const double2* D, double2* X, const int* flags)> add;
+  std::function<int(const double2* X, double2* R, const int* flags)> residual;
+};
+
+// Mixed-precision refinement of S systems in ONE graph launch (nested
+// conditional WHILE nodes: refinement steps around the restart cycles of the
+// inner GMRES): per step, act = relres > tol; the inner FP32-operator GMRES
+// (restart m, at most maxit_in cycles, FP64 or FP32 basis) solves A d = r to
+// the system's own tolerance min(0.5, max(0.5 tol ||b|| / ||r||, 1e-5)); then
+// x += d and r = b - A64 x with FP64 norms; at most max_refine steps.  The
+// arithmetic and the results are those of the host-driven refinement; *ran =
+// false (nothing done) when the graph cannot be built, e.g. on a driver
+// without conditional nodes.  X: S x n solutions (stride n).
+int refine_batch_graph(marie_plan* p, const BatchOp& A32, const BatchOp* L1, const BatchOp* R1, const RefineOps& ops,
+                       const double2* Bv, long long n, int S, int m, double tol, int maxit_in, int max_refine,
+                       bool fp32_basis, double2* X, std::vector<GmresResult>& out, bool* ran);
+// Batched FP64 norms of S vectors (stride xs) into out[S] on the device; with
+// mask, only the systems whose mask[s] >= 1 (the others keep out[s]).  part:
+// batch_norm_scratch(S) doubles of scratch.
+size_t batch_norm_scratch(int S);
+int batch_norms_dev(marie_plan* p, const double2* X, long long xs, long long n, int S, const int* mask, double* part,
+                    double* out);
+
 int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchOp* R1, const double2* B,
                 long long bs, long long n, int S, int restart, double tol, int maxit, double2* X, long long xs,
                 std::vector<GmresResult>& out, bool use_graph, const std::vector<int>* active_in,

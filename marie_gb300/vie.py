@@ -225,6 +225,12 @@ class Operator:
         check(self.lib.marie_plan_set_batch_groups(self.plan, int(groups)))
         return self
 
+    def set_graph_refinement(self, on):
+        """Mixed-precision refinement as one graph launch (True, default) or
+        driven from the host (False); the results are the same."""
+        check(self.lib.marie_plan_set_graph_refinement(self.plan, 1 if on else 0))
+        return self
+
     def to_array(self):
         """The FP64 operator as a 2L x 2M x 2N x 6 numpy array."""
         ptr, arr = _out((2 * self.L, 2 * self.M, 2 * self.N, 6), False)

@@ -171,6 +171,45 @@ def test_batch_in_two_groups_gives_the_same_bits(precision, precond):
     op.close()
 
 
+@pytest.mark.parametrize("basis,precond,groups", [("fp64", 0, 2), ("fp64", "R", 1), ("fp32", "L", 2),
+                                                  ("fp64", "L", 1)])
+def test_graph_refinement_matches_host_driven(basis, precond, groups):
+    """The mixed-precision refinement as one graph launch (nested conditional
+    WHILE nodes, the device deciding every step) gives bit for bit the
+    fields, flags, iteration counts and residual histories of the
+    host-driven refinement, for a batch and for a single excitation."""
+    import marie_gb300 as mg
+
+    L, dx = 12, 5e-3
+    r, er, E1 = sphere_problem(L, dx, 0.025, eps_r=80.0, sigma=1.0)
+    em = vo.EMconstants(FREQ)
+    E2, _ = vo.PlaneWave_Excitation(r, [0, 0, em["ko"]], em["omega_mu"], [0, 1, 0])
+    E3 = vo.Dipole_Excitation(r, em["ko"], np.array([[0, 0, 1.0]]), np.array([[0.06, 0.0, 0.01]]))
+    Eb = np.asfortranarray(np.stack([E1, E2, E3], axis=4))
+    op = mg.Operator.assemble(L, L, L, dx, FREQ, precision="mixed", nrhs_max=3)
+    op.set_inner_precision(basis).set_batch_groups(groups).set_inner_restart(6)
+    kw = dict(tol=1e-9, precond=precond, inner_it=30)
+    lib = mg.load()
+    res = {}
+    for graph in (False, True):
+        op.set_graph_refinement(graph)
+        n0 = lib.marie_graph_loops()
+        batch = mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, **kw)
+        single = mg.JVIE_Solver(np.asfortranarray(E2), er, r, FREQ, op, solver="G", **kw)
+        res[graph] = (batch, single, lib.marie_graph_loops() - n0)
+    (bh, sh, _), (bg, sg, loops) = res[False], res[True]
+    assert loops >= 2  # the batch and the single solve each ran as one graph launch
+    np.testing.assert_array_equal(bg[0], bh[0])
+    assert list(map(list, bg[3])) == list(map(list, bh[3]))
+    np.testing.assert_array_equal(bg[2], bh[2])
+    assert list(bg[1]) == list(bh[1]) == [0, 0, 0]
+    np.testing.assert_array_equal(sg[0], sh[0])
+    assert sg[1] == sh[1] == 0 and list(sg[3]) == list(sh[3]) and sg[2] == sh[2]
+    np.testing.assert_array_equal(np.asarray(sg[4]), np.asarray(sh[4]))
+    assert len(sg[4]) > 10
+    op.close()
+
+
 def test_uneven_bodies_solved_concurrently():
     """Three bodies of different grid sizes with two dipole excitations each
     (c3 structure at test sizes) give the same fields as separate solves."""
