@@ -328,19 +328,32 @@ struct SolverArgs {
   int ritz = 5;       // pgmresDR deflation vectors
 };
 
+// Work of several bodies gathered for one graph launch: their refinement
+// jobs, the steps that follow each job (run in order after the launch), and
+// the buffers those steps need.
+struct Deferred {
+  std::vector<std::unique_ptr<RefineJob>> jobs;
+  bool launched = false;  // the jobs' graph ran
+  std::vector<std::function<int()>> after;
+  std::vector<std::shared_ptr<void>> keep;
+};
+
 static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, int S_exc, double2* X, char precond,
-                         double tol, int inner_it, int outer_it, SolveOut& out);
+                         double tol, int inner_it, int outer_it, SolveOut& out, Deferred* dfr = nullptr);
 static int solve_single(marie_plan* p, const JvieState& S, const double2* Bv, double2* X, char precond, double tol,
                         int inner_it, int outer_it, const SolverArgs& sa, SolveOut& out,
                         const double2* x0 = nullptr);
 
 // Solves the S excitations E (3V x S, column stride es) of one body.
+// With dfr, a mixed-precision 'G' solve leaves its refinement to dfr's
+// shared graph launch and the DOF scatter to dfr's steps after it.
 static int jvie_solve_core(marie_plan* p, const double2* E, long long es, int S_exc, const double2* er, double dx,
                            double freq, int form, char precond, double tol, int inner_it, int outer_it, double2* Je,
-                           long long js, SolveOut& out, const SolverArgs& sa = SolverArgs()) {
+                           long long js, SolveOut& out, const SolverArgs& sa = SolverArgs(), Deferred* dfr = nullptr) {
   cudaStream_t st = p->stream;
   const long long V = p->d.V;
-  JvieState S;
+  auto Sp = std::make_shared<JvieState>();
+  JvieState& S = *Sp;
   MARIE_TRY(jvie_setup(p, er, dx, freq, form, S));
   for (int e = 0; e < S_exc; ++e) MARIE_CUDA_TRY(cudaMemsetAsync(Je + e * js, 0, 3 * V * sizeof(double2), st));
   out.r.assign(S_exc, GmresResult());
@@ -355,26 +368,36 @@ static int jvie_solve_core(marie_plan* p, const double2* E, long long es, int S_
     return MARIE_OK;
   }
   const long long n = S.n;
-  DBuf rhs, x;
-  MARIE_TRY(rhs.alloc((size_t)S_exc * n * sizeof(double2), st));
-  MARIE_TRY(x.alloc((size_t)S_exc * n * sizeof(double2), st));
+  auto rhs = std::make_shared<DBuf>(), x = std::make_shared<DBuf>();
+  MARIE_TRY(rhs->alloc((size_t)S_exc * n * sizeof(double2), st));
+  MARIE_TRY(x->alloc((size_t)S_exc * n * sizeof(double2), st));
   k_jvie_rhs<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(S.f.as<double2>(), S.idx3.as<int64_t>(), n, E, es,
-                                                      rhs.as<double2>());
+                                                      rhs->as<double2>());
   count_launch();
   if (sa.solver == 'G')
-    MARIE_TRY(solve_systems(p, S, rhs.as<double2>(), S_exc, x.as<double2>(), precond, tol, inner_it, outer_it, out));
+    MARIE_TRY(solve_systems(p, S, rhs->as<double2>(), S_exc, x->as<double2>(), precond, tol, inner_it, outer_it, out,
+                            dfr));
   else
-    MARIE_TRY(solve_single(p, S, rhs.as<double2>(), x.as<double2>(), precond, tol, inner_it, outer_it, sa, out));
-  k_scatter_dofs<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(x.as<double2>(), S.idx3.as<int64_t>(), n, Je, js);
-  count_launch();
-  MARIE_CUDA_TRY(cudaGetLastError());
+    MARIE_TRY(solve_single(p, S, rhs->as<double2>(), x->as<double2>(), precond, tol, inner_it, outer_it, sa, out));
+  auto scatter = [p, Sp, x, n, S_exc, Je, js]() -> int {
+    k_scatter_dofs<<<dim3(grid_n(n), S_exc), 256, 0, p->stream>>>(x->as<double2>(), Sp->idx3.as<int64_t>(), n, Je,
+                                                                   js);
+    count_launch();
+    MARIE_CUDA_TRY(cudaGetLastError());
+    return MARIE_OK;
+  };
+  if (!dfr) return scatter();
+  dfr->keep.push_back(Sp);
+  dfr->keep.push_back(rhs);
+  dfr->keep.push_back(x);
+  dfr->after.push_back(scatter);
   return MARIE_OK;
 }
 
 // Solves A2 x_e = B_e (form-2 J-VIE operator of the state S) for S_exc
 // right-hand sides: FP64 pgmres, or GMRES-IR on a MARIE_MIXED plan.
 static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, int S_exc, double2* X, char precond,
-                         double tol, int inner_it, int outer_it, SolveOut& out) {
+                         double tol, int inner_it, int outer_it, SolveOut& out, Deferred* dfr) {
   cudaStream_t st = p->stream;
   const long long n = S.n;
   out.r.assign(S_exc, GmresResult());
@@ -394,8 +417,6 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
                            S.bf.as<float2>());
     BatchOp P32 = make_bop(p, MARIE_FP32, S, S.pa.as<double2>(), S.pb.as<double2>(), !pb_nz, S.paf.as<float2>(),
                            S.pbf.as<float2>());
-    const BatchOp* L1m = precond == 'L' ? &P32 : nullptr;
-    const BatchOp* R1m = precond == 'R' ? &P32 : nullptr;
     const int max_refine = 20;
     // restart of the inner solves: the plan's setting, else with an FP64
     // basis kInnerRestart64 (its Gram-Schmidt is FP64-pipe-bound, so
@@ -403,9 +424,88 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
     const int m_in = p->inner_restart > 0 ? p->inner_restart
                      : p->inner_prec == MARIE_FP64 ? std::min(inner_it, kInnerRestart64)
                                                    : inner_it;
+    const bool fp32b = p->inner_prec == MARIE_FP32;
+    SolveOut* outp = &out;
+    // The refinement driven from the host: the form selected by the plan, and
+    // the fallback of the graph launch (it starts from x = 0 again).
+    auto host_refine = [p, A32, P32, A64, precond, Bv, X, n, S_exc, tol, m_in, outer_it, max_refine, fp32b,
+                        outp]() -> int {
+      cudaStream_t st = p->stream;
+      SolveOut& out = *outp;
+      const BatchOp* L1m = precond == 'L' ? &P32 : nullptr;
+      const BatchOp* R1m = precond == 'R' ? &P32 : nullptr;
+      DBuf rb, db, flags, nrm;
+      MARIE_TRY(rb.alloc((size_t)S_exc * n * sizeof(double2), st));
+      MARIE_TRY(db.alloc((size_t)S_exc * n * sizeof(double2), st));
+      MARIE_TRY(flags.alloc(S_exc * sizeof(int), st));
+      MARIE_TRY(nrm.alloc((S_exc + batch_norm_scratch(S_exc)) * sizeof(double), st));
+      double2* Rr = rb.as<double2>();
+      double2* D = db.as<double2>();
+      MARIE_CUDA_TRY(cudaMemsetAsync(X, 0, (size_t)S_exc * n * sizeof(double2), st));
+      MARIE_CUDA_TRY(cudaMemcpyAsync(Rr, Bv, (size_t)S_exc * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      std::vector<double> bn(S_exc), rn(S_exc);
+      // the norms of the graph-launched refinement (same kernels, same bits)
+      double* nrm_d = nrm.as<double>();
+      auto norms = [&](const double2* V, const int* mask, std::vector<double>& h) -> int {
+        MARIE_TRY(batch_norms_dev(p, V, n, n, S_exc, mask, nrm_d + S_exc, nrm_d));
+        MARIE_CUDA_TRY(cudaMemcpyAsync(h.data(), nrm_d, S_exc * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MARIE_CUDA_TRY(cudaStreamSynchronize(st));
+        return MARIE_OK;
+      };
+      MARIE_TRY(norms(Bv, nullptr, bn));
+      rn = bn;
+      std::vector<int> act(S_exc), inner_total(S_exc, 0), last_p(S_exc, 0);
+      for (int e = 0; e < S_exc; ++e) {
+        out.r[e].relres = rn[e] / bn[e];
+        out.r[e].resvec.push_back(out.r[e].relres);
+      }
+      std::vector<double> inner_tols(S_exc, 0.5), rn_new(S_exc);
+      for (int it = 0; it < max_refine; ++it) {
+        bool any = false;
+        double inner_tol = 0.5;
+        for (int e = 0; e < S_exc; ++e) {
+          act[e] = out.r[e].relres > tol ? 1 : 0;
+          if (act[e]) {
+            any = true;
+            // half of what is still missing, not below the FP32 floor; each
+            // system of a batch stops its inner solve at its own tolerance
+            inner_tols[e] = std::min(0.5, std::max(0.5 * tol * bn[e] / rn[e], 1e-5));
+            inner_tol = std::min(inner_tol, inner_tols[e]);
+          }
+        }
+        if (!any) break;
+        MARIE_TRACE("refinement step");
+        std::vector<GmresResult> ri;
+        MARIE_TRY(gmres_batch(p, A32, L1m, R1m, Rr, n, n, S_exc, m_in, inner_tol, outer_it, D, n, ri, true, &act,
+                              false, p->inner_prec == MARIE_FP32, &inner_tols));
+        MARIE_CUDA_TRY(cudaMemcpyAsync(flags.p, act.data(), S_exc * sizeof(int), cudaMemcpyHostToDevice, st));
+        k_add_b<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(D, X, n, flags.as<int>());
+        count_launch();
+        // r = b - A64 x (FP64) for the systems that moved
+        MARIE_TRY(A64.apply(X, n, Rr, n, S_exc, flags.as<int>(), 1));
+        k_sub_b<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(Bv, Rr, n, flags.as<int>());
+        count_launch();
+        MARIE_CUDA_TRY(cudaGetLastError());
+        MARIE_TRY(norms(Rr, flags.as<int>(), rn_new));
+        for (int e = 0; e < S_exc; ++e) {
+          if (!act[e]) continue;
+          for (size_t i = 1; i < ri[e].resvec.size(); ++i) out.r[e].resvec.push_back(ri[e].resvec[i] * rn[e] / bn[e]);
+          inner_total[e] += ri[e].iter[1];
+          last_p[e] = ri[e].iter[0];
+          rn[e] = rn_new[e];
+          out.r[e].relres = rn[e] / bn[e];
+          out.r[e].resvec.push_back(out.r[e].relres);
+        }
+      }
+      for (int e = 0; e < S_exc; ++e) {
+        out.r[e].flag = out.r[e].relres <= tol ? 0 : 1;
+        out.r[e].iter[0] = last_p[e];
+        out.r[e].iter[1] = inner_total[e];
+      }
+      return MARIE_OK;
+    };
     if (p->graph_refine) {
-      // the whole refinement in one graph launch; the host-driven loop below
-      // when the graph cannot be built
+      // the whole refinement in one graph launch
       RefineOps ops;
       ops.add = [p, n, S_exc](const double2* D, double2* Xv, const int* fl) -> int {
         k_add_b<<<dim3(grid_n(n), S_exc), 256, 0, p->stream>>>(D, Xv, n, fl);
@@ -413,86 +513,35 @@ static int solve_systems(marie_plan* p, const JvieState& S, const double2* Bv, i
         MARIE_CUDA_TRY(cudaGetLastError());
         return MARIE_OK;
       };
-      ops.residual = [p, n, S_exc, &A64, Bv](const double2* Xv, double2* R, const int* fl) -> int {
+      ops.residual = [p, n, S_exc, A64, Bv](const double2* Xv, double2* R, const int* fl) -> int {
         MARIE_TRY(A64.apply(Xv, n, R, n, S_exc, fl, 1));
         k_sub_b<<<dim3(grid_n(n), S_exc), 256, 0, p->stream>>>(Bv, R, n, fl);
         count_launch();
         MARIE_CUDA_TRY(cudaGetLastError());
         return MARIE_OK;
       };
-      bool ran = false;
-      MARIE_TRY(refine_batch_graph(p, A32, L1m, R1m, ops, Bv, n, S_exc, m_in, tol, outer_it, max_refine,
-                                   p->inner_prec == MARIE_FP32, X, out.r, &ran));
-      if (ran) return MARIE_OK;
-    }
-    DBuf rb, db, flags, nrm;
-    MARIE_TRY(rb.alloc((size_t)S_exc * n * sizeof(double2), st));
-    MARIE_TRY(db.alloc((size_t)S_exc * n * sizeof(double2), st));
-    MARIE_TRY(flags.alloc(S_exc * sizeof(int), st));
-    MARIE_TRY(nrm.alloc((S_exc + batch_norm_scratch(S_exc)) * sizeof(double), st));
-    double2* Rr = rb.as<double2>();
-    double2* D = db.as<double2>();
-    MARIE_CUDA_TRY(cudaMemsetAsync(X, 0, (size_t)S_exc * n * sizeof(double2), st));
-    MARIE_CUDA_TRY(cudaMemcpyAsync(Rr, Bv, (size_t)S_exc * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-    std::vector<double> bn(S_exc), rn(S_exc);
-    // the norms of the graph-launched refinement (same kernels, same bits)
-    double* nrm_d = nrm.as<double>();
-    auto norms = [&](const double2* V, const int* mask, std::vector<double>& h) -> int {
-      MARIE_TRY(batch_norms_dev(p, V, n, n, S_exc, mask, nrm_d + S_exc, nrm_d));
-      MARIE_CUDA_TRY(cudaMemcpyAsync(h.data(), nrm_d, S_exc * sizeof(double), cudaMemcpyDeviceToHost, st));
-      MARIE_CUDA_TRY(cudaStreamSynchronize(st));
-      return MARIE_OK;
-    };
-    MARIE_TRY(norms(Bv, nullptr, bn));
-    rn = bn;
-    std::vector<int> act(S_exc), inner_total(S_exc, 0), last_p(S_exc, 0);
-    for (int e = 0; e < S_exc; ++e) {
-      out.r[e].relres = rn[e] / bn[e];
-      out.r[e].resvec.push_back(out.r[e].relres);
-    }
-    std::vector<double> inner_tols(S_exc, 0.5), rn_new(S_exc);
-    for (int it = 0; it < max_refine; ++it) {
-      bool any = false;
-      double inner_tol = 0.5;
-      for (int e = 0; e < S_exc; ++e) {
-        act[e] = out.r[e].relres > tol ? 1 : 0;
-        if (act[e]) {
-          any = true;
-          // half of what is still missing, not below the FP32 floor; each
-          // system of a batch stops its inner solve at its own tolerance
-          inner_tols[e] = std::min(0.5, std::max(0.5 * tol * bn[e] / rn[e], 1e-5));
-          inner_tol = std::min(inner_tol, inner_tols[e]);
-        }
+      auto job = std::make_unique<RefineJob>();
+      bool ok = false;
+      MARIE_TRY(job->prepare(p, A32, precond == 'L' ? &P32 : nullptr, precond == 'R' ? &P32 : nullptr, ops, Bv, n,
+                             S_exc, m_in, tol, outer_it, max_refine, fp32b, X, &ok));
+      if (ok && dfr) {
+        // one launch with the other bodies' refinements; the results (or the
+        // host-driven refinement, if that graph could not run) afterwards
+        RefineJob* jp = job.get();
+        dfr->jobs.push_back(std::move(job));
+        dfr->after.push_back([dfr, jp, outp, host_refine]() -> int {
+          return dfr->launched ? jp->finish(outp->r) : host_refine();
+        });
+        return MARIE_OK;
       }
-      if (!any) break;
-      MARIE_TRACE("refinement step");
-      std::vector<GmresResult> ri;
-      MARIE_TRY(gmres_batch(p, A32, L1m, R1m, Rr, n, n, S_exc, m_in, inner_tol, outer_it, D, n, ri, true, &act,
-                            false, p->inner_prec == MARIE_FP32, &inner_tols));
-      MARIE_CUDA_TRY(cudaMemcpyAsync(flags.p, act.data(), S_exc * sizeof(int), cudaMemcpyHostToDevice, st));
-      k_add_b<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(D, X, n, flags.as<int>());
-      count_launch();
-      // r = b - A64 x (FP64) for the systems that moved
-      MARIE_TRY(A64.apply(X, n, Rr, n, S_exc, flags.as<int>(), 1));
-      k_sub_b<<<dim3(grid_n(n), S_exc), 256, 0, st>>>(Bv, Rr, n, flags.as<int>());
-      count_launch();
-      MARIE_CUDA_TRY(cudaGetLastError());
-      MARIE_TRY(norms(Rr, flags.as<int>(), rn_new));
-      for (int e = 0; e < S_exc; ++e) {
-        if (!act[e]) continue;
-        for (size_t i = 1; i < ri[e].resvec.size(); ++i) out.r[e].resvec.push_back(ri[e].resvec[i] * rn[e] / bn[e]);
-        inner_total[e] += ri[e].iter[1];
-        last_p[e] = ri[e].iter[0];
-        rn[e] = rn_new[e];
-        out.r[e].relres = rn[e] / bn[e];
-        out.r[e].resvec.push_back(out.r[e].relres);
+      if (ok) {
+        std::vector<RefineJob*> one{job.get()};
+        bool ran = false;
+        MARIE_TRY(launch_refine_jobs(one, p->stream, &ran));
+        if (ran) return job->finish(out.r);
       }
     }
-    for (int e = 0; e < S_exc; ++e) {
-      out.r[e].flag = out.r[e].relres <= tol ? 0 : 1;
-      out.r[e].iter[0] = last_p[e];
-      out.r[e].iter[1] = inner_total[e];
-    }
+    return host_refine();
   }
   return MARIE_OK;
 }
@@ -741,6 +790,81 @@ __global__ void k_scale_field(double2* __restrict__ x, double s, long long n) {
 
 using namespace marie;
 
+
+// The bodies of marie_jvie_solve_bodies with their refinements in ONE graph
+// launch: each body's set-up, right-hand sides and refinement start run on
+// its plan's stream; the refinement loops of all bodies are independent
+// branches of one graph launched once; then each body's results, DOF scatter
+// and host copies.
+static int solve_bodies_one_launch(int nbody, marie_plan* const* plans, const double* const* Einc,
+                                   const int64_t* nexc, const double* const* e_r, const double* dx, double freq,
+                                   int form, char precond, double tol, int inner_it, int outer_it, double* const* Je,
+                                   int* flag, double* relres, int* iter) {
+  Deferred dfr;
+  long long off = 0;
+  for (int b = 0; b < nbody; ++b) {
+    marie_plan* p = plans[b];
+    auto fail = [&](int code) {
+      const std::string m = marie_last_error();
+      return set_error(code, "body %d: %s", b, m.c_str());
+    };
+    if (!Einc[b] || !e_r[b] || !Je[b] || nexc[b] < 1) return set_error(MARIE_EINVAL, "body %d: NULL argument", b);
+    if (!p->has_op) return set_error(MARIE_ENOOP, "body %d: plan has no operator", b);
+    if (!(dx[b] > 0) || !(freq > 0)) return set_error(MARIE_EINVAL, "body %d: dx and freq must be positive", b);
+    double tb = tol;
+    int fb = form, ib = inner_it, ob = outer_it;
+    char pb = precond;
+    int s = clamp_args(tb, fb, pb, ib, ob);
+    if (s != MARIE_OK) return fail(s);
+    cudaStream_t st = p->stream;
+    const long long V = p->d.V;
+    const size_t jbytes = (size_t)nexc[b] * 3 * V * sizeof(double2);
+    auto tE = std::make_shared<DBuf>(), tER = std::make_shared<DBuf>(), tJe = std::make_shared<DBuf>();
+    const void *E_d, *er_d;
+    void* Je_d;
+    if ((s = stage_in(Einc[b], jbytes, st, *tE, &E_d)) != MARIE_OK) return fail(s);
+    if ((s = stage_in(e_r[b], V * sizeof(double2), st, *tER, &er_d)) != MARIE_OK) return fail(s);
+    if ((s = stage_out(Je[b], jbytes, st, *tJe, &Je_d)) != MARIE_OK) return fail(s);
+    auto pf = std::make_shared<HostPrefault>();
+    pf->start(Je[b], jbytes);
+    auto so = std::make_shared<SolveOut>();
+    s = jvie_solve_core(p, (const double2*)E_d, 3 * V, (int)nexc[b], (const double2*)er_d, dx[b], freq, fb, pb, tb,
+                        ib, ob, (double2*)Je_d, 3 * V, *so, SolverArgs(), &dfr);
+    if (s != MARIE_OK) return fail(s);
+    dfr.keep.push_back(tE);
+    dfr.keep.push_back(tER);
+    dfr.keep.push_back(tJe);
+    dfr.keep.push_back(pf);
+    dfr.keep.push_back(so);
+    void* Jh = Je[b];
+    const long long ne = nexc[b], o = off;
+    dfr.after.push_back([p, pf, so, Jh, Je_d, jbytes, ne, o, flag, relres, iter]() -> int {
+      pf->join();
+      MARIE_TRY(finish_out(Jh, Je_d, jbytes, p->stream));
+      MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
+      for (long long e = 0; e < ne; ++e) {
+        if (flag) flag[o + e] = so->r[e].flag;
+        if (relres) relres[o + e] = so->r[e].relres;
+        if (iter) {
+          iter[2 * (o + e)] = so->r[e].iter[0];
+          iter[2 * (o + e) + 1] = so->r[e].iter[1];
+        }
+      }
+      return check_kernel_status(p);
+    });
+    off += nexc[b];
+  }
+  if (!dfr.jobs.empty()) {
+    std::vector<RefineJob*> jobs;
+    for (auto& j : dfr.jobs) jobs.push_back(j.get());
+    bool ran = false;
+    MARIE_TRY(launch_refine_jobs(jobs, plans[0]->stream, &ran));
+    dfr.launched = ran;
+  }
+  for (auto& step : dfr.after) MARIE_TRY(step());
+  return MARIE_OK;
+}
+
 extern "C" {
 
 int marie_scat_solver(marie_plan* p, const double* Einc, const double* Hinc, double dx, double freq,
@@ -984,7 +1108,27 @@ int marie_jvie_solve_bodies(int nbody, marie_plan* const* plans, const double* c
                             double tol, int inner_it, int outer_it, double* const* Je, int* flag, double* relres,
                             int* iter, double* solvert) {
   if (nbody < 1 || !plans || !Einc || !nexc || !e_r || !dx || !Je) return set_error(MARIE_EINVAL, "NULL argument");
+  for (int b = 0; b < nbody; ++b)
+    if (!plans[b]) return set_error(MARIE_EINVAL, "NULL plan (body %d)", b);
   const auto t0 = std::chrono::steady_clock::now();
+  // bodies on one device whose plans refine in graphs: all refinements in one
+  // graph launch
+  bool one_launch = nbody >= 2;
+  for (int b = 0; b < nbody && one_launch; ++b)
+    one_launch = plans[b]->device == plans[0]->device && plans[b]->graph_refine &&
+                 plans[b]->precision == MARIE_MIXED;
+  if (one_launch) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaSetDevice(plans[0]->device);
+    const int s = solve_bodies_one_launch(nbody, plans, Einc, nexc, e_r, dx, freq, form, precond, tol, inner_it,
+                                          outer_it, Je, flag, relres, iter);
+    cudaSetDevice(dev);
+    if (s != MARIE_OK) return s;
+    const auto t1 = std::chrono::steady_clock::now();
+    if (solvert) *solvert = std::chrono::duration<double>(t1 - t0).count();
+    return MARIE_OK;
+  }
   std::vector<int> status(nbody, MARIE_OK);
   std::vector<std::string> msg(nbody);
   std::vector<long long> off(nbody + 1, 0);

@@ -1141,80 +1141,147 @@ static long long kernel_nodes(cudaGraph_t g) {
   return k;
 }
 
-int refine_batch_graph(marie_plan* p, const BatchOp& A32, const BatchOp* L1, const BatchOp* R1, const RefineOps& ops,
+struct RefineJob::Impl {
+  marie_plan* p = nullptr;
+  BatchOp A32;
+  BatchOp L1v, R1v;
+  bool hasL1 = false, hasR1 = false;
+  RefineOps ops;
+  const double2* Bv = nullptr;
+  double2* X = nullptr;
+  long long n = 0, cap = 0;
+  int S = 0, m = 0, maxit_in = 0, MR = 0;
+  double tol = 0;
+  BatchWork W;
+  DBuf rr, dd, rv, bp, dv, iv, hs, sv;
+  // views of the buffers
+  double2 *Rr = nullptr, *D = nullptr, *Rv = nullptr, *bpb = nullptr;
+  double *dp = nullptr, *bn = nullptr, *rn = nullptr, *rn_new = nullptr, *relres = nullptr, *itol = nullptr,
+         *bnorm_in = nullptr, *rn_in = nullptr, *npart = nullptr, *hist = nullptr, *step_scale = nullptr,
+         *step_relres = nullptr;
+  int *ip = nullptr, *act = nullptr, *act_in = nullptr, *outit = nullptr, *pk = nullptr, *inner_total = nullptr,
+      *last_p = nullptr, *hlen = nullptr, *allstop = nullptr, *err = nullptr, *ncyc = nullptr, *nstep = nullptr,
+      *tcyc = nullptr, *step_end = nullptr, *step_act = nullptr;
+  size_t nd = 0;
+  long long nodes_step = 0, nodes_cycle = 0;
+  const BatchOp* L1() const { return hasL1 ? &L1v : nullptr; }
+  const BatchOp* R1() const { return hasR1 ? &R1v : nullptr; }
+  int run_cycle() {
+    return W.f32 ? cycle<float2>(p, W, A32, L1(), R1(), D, n, Rv, n) : cycle<double2>(p, W, A32, L1(), R1(), D, n, Rv, n);
+  }
+};
+
+RefineJob::RefineJob() : d(new Impl) {}
+RefineJob::~RefineJob() = default;
+
+int RefineJob::prepare(marie_plan* p, const BatchOp& A32, const BatchOp* L1, const BatchOp* R1, const RefineOps& ops,
                        const double2* Bv, long long n, int S, int m, double tol, int maxit_in, int max_refine,
-                       bool fp32_basis, double2* X, std::vector<GmresResult>& out, bool* ran) {
-  *ran = false;
+                       bool fp32_basis, double2* X, bool* ok) {
+  *ok = false;
   if (S < 1 || m < 1 || m > 127 || max_refine < 1) return MARIE_OK;
-  const int MR = max_refine;
-  const long long cap = (long long)m * (maxit_in > 0 ? maxit_in : 1) * MR;  // inner history entries per system
+  const long long cap = (long long)m * (maxit_in > 0 ? maxit_in : 1) * max_refine;  // inner history per system
   if (cap * S > (16LL << 20)) return MARIE_OK;
   if (fp32_basis && (!A32.apply32 || (L1 && !L1->apply32) || (R1 && !R1->apply32))) return MARIE_OK;
+  Impl& J = *d;
+  J.p = p;
+  J.A32 = A32;
+  if (L1) J.L1v = *L1;
+  if (R1) J.R1v = *R1;
+  J.hasL1 = L1 != nullptr;
+  J.hasR1 = R1 != nullptr;
+  J.ops = ops;
+  J.Bv = Bv;
+  J.X = X;
+  J.n = n;
+  J.cap = cap;
+  J.S = S;
+  J.m = m;
+  J.maxit_in = maxit_in;
+  J.MR = max_refine;
+  J.tol = tol;
   cudaStream_t st = p->stream;
   // matvec workspaces at their largest, so that nothing is allocated while capturing
   MARIE_TRY(ensure_workspace(p, MARIE_FP64, S < p->nrhs_max ? S : p->nrhs_max, true));
-  BatchWork W;
-  MARIE_TRY(W.init(st, S, m, n, fp32_basis));
-  if (p->batch_groups == 2 && S >= 2) MARIE_TRY(W.init_groups());
-  DBuf rr, dd, rv, bp, dv, iv, hs, sv;
-  MARIE_TRY(rr.alloc((size_t)S * n * sizeof(double2), st));
-  MARIE_TRY(dd.alloc((size_t)S * n * sizeof(double2), st));
-  MARIE_TRY(rv.alloc((size_t)S * n * sizeof(double2), st));
-  if (L1) MARIE_TRY(bp.alloc((size_t)S * n * sizeof(double2), st));
+  MARIE_TRY(J.W.init(st, S, m, n, fp32_basis));
+  if (p->batch_groups == 2 && S >= 2) MARIE_TRY(J.W.init_groups());
+  MARIE_TRY(J.rr.alloc((size_t)S * n * sizeof(double2), st));
+  MARIE_TRY(J.dd.alloc((size_t)S * n * sizeof(double2), st));
+  MARIE_TRY(J.rv.alloc((size_t)S * n * sizeof(double2), st));
+  if (L1) MARIE_TRY(J.bp.alloc((size_t)S * n * sizeof(double2), st));
   // FP64 per system: bn rn rn_new relres itol bnorm_in rn_in, then the norm scratch
-  const size_t nd = 7 * (size_t)S + batch_norm_scratch(S);
-  MARIE_TRY(dv.alloc(nd * sizeof(double), st));
-  // int per system: act act_in outit pk inner_total last_p hlen allstop, then err ncycles nstep
-  MARIE_TRY(iv.alloc((8 * (size_t)S + 4) * sizeof(int), st));
-  MARIE_TRY(hs.alloc((size_t)S * cap * sizeof(double), st));
+  J.nd = 7 * (size_t)S + batch_norm_scratch(S);
+  MARIE_TRY(J.dv.alloc(J.nd * sizeof(double), st));
+  // int per system: act act_in outit pk inner_total last_p hlen allstop, then err ncycles nstep cycles
+  MARIE_TRY(J.iv.alloc((8 * (size_t)S + 4) * sizeof(int), st));
+  MARIE_TRY(J.hs.alloc((size_t)S * cap * sizeof(double), st));
   // per system and step: scale, relres (FP64), end, act (int)
-  MARIE_TRY(sv.alloc((size_t)S * MR * (2 * sizeof(double) + 2 * sizeof(int)), st));
-  double2 *Rr = rr.as<double2>(), *D = dd.as<double2>(), *Rv = rv.as<double2>(), *bpb = bp.as<double2>();
-  double* dp = dv.as<double>();
-  double *bn = dp, *rn = dp + S, *rn_new = dp + 2 * S, *relres = dp + 3 * S, *itol = dp + 4 * S,
-         *bnorm_in = dp + 5 * S, *rn_in = dp + 6 * S, *npart = dp + 7 * S;
-  int* ip = iv.as<int>();
-  int *act = ip, *act_in = ip + S, *outit = ip + 2 * S, *pk = ip + 3 * S, *inner_total = ip + 4 * S,
-      *last_p = ip + 5 * S, *hlen = ip + 6 * S, *allstop = ip + 7 * S, *err = ip + 8 * S, *ncyc = err + 1,
-      *nstep = err + 2, *tcyc = err + 3;
-  double* hist = hs.as<double>();
-  double* step_scale = sv.as<double>();
-  double* step_relres = step_scale + (size_t)S * MR;
-  int* step_end = reinterpret_cast<int*>(step_relres + (size_t)S * MR);
-  int* step_act = step_end + (size_t)S * MR;
+  MARIE_TRY(J.sv.alloc((size_t)S * max_refine * (2 * sizeof(double) + 2 * sizeof(int)), st));
+  J.Rr = J.rr.as<double2>();
+  J.D = J.dd.as<double2>();
+  J.Rv = J.rv.as<double2>();
+  J.bpb = J.bp.as<double2>();
+  J.dp = J.dv.as<double>();
+  J.bn = J.dp;
+  J.rn = J.dp + S;
+  J.rn_new = J.dp + 2 * S;
+  J.relres = J.dp + 3 * S;
+  J.itol = J.dp + 4 * S;
+  J.bnorm_in = J.dp + 5 * S;
+  J.rn_in = J.dp + 6 * S;
+  J.npart = J.dp + 7 * S;
+  J.ip = J.iv.as<int>();
+  J.act = J.ip;
+  J.act_in = J.ip + S;
+  J.outit = J.ip + 2 * S;
+  J.pk = J.ip + 3 * S;
+  J.inner_total = J.ip + 4 * S;
+  J.last_p = J.ip + 5 * S;
+  J.hlen = J.ip + 6 * S;
+  J.allstop = J.ip + 7 * S;
+  J.err = J.ip + 8 * S;
+  J.ncyc = J.err + 1;
+  J.nstep = J.err + 2;
+  J.tcyc = J.err + 3;
+  J.hist = J.hs.as<double>();
+  J.step_scale = J.sv.as<double>();
+  J.step_relres = J.step_scale + (size_t)S * max_refine;
+  J.step_end = reinterpret_cast<int*>(J.step_relres + (size_t)S * max_refine);
+  J.step_act = J.step_end + (size_t)S * max_refine;
   // eager start: x = 0, r = b, ||b||, relres = 1, counters 0
   MARIE_CUDA_TRY(cudaMemsetAsync(X, 0, (size_t)S * n * sizeof(double2), st));
-  MARIE_CUDA_TRY(cudaMemcpyAsync(Rr, Bv, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-  MARIE_TRY(batch_norms_dev(p, Bv, n, n, S, nullptr, npart, bn));
-  kr_start<<<1, 128, 0, st>>>(S, bn, rn, relres);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(J.Rr, Bv, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  MARIE_TRY(batch_norms_dev(p, Bv, n, n, S, nullptr, J.npart, J.bn));
+  kr_start<<<1, 128, 0, st>>>(S, J.bn, J.rn, J.relres);
   count_launch();
-  MARIE_CUDA_TRY(cudaMemsetAsync(ip, 0, (8 * (size_t)S + 4) * sizeof(int), st));
-  {
-    std::vector<int> big(S, 1 << 30);
-    MARIE_CUDA_TRY(cudaMemcpyAsync(allstop, big.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
-  }
+  MARIE_CUDA_TRY(cudaMemsetAsync(J.ip, 0, (8 * (size_t)S + 4) * sizeof(int), st));
+  std::vector<int> big(S, 1 << 30);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(J.allstop, big.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
   MARIE_CUDA_TRY(cudaGetLastError());
-  MARIE_CUDA_TRY(cudaStreamSynchronize(st));  // the pageable staging vector above
+  MARIE_CUDA_TRY(cudaStreamSynchronize(st));  // the start is done before any graph of it launches
+  *ok = true;
+  return MARIE_OK;
+}
 
-  // ---- the graph: WHILE(refinement step) { open ; WHILE(restart cycle) { cycle ; close } ; update ; close }
-  const long long launches0 = marie_launch_count();
-  cudaGraph_t g = nullptr;
-  cudaGraphExec_t exec = nullptr;
+// Adds WHILE(refinement step) { open ; WHILE(restart cycle) { cycle ; close } ;
+// update ; close } to g, as a root node independent of g's other nodes.
+bool RefineJob::add_to(cudaGraph_t g) {
+  Impl& J = *d;
+  marie_plan* p = J.p;
+  cudaStream_t st = p->stream;
+  const int S = J.S, m = J.m;
+  const long long n = J.n;
   bool capturing = false;
-  auto fail = [&]() {
+  auto stop_capture = [&]() {
     if (capturing) {
       cudaGraph_t junk = nullptr;
       cudaStreamEndCapture(st, &junk);
-      if (junk) cudaGraphDestroy(junk);
+      capturing = false;
     }
     cudaGetLastError();
-    if (exec) cudaGraphExecDestroy(exec);
-    if (g) cudaGraphDestroy(g);
-    count_launch(launches0 - marie_launch_count());  // nothing of the captures ran
-    return MARIE_OK;  // *ran stays false: the caller refines from the host
+    return false;
   };
-  auto begin = [&](cudaGraph_t body, const cudaGraphNode_t* deps, size_t nd_) {
-    if (cudaStreamBeginCaptureToGraph(st, body, deps, nullptr, nd_, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+  auto begin = [&](cudaGraph_t body, const cudaGraphNode_t* deps, size_t ndeps) {
+    if (cudaStreamBeginCaptureToGraph(st, body, deps, nullptr, ndeps, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
       return false;
     capturing = true;
     return true;
@@ -1224,97 +1291,94 @@ int refine_batch_graph(marie_plan* p, const BatchOp& A32, const BatchOp* L1, con
     capturing = false;
     return cudaStreamEndCapture(st, &tmp) == cudaSuccess;
   };
-  auto run_cycle = [&]() {
-    return W.f32 ? cycle<float2>(p, W, A32, L1, R1, D, n, Rv, n) : cycle<double2>(p, W, A32, L1, R1, D, n, Rv, n);
-  };
-  if (cudaGraphCreate(&g, 0) != cudaSuccess) return fail();
   cudaGraphConditionalHandle h_step, h_cycle;
-  if (cudaGraphConditionalHandleCreate(&h_step, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) return fail();
+  if (cudaGraphConditionalHandleCreate(&h_step, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) return stop_capture();
   cudaGraphNodeParams cp = {};
   cp.type = cudaGraphNodeTypeConditional;
   cp.conditional.handle = h_step;
   cp.conditional.type = cudaGraphCondTypeWhile;
   cp.conditional.size = 1;
   cudaGraphNode_t n_step;
-  if (cudaGraphAddNode(&n_step, g, nullptr, nullptr, 0, &cp) != cudaSuccess) return fail();
+  if (cudaGraphAddNode(&n_step, g, nullptr, nullptr, 0, &cp) != cudaSuccess) return stop_capture();
   cudaGraph_t b_step = cp.conditional.phGraph_out[0];
-  if (cudaGraphConditionalHandleCreate(&h_cycle, b_step, 0, 0) != cudaSuccess) return fail();
+  if (cudaGraphConditionalHandleCreate(&h_cycle, b_step, 0, 0) != cudaSuccess) return stop_capture();
   // step, part 1: open, inner start (x0 = 0, r = the step's residual, left preconditioning), inner open
-  if (!begin(b_step, nullptr, 0)) return fail();
+  if (!begin(b_step, nullptr, 0)) return stop_capture();
   {
-    kr_open<<<1, 128, 0, st>>>(S, tol, relres, bn, rn, act, itol);
+    kr_open<<<1, 128, 0, st>>>(S, J.tol, J.relres, J.bn, J.rn, J.act, J.itol);
     count_launch();
-    int rc = cudaMemsetAsync(D, 0, (size_t)S * n * sizeof(double2), st) == cudaSuccess &&
-                     cudaMemcpyAsync(Rv, Rr, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st) ==
-                         cudaSuccess
-                 ? MARIE_OK
-                 : MARIE_ECUDA;
-    if (rc == MARIE_OK && L1) {
-      rc = L1->apply(Rv, n, W.t1.as<double2>(), n, S, allstop, 1);
-      if (rc == MARIE_OK &&
-          (cudaMemcpyAsync(Rv, W.t1.p, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
-           cudaMemcpyAsync(bpb, Rv, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st) != cudaSuccess))
-        rc = MARIE_ECUDA;
+    bool ok = cudaMemsetAsync(J.D, 0, (size_t)S * n * sizeof(double2), st) == cudaSuccess &&
+              cudaMemcpyAsync(J.Rv, J.Rr, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st) ==
+                  cudaSuccess;
+    if (ok && J.hasL1) {
+      ok = J.L1v.apply(J.Rv, n, J.W.t1.as<double2>(), n, S, J.allstop, 1) == MARIE_OK &&
+           cudaMemcpyAsync(J.Rv, J.W.t1.p, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st) ==
+               cudaSuccess &&
+           cudaMemcpyAsync(J.bpb, J.Rv, (size_t)S * n * sizeof(double2), cudaMemcpyDeviceToDevice, st) == cudaSuccess;
     }
-    if (rc == MARIE_OK) rc = batch_norms_dev(p, L1 ? bpb : Rr, n, n, S, nullptr, npart, bnorm_in);
-    if (rc == MARIE_OK) rc = batch_norms_dev(p, Rv, n, n, S, nullptr, npart, rn_in);
-    kr_inner_open<<<1, 128, 0, st>>>(S, m, maxit_in, act, itol, bnorm_in, rn_in, W.tol.as<double>(),
-                                     W.stop.as<int>(), act_in, outit, pk, err, ncyc, h_cycle);
+    ok = ok && batch_norms_dev(p, J.hasL1 ? J.bpb : J.Rr, n, n, S, nullptr, J.npart, J.bnorm_in) == MARIE_OK;
+    ok = ok && batch_norms_dev(p, J.Rv, n, n, S, nullptr, J.npart, J.rn_in) == MARIE_OK;
+    kr_inner_open<<<1, 128, 0, st>>>(S, m, J.maxit_in, J.act, J.itol, J.bnorm_in, J.rn_in, J.W.tol.as<double>(),
+                                     J.W.stop.as<int>(), J.act_in, J.outit, J.pk, J.err, J.ncyc, h_cycle);
     count_launch();
-    if (!end() || rc != MARIE_OK) return fail();
+    if (!end() || !ok) return stop_capture();
   }
   std::vector<cudaGraphNode_t> lv;
-  if (graph_leaves(b_step, lv) != MARIE_OK) return fail();
+  if (graph_leaves(b_step, lv) != MARIE_OK) return stop_capture();
   cudaGraphNodeParams ip2 = {};
   ip2.type = cudaGraphNodeTypeConditional;
   ip2.conditional.handle = h_cycle;
   ip2.conditional.type = cudaGraphCondTypeWhile;
   ip2.conditional.size = 1;
   cudaGraphNode_t n_cycle;
-  if (cudaGraphAddNode(&n_cycle, b_step, lv.data(), nullptr, lv.size(), &ip2) != cudaSuccess) return fail();
+  if (cudaGraphAddNode(&n_cycle, b_step, lv.data(), nullptr, lv.size(), &ip2) != cudaSuccess) return stop_capture();
   cudaGraph_t b_cycle = ip2.conditional.phGraph_out[0];
   // the restart cycle and its device-side close
-  if (!begin(b_cycle, nullptr, 0)) return fail();
+  if (!begin(b_cycle, nullptr, 0)) return stop_capture();
   {
-    const int rc = run_cycle();
-    kb_cycle_close<<<1, 128, 0, st>>>(S, m, maxit_in, W.resv.as<double>(), bnorm_in, itol, W.stop.as<int>(), act_in,
-                                      outit, pk, hist, hlen, cap, err, ncyc, h_cycle);
+    const int rc = J.run_cycle();
+    kb_cycle_close<<<1, 128, 0, st>>>(S, m, J.maxit_in, J.W.resv.as<double>(), J.bnorm_in, J.itol,
+                                      J.W.stop.as<int>(), J.act_in, J.outit, J.pk, J.hist, J.hlen, J.cap, J.err,
+                                      J.ncyc, h_cycle);
     count_launch();
-    if (!end() || rc != MARIE_OK) return fail();
+    if (!end() || rc != MARIE_OK) return stop_capture();
   }
   // step, part 2: x += d, the FP64 residual and its norm, close
-  if (!begin(b_step, &n_cycle, 1)) return fail();
+  if (!begin(b_step, &n_cycle, 1)) return stop_capture();
   {
-    int rc = ops.add(D, X, act);
-    if (rc == MARIE_OK) rc = ops.residual(X, Rr, act);
-    if (rc == MARIE_OK) rc = batch_norms_dev(p, Rr, n, n, S, act, npart, rn_new);
-    kr_close<<<1, 128, 0, st>>>(S, MR, tol, max_refine, act, outit, pk, rn_new, bn, hlen, rn, relres, inner_total,
-                                last_p, step_end, step_scale, step_relres, step_act, nstep, err, ncyc, tcyc, h_step);
+    int rc = J.ops.add(J.D, J.X, J.act);
+    if (rc == MARIE_OK) rc = J.ops.residual(J.X, J.Rr, J.act);
+    if (rc == MARIE_OK) rc = batch_norms_dev(p, J.Rr, n, n, S, J.act, J.npart, J.rn_new);
+    kr_close<<<1, 128, 0, st>>>(S, J.MR, J.tol, J.MR, J.act, J.outit, J.pk, J.rn_new, J.bn, J.hlen, J.rn, J.relres,
+                                J.inner_total, J.last_p, J.step_end, J.step_scale, J.step_relres, J.step_act, J.nstep,
+                                J.err, J.ncyc, J.tcyc, h_step);
     count_launch();
-    if (!end() || rc != MARIE_OK) return fail();
+    if (!end() || rc != MARIE_OK) return stop_capture();
   }
-  const long long nodes_step = kernel_nodes(b_step), nodes_cycle = kernel_nodes(b_cycle);
-  if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) return fail();
-  count_launch(launches0 - marie_launch_count());  // the captures ran nothing; counted below
-  if (cudaGraphLaunch(exec, st) != cudaSuccess) return fail();
-  *ran = true;
-  count_graph_loop();
-  // ---- results
-  std::vector<double> hd(nd), hh((size_t)S * cap), hsv((size_t)S * MR * 2);
+  J.nodes_step = kernel_nodes(b_step);
+  J.nodes_cycle = kernel_nodes(b_cycle);
+  return true;
+}
+
+int RefineJob::finish(std::vector<GmresResult>& out) {
+  Impl& J = *d;
+  cudaStream_t st = J.p->stream;
+  const int S = J.S, MR = J.MR;
+  const long long cap = J.cap;
+  std::vector<double> hd(J.nd), hsv((size_t)S * MR * 2);
   std::vector<int> hi(8 * (size_t)S + 4), hsi((size_t)S * MR * 2);
-  MARIE_CUDA_TRY(cudaMemcpyAsync(hd.data(), dp, nd * sizeof(double), cudaMemcpyDeviceToHost, st));
-  MARIE_CUDA_TRY(cudaMemcpyAsync(hi.data(), ip, hi.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
-  MARIE_CUDA_TRY(cudaMemcpyAsync(hsv.data(), step_scale, hsv.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-  MARIE_CUDA_TRY(cudaMemcpyAsync(hsi.data(), step_end, hsi.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
-  const cudaError_t es = cudaStreamSynchronize(st);
-  cudaGraphExecDestroy(exec);
-  cudaGraphDestroy(g);
-  MARIE_CUDA_TRY(es);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hd.data(), J.dp, J.nd * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hi.data(), J.ip, hi.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hsv.data(), J.step_scale, hsv.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(hsi.data(), J.step_end, hsi.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(st));
   const int e_code = hi[8 * S], steps = hi[8 * S + 2], cycles = hi[8 * S + 3];
-  count_launch((long long)steps * nodes_step + (long long)cycles * nodes_cycle);
+  count_launch((long long)steps * J.nodes_step + (long long)cycles * J.nodes_cycle);
   if (e_code != 0) return set_error(MARIE_EBREAKDOWN, "non-finite GMRES residual (system %d)", e_code - 1);
+  std::vector<double> hh;
   if (*std::max_element(hi.begin() + 6 * S, hi.begin() + 7 * S) > 0) {
-    MARIE_CUDA_TRY(cudaMemcpyAsync(hh.data(), hist, (size_t)S * cap * sizeof(double), cudaMemcpyDeviceToHost, st));
+    hh.resize((size_t)S * cap);
+    MARIE_CUDA_TRY(cudaMemcpyAsync(hh.data(), J.hist, hh.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     MARIE_CUDA_TRY(cudaStreamSynchronize(st));
   }
   const double* h_bn = hd.data();
@@ -1336,11 +1400,52 @@ int refine_batch_graph(marie_plan* p, const BatchOp& A32, const BatchOp* L1, con
       r.resvec.push_back(h_srel[o]);
     }
     r.relres = h_relres[s];
-    r.flag = r.relres <= tol ? 0 : 1;
+    r.flag = r.relres <= J.tol ? 0 : 1;
     r.iter[0] = hi[5 * S + s];
     r.iter[1] = hi[4 * S + s];
   }
   return MARIE_OK;
+}
+
+int launch_refine_jobs(const std::vector<RefineJob*>& jobs, cudaStream_t st, bool* ran) {
+  *ran = false;
+  const long long launches0 = marie_launch_count();
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  auto fail = [&]() {
+    cudaGetLastError();
+    if (exec) cudaGraphExecDestroy(exec);
+    if (g) cudaGraphDestroy(g);
+    count_launch(launches0 - marie_launch_count());  // nothing of the captures ran
+    return MARIE_OK;  // *ran stays false: the callers refine from the host
+  };
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return fail();
+  for (RefineJob* j : jobs)
+    if (!j->add_to(g)) return fail();
+  if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) return fail();
+  count_launch(launches0 - marie_launch_count());  // the captures ran nothing; counted by finish()
+  if (cudaGraphLaunch(exec, st) != cudaSuccess) return fail();
+  *ran = true;
+  count_graph_loop();
+  const cudaError_t es = cudaStreamSynchronize(st);
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(g);
+  MARIE_CUDA_TRY(es);
+  return MARIE_OK;
+}
+
+int refine_batch_graph(marie_plan* p, const BatchOp& A32, const BatchOp* L1, const BatchOp* R1, const RefineOps& ops,
+                       const double2* Bv, long long n, int S, int m, double tol, int maxit_in, int max_refine,
+                       bool fp32_basis, double2* X, std::vector<GmresResult>& out, bool* ran) {
+  *ran = false;
+  RefineJob job;
+  bool ok = false;
+  MARIE_TRY(job.prepare(p, A32, L1, R1, ops, Bv, n, S, m, tol, maxit_in, max_refine, fp32_basis, X, &ok));
+  if (!ok) return MARIE_OK;
+  std::vector<RefineJob*> one{&job};
+  MARIE_TRY(launch_refine_jobs(one, p->stream, ran));
+  if (!*ran) return MARIE_OK;
+  return job.finish(out);
 }
 
 }  // namespace marie

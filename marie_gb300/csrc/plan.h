@@ -3,6 +3,7 @@
 #include <unistd.h>
 
 #include <functional>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -222,6 +223,28 @@ struct RefineOps {
 int refine_batch_graph(marie_plan* p, const BatchOp& A32, const BatchOp* L1, const BatchOp* R1, const RefineOps& ops,
                        const double2* Bv, long long n, int S, int m, double tol, int maxit_in, int max_refine,
                        bool fp32_basis, double2* X, std::vector<GmresResult>& out, bool* ran);
+// The same in parts, so that the refinements of several plans (bodies) run in
+// one graph launch: prepare (allocations and the eager start on the plan's
+// stream; *ok = false when the graph form does not apply), then
+// launch_refine_jobs (each job's loops as independent root nodes of one
+// graph, launched once on st and waited for; *ran = false when the graph
+// cannot be built), then finish (the results) -- or, when nothing ran, the
+// host-driven refinement from scratch.  A job keeps copies of the operators.
+class RefineJob {
+ public:
+  RefineJob();
+  ~RefineJob();
+  int prepare(marie_plan* p, const BatchOp& A32, const BatchOp* L1, const BatchOp* R1, const RefineOps& ops,
+              const double2* Bv, long long n, int S, int m, double tol, int maxit_in, int max_refine, bool fp32_basis,
+              double2* X, bool* ok);
+  bool add_to(cudaGraph_t g);
+  int finish(std::vector<GmresResult>& out);
+
+ private:
+  struct Impl;
+  std::unique_ptr<Impl> d;
+};
+int launch_refine_jobs(const std::vector<RefineJob*>& jobs, cudaStream_t st, bool* ran);
 // Batched FP64 norms of S vectors (stride xs) into out[S] on the device; with
 // mask, only the systems whose mask[s] >= 1 (the others keep out[s]).  part:
 // batch_norm_scratch(S) doubles of scratch.

@@ -234,6 +234,37 @@ def test_uneven_bodies_solved_concurrently():
             assert np.linalg.norm(Je[..., e] - ref[e]) <= 1e-5 * np.linalg.norm(ref[e])
 
 
+def test_uneven_bodies_in_one_graph_launch():
+    """The refinements of three bodies of different grid sizes run as ONE
+    graph launch (their loops are independent branches of one graph) and
+    give bit for bit each body's own batched solve."""
+    import marie_gb300 as mg
+    from marie_gb300 import phantoms
+
+    em = vo.EMconstants(FREQ)
+    bodies = []
+    for seed, L in ((1, 12), (2, 16), (3, 24)):
+        r, er, _ = phantoms.ellipsoids(L, L, L, 2e-3, 3, seed, FREQ)
+        pos = phantoms.dipole_ring(0.6 * L * 2e-3, [0.0, 0.25 * L * 2e-3], 1)
+        Eb = np.asfortranarray(np.stack([vo.Dipole_Excitation(r, em["ko"], np.array([[0, 0, 1.0]]), p[None])
+                                         for p in pos], axis=4))
+        op = mg.Operator.assemble(L, L, L, 2e-3, FREQ, precision="mixed", nrhs_max=2)
+        op.set_inner_restart(8)
+        bodies.append((Eb, er, r, op))
+    lib = mg.load()
+    alone = [mg.JVIE_Solver_batch(Eb, er, r, FREQ, op, tol=1e-8) for Eb, er, r, op in bodies]
+    n0 = lib.marie_graph_loops()
+    res, _ = mg.JVIE_Solver_bodies(bodies, FREQ, tol=1e-8)
+    assert lib.marie_graph_loops() == n0 + 1  # one launch for all three bodies
+    for (Je, flg, rel, it), ref in zip(res, alone):
+        np.testing.assert_array_equal(Je, ref[0])
+        assert list(flg) == list(ref[1]) == [0, 0]
+        np.testing.assert_array_equal(rel, ref[2])
+        assert list(map(list, it)) == list(map(list, ref[3]))
+    for b in bodies:
+        b[3].close()
+
+
 def test_mixed_precision_solve_matches_fp64():
     import marie_gb300 as mg
 
