@@ -331,9 +331,10 @@ def run_gpu(args, world, rank, local):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64 matvec + inner krylov / c128 refinement",
             "data": "synthetic (seeded ellipsoid phantom, plane wave)",
             "config": headline_config(er, world),
-            "method": "mixed precision: inner GMRES(50) with the FP32 matvec and an FP64 Krylov basis "
-                      "(Arnoldi, Givens and residual estimates in FP64), FP64 true residuals and refinement "
-                      "(GMRES-IR)",
+            "method": "mixed precision: inner GMRES with the FP32 matvec and an FP64 Krylov basis "
+                      "(Arnoldi, Givens and residual estimates in FP64; restart 20), FP64 true residuals and "
+                      "refinement (GMRES-IR); the whole solve is one CUDA graph launch (nested conditional "
+                      "WHILE nodes)",
             "solve": {"mixed": {"flag": flag_m, "relres": relres_m, "iter": iter_m,
                                 "matvecs": len(resvec_m) - 1, "solves_per_s": round(value / world, 4)},
                       "fp64": {"flag": flag64, "relres": relres64, "iter": it64, "iterations": n_it64,
