@@ -208,6 +208,10 @@ def run_gpu(args, world, rank, local):
         # (fused x+y passes, default radix schedules; a tuning run under a
         # profiler would time the candidates serialised and could pick another)
         op.set_schedule(1, 0, 0)
+        # refinement steps and restart cycles driven from the host (plain
+        # graphs): ncu does not profile kernels inside conditional graphs;
+        # the kernels and their results are those of the one-launch solve
+        op.set_graph_refinement(False)
         for _ in range(args.warmup + args.steps):
             res = solve(op, Ed, erd, r)
         torch.cuda.synchronize()

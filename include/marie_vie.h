@@ -360,12 +360,16 @@ int marie_plan_set_inner_restart(marie_plan* plan, int restart);
  * other group's FP32 matvec; 1 steps all excitations together.  Per system the
  * arithmetic is the same either way: the results are identical. */
 int marie_plan_set_batch_groups(marie_plan* plan, int groups);
-/* Control of the mixed-precision refinement (no counterpart in the
- * reference): 1 (the default) runs a MARIE_MIXED plan's GMRES solve -- every
- * refinement step with its inner restart cycles, FP64 residuals and
- * tolerance updates -- as one launch of a CUDA graph with nested conditional
- * WHILE nodes, the device deciding every step; 0 drives the refinement steps
- * from the host.  The arithmetic and the results are the same. */
+/* Control of the device-driven loops (no counterpart in the reference): 1
+ * (the default) runs a MARIE_MIXED plan's GMRES solve -- every refinement
+ * step with its inner restart cycles, FP64 residuals and tolerance updates --
+ * as one launch of a CUDA graph with nested conditional WHILE nodes, the
+ * device deciding every step, and the restart cycles of other GMRES solves in
+ * one conditional-graph launch; 0 drives the refinement steps and the restart
+ * cycles from the host, one plain CUDA graph per cycle (the form whose kernels
+ * a profiler that replays kernels, such as ncu, can see: it does not profile
+ * kernels inside graphs with conditional nodes).  The arithmetic and the
+ * results are the same. */
 int marie_plan_set_graph_refinement(marie_plan* plan, int on);
 /* Host-side fault injection for tests (no reference counterpart): the nth
  * device allocation from now on fails with MARIE_ENOMEM (0 switches it off). */

@@ -924,7 +924,7 @@ int gmres_batch(marie_plan* p, const BatchOp& A, const BatchOp* L1, const BatchO
     if (!any) break;
     MARIE_TRACE("pgmres restart cycle");
     MARIE_CUDA_TRY(cudaMemcpyAsync(W.stop.p, stop.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
-    if (use_graph && cycles >= 1 && !loop_tried) {
+    if (use_graph && cycles >= 1 && !loop_tried && p->graph_refine) {
       // every remaining cycle in one graph launch (a conditional WHILE node
       // whose body is one cycle and its device-side close); the per-cycle
       // graphs below when the device or the sizes do not allow it

@@ -29,7 +29,7 @@ struct marie_plan {
   int inner_prec = MARIE_FP64;  // Krylov basis of the mixed-precision inner solves
   int inner_restart = 0;        // their restart length (0: the caller's inner_it)
   int batch_groups = 2;         // batched GMRES: systems split into this many groups on their own streams
-  bool graph_refine = true;     // mixed-precision refinement in one graph launch (host-driven when false)
+  bool graph_refine = true;     // conditional-graph loops (refinement, restart cycles); host-driven when false
   int oct = 0;  // 1: fN64/fN32 hold the (L+1)(M+1)(N+1) octant, 0: the full array
 
   // The FP32 N operator stored full along x for the z pass's bulk tile copy

@@ -226,8 +226,9 @@ class Operator:
         return self
 
     def set_graph_refinement(self, on):
-        """Mixed-precision refinement as one graph launch (True, default) or
-        driven from the host (False); the results are the same."""
+        """Refinement steps and restart cycles in conditional-graph launches
+        (True, default) or driven from the host with one plain graph per cycle
+        (False, the form kernel profilers can see); the results are the same."""
         check(self.lib.marie_plan_set_graph_refinement(self.plan, 1 if on else 0))
         return self
 
