@@ -219,16 +219,13 @@ int marie_jvie_solve(marie_plan* plan, const double* Einc, const double* e_r, do
                      double* iter, double* resvec, int64_t resvec_cap, int64_t* resvec_len,
                      double* solvert);
 
-/* JVIE_Solver for nexc excitations of one body solved together: Einc and Je
- * are nexc consecutive L x M x N x 3 arrays; the solves advance in lockstep
- * (one batched matvec per GMRES step, one graph launch per restart cycle).
- * Per excitation: flag[e], relres[e], iter[2e..2e+1].  The reference solves
- * excitations one at a time (JVIE_Solver.m is called per port/excitation). */
 /* Several bodies of uneven grid size (one plan each), each with nexc[b]
- * excitations, solved concurrently: every body's batch runs on its plan's
- * stream from its own host thread.  Outputs are concatenated over bodies
- * (flag, relres: sum(nexc); iter: 2 per excitation).  The reference solves one
- * body at a time. */
+ * excitations, solved concurrently.  On MARIE_MIXED plans of one device the
+ * refinements of all bodies are branches of ONE graph launch (each body's
+ * set-up, right-hand sides and results on its plan's stream); otherwise every
+ * body's batch runs on its plan's stream from its own host thread.  Outputs
+ * are concatenated over bodies (flag, relres: sum(nexc); iter: 2 per
+ * excitation).  The reference solves one body at a time. */
 int marie_jvie_solve_bodies(int nbody, marie_plan* const* plans, const double* const* Einc,
                             const int64_t* nexc, const double* const* e_r, const double* dx,
                             double freq, int form, char precond, double tol, int inner_it,
@@ -260,6 +257,13 @@ int marie_jvie2solver(marie_plan* plan, const int64_t* idx, int64_t n_idx, const
                       double Gram, const double* Vrhs, double tol, int max_it, const double* Vini, double* Vsol,
                       int* flag, double* relres, double* iter, double* solvert);
 
+/* JVIE_Solver for nexc excitations of one body solved together: Einc and Je
+ * are nexc consecutive L x M x N x 3 arrays; the solves advance in lockstep,
+ * one batched matvec per GMRES step for each of two groups of excitations (see
+ * marie_plan_set_batch_groups).  On a MARIE_MIXED plan the whole refinement is
+ * one graph launch (marie_plan_set_graph_refinement).  Per excitation:
+ * flag[e], relres[e], iter[2e..2e+1].  The reference solves excitations one at
+ * a time (JVIE_Solver.m is called per port/excitation). */
 int marie_jvie_solve_batch(marie_plan* plan, const double* Einc, int64_t nexc, const double* e_r,
                            double dx, double freq, int form, char precond, double tol, int inner_it,
                            int outer_it, double* Je, int* flag, double* relres, int* iter,
