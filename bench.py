@@ -347,7 +347,11 @@ def run_gpu(args, world, rank, local):
                       "field_rel_err_mixed_vs_fp64": field_err, "mixed_inner_fp32_basis": inner32,
                       "mixed_other_solvers": variants},
             "matvec_ms": {"fp32": mv["fp32_ms"], "fp64": mv["fp64_ms"], "fp32_passes_ms": mv["fp32_passes"],
-                          "fp64_passes_ms": mv["fp64_passes"], "fp32_cufft_comparison": mv["fp32_cufft_ms"]},
+                          "fp64_passes_ms": mv["fp64_passes"], "fp32_cufft_comparison": mv["fp32_cufft_ms"],
+                          "fp32_bound": mv["fp32_bound_ms"], "fp64_bound": mv["fp64_bound_ms"],
+                          "note": "fp32/fp64: marie_mv_AN per call, which rebuilds the DOF map and coefficients; "
+                                  "*_bound: marie_plan_apply_mv_AN, the solver's matvec (map and coefficients "
+                                  "bound once; FP32 epilogue in FP32)"},
             "assembly_s": round(t_asm, 3),
             "autotune": {"chosen": {"fused_xy": tuned[0], "xy_variant": tuned[1], "z_variant": tuned[2]},
                          "candidates_ms": [{"fused_xy": f, "xy_variant": fv, "z_variant": z, "ms": round(ms, 4)}
@@ -357,7 +361,9 @@ def run_gpu(args, world, rank, local):
                          "traffic": zmul_traffic() if dom["name"] == "z_multiply" else None,
                          "peak_kind": kind, "alg_bytes_per_launch": dom["bytes"]},
             "matvec_roofline": {"alg_bytes": mv["alg_bytes"], "gbs": round(mv["alg_bytes"] / (mv["fp32_ms"] / 1e3) / 1e9, 1),
-                                "frac": round(mv["alg_bytes"] / (mv["fp32_ms"] / 1e3) / 1e9 / hbm, 4)},
+                                "frac": round(mv["alg_bytes"] / (mv["fp32_ms"] / 1e3) / 1e9 / hbm, 4),
+                                "bound_gbs": round(mv["alg_bytes"] / (mv["fp32_bound_ms"] / 1e3) / 1e9, 1),
+                                "bound_frac": round(mv["alg_bytes"] / (mv["fp32_bound_ms"] / 1e3) / 1e9 / hbm, 4)},
             "e2e": {"value": round(world / t_e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": 4 * V * 16,
                     "d2h_bytes_per_step": 3 * V * 16, "per_solve_ms": e2e_ms, "library_ms": e2e_lib_ms,
                     "clocks": clk_e2e.summary()},
@@ -416,6 +422,24 @@ def matvec_times(mg, op, op64, er, lib):
         e1.synchronize()
         res[name + "_ms"] = round(e0.elapsed_time(e1) / reps, 4)
         res[name + "_passes"] = passes
+        # the same product with the DOF map and coefficients bound to the plan
+        # once (marie_plan_apply_mv_AN: the solver's matvec, no per-call set-up;
+        # FP32 with its epilogue in FP32 as in the inner solves)
+        opr.bind_mv_AN(Mr, Mc, 8e-9, "notransp", idx_d)
+
+        def apply():
+            s = lib.marie_plan_apply_mv_AN(opr.plan, C.c_void_p(J.data_ptr()), C.c_void_p(out.data_ptr()), 1, prec)
+            assert s == 0, lib.marie_last_error()
+
+        for _ in range(3):
+            apply()
+        st.synchronize()
+        e0.record(st)
+        for _ in range(reps):
+            apply()
+        e1.record(st)
+        e1.synchronize()
+        res[name + "_bound_ms"] = round(e0.elapsed_time(e1) / reps, 4)
     # the same FP32 matvec through cuFFT (padded arrays, full operator), for comparison
     ms = C.c_float()
     cf = []

@@ -159,6 +159,16 @@ int marie_mv_K(marie_plan* plan, const double* JIn0, const int64_t* idx, int64_t
  * until the next bind or marie_plan_destroy. */
 int marie_plan_bind_mv_AN(marie_plan* plan, const double* Mr, const double* Mc, double Gram, int transp,
                           const int64_t* idx, int64_t n_idx);
+/* JOut = mv_AN(JIn0) with the mv_AN bound to the plan (one call of the handle
+ * fA of JVIE_Solver.m:211-297): no DOF map or coefficients are rebuilt per
+ * call, unlike marie_mv_AN.  JIn0, JOut: n_idx x nrhs complex, host or device.
+ * precision MARIE_FP32 runs the whole product in FP32 (transforms and the
+ * epilogue Gram*Mr*J - Mc*(N J), the matvec of the mixed-precision inner
+ * solves); MARIE_FP64 in FP64.  With device output the call returns without
+ * waiting for the plan's stream (a bounded-wait timeout is then reported by
+ * the next call that synchronises the plan); with host output it returns
+ * after the copy. */
+int marie_plan_apply_mv_AN(marie_plan* plan, const double* JIn0, double* JOut, int64_t nrhs, int precision);
 
 /* Replaces pgmres(A, b, restart, tol, maxit, L1, L2, R1, R2, x0)
  * (src_numeric/src_iterative/pgmres.m:70-181, pgmres_iter.m:22-150): restarted

@@ -88,6 +88,7 @@ SIGNATURES = {
     "marie_plan_set_inner_precision": (C.c_int, [_vp, C.c_int]),
     "marie_plan_set_inner_restart": (C.c_int, [_vp, C.c_int]),
     "marie_plan_set_batch_groups": (C.c_int, [_vp, C.c_int]),
+    "marie_plan_apply_mv_AN": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int]),
     "marie_plan_set_graph_refinement": (C.c_int, [_vp, C.c_int]),
     "marie_plan_bind_mv_AN": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, _vp, C.c_int64]),
     "marie_inject_alloc_failure": (None, [C.c_int64]),

@@ -628,10 +628,19 @@ static void free_bound(marie_plan* p) {
   cudaFree(p->bnd_inv);
   cudaFree(p->bnd_a);
   cudaFree(p->bnd_b);
+  cudaFree(p->bnd_af);
+  cudaFree(p->bnd_bf);
   p->bnd_idx = nullptr;
   p->bnd_inv = nullptr;
   p->bnd_a = p->bnd_b = nullptr;
+  p->bnd_af = p->bnd_bf = nullptr;
   p->bnd_n = 0;
+}
+
+// out[k] = (float2) in[k]
+__global__ void k_to_f32(const double2* __restrict__ in, long long n, float2* __restrict__ out) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    out[k] = make_float2((float)in[k].x, (float)in[k].y);
 }
 
 namespace marie {
@@ -743,6 +752,18 @@ int marie_plan_bind_mv_AN(marie_plan* p, const double* Mr, const double* Mc, dou
   if (s == MARIE_OK)
     s = build_coefficients(p, p->bnd_idx, n, (const double2*)Mr_d, (const double2*)Mc_d, Gram, transp, p->bnd_a,
                            p->bnd_b);
+  if (s == MARIE_OK && p->fN32) {
+    // FP32 copies for the FP32 applications, whose epilogue runs in FP32
+    if (cudaMalloc(&p->bnd_af, n * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&p->bnd_bf, n * sizeof(float2)) != cudaSuccess) {
+      cudaGetLastError();
+      s = set_error(MARIE_ENOMEM, "bound mv_AN: device allocation failed");
+    } else {
+      k_to_f32<<<grid_stride_blocks(n, 8), 256, 0, p->stream>>>(p->bnd_a, n, p->bnd_af);
+      k_to_f32<<<grid_stride_blocks(n, 8), 256, 0, p->stream>>>(p->bnd_b, n, p->bnd_bf);
+      count_launch(2);
+    }
+  }
   if (s == MARIE_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) s = set_error(MARIE_ECUDA, "bind mv_AN failed");
   if (s != MARIE_OK) {
     free_bound(p);
@@ -1032,6 +1053,41 @@ int marie_mv_AN(marie_plan* p, const double* JIn0, const double* Mr, const doubl
   MARIE_TRY(finish_out(JOut, out_d, n * nrhs * sizeof(double2), p->stream));
   MARIE_CUDA_TRY(cudaStreamSynchronize(p->stream));
   return check_kernel_status(p);
+}
+
+int marie_plan_apply_mv_AN(marie_plan* p, const double* JIn0, double* JOut, int64_t nrhs, int precision) {
+  if (!p || !JIn0 || !JOut) return set_error(MARIE_EINVAL, "NULL argument");
+  if (nrhs < 1) return set_error(MARIE_EINVAL, "nrhs must be >= 1");
+  if (!p->bnd_n) return set_error(MARIE_EINVAL, "no mv_AN bound to the plan (marie_plan_bind_mv_AN)");
+  MARIE_TRY(check_prec(p, precision));
+  const long long n = p->bnd_n;
+  DBuf tJ, tout;
+  const void* J_d;
+  void* out_d;
+  MARIE_TRY(stage_in(JIn0, n * nrhs * sizeof(double2), p->stream, tJ, &J_d));
+  MARIE_TRY(stage_out(JOut, n * nrhs * sizeof(double2), p->stream, tout, &out_d));
+  Prologue pro{nullptr, 0};
+  Epilogue ep{};
+  ep.a = p->bnd_a;
+  if (p->bnd_transp == 0) {
+    ep.b = p->bnd_b;
+  } else {
+    pro.pre = p->bnd_b;
+    pro.conjin = 1;
+    ep.conjout = 1;
+  }
+  if (precision == MARIE_FP32) {
+    // the FP32 operator's epilogue in FP32, as in the solver's inner matvecs
+    ep.af = p->bnd_af;
+    ep.bf = p->bnd_bf;
+  }
+  MARIE_TRY(run_matvec(p, precision, (const double2*)J_d, (double2*)out_d, n, (int)nrhs, p->bnd_inv, pro, ep));
+  if (out_d != JOut) {
+    MARIE_TRY(finish_out(JOut, out_d, n * nrhs * sizeof(double2), p->stream));
+    return check_kernel_status(p);
+  }
+  MARIE_CUDA_TRY(cudaGetLastError());
+  return MARIE_OK;
 }
 
 int marie_mv_L(marie_plan* p, const double* JIn0, double Gram, const int64_t* idx, int64_t n_idx, double* JOut,

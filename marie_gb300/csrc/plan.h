@@ -70,6 +70,8 @@ struct marie_plan {
   int* bnd_inv = nullptr;
   double2* bnd_a = nullptr;
   double2* bnd_b = nullptr;
+  float2* bnd_af = nullptr;  // FP32 copies of bnd_a / bnd_b (plans with an FP32 operator)
+  float2* bnd_bf = nullptr;
   long long bnd_n = 0;
   int bnd_transp = 0;
 

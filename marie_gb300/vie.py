@@ -107,6 +107,11 @@ def release_cached_memory():
     check(_lib.load().marie_release_cached_memory())
 
 
+def _sync_stream(op):
+    """Waits for the work queued on an Operator's plan stream."""
+    torch.cuda.ExternalStream(op.lib.marie_plan_stream(op.plan)).synchronize()
+
+
 def _sync():
     if torch is not None and torch.cuda.is_available():
         torch.cuda.current_stream().synchronize()
@@ -213,6 +218,19 @@ class Operator:
         check(self.lib.marie_plan_bind_mv_AN(self.plan, mrp, mcp, float(Gram), 1 if transp_flag == "transp" else 0,
                                              ip, n))
         return self
+
+    def apply_mv_AN(self, J, precision="fp64"):
+        """mv_AN bound with bind_mv_AN applied to J (n or n x nrhs; numpy or a
+        CUDA torch tensor), without rebuilding the DOF map per call.
+        precision 'fp32' runs the product in FP32 throughout."""
+        cuda = _is_cuda(J)
+        nrhs = 1 if J.ndim == 1 else J.shape[1]
+        jp, jk = _in(J)
+        op_, out = _out(J.shape, cuda)
+        check(self.lib.marie_plan_apply_mv_AN(self.plan, jp, op_, nrhs, _PREC[precision]))
+        if cuda:
+            _sync_stream(self)
+        return out
 
     def set_inner_restart(self, restart):
         """Restart length of the inner GMRES of a 'mixed' plan (0: the solver's inner_it)."""

@@ -61,3 +61,30 @@ def test_null_operator_needs_a_binding(cuda):
         mg.pgmres(op, b[:-3], 10, 1e-8, 5)
     with pytest.raises(ValueError):
         op.bind_mv_AN(Mr, Mc, Gram, "both", idx)
+
+
+@pytest.mark.parametrize("transp", ["notransp", "transp"])
+def test_apply_bound_mv_AN(cuda, transp):
+    """marie_plan_apply_mv_AN: the bound mv_AN without a per-call DOF map; FP64
+    gives the bits of marie_mv_AN, FP32 (epilogue in FP32 too) meets the FP32
+    bar against the oracle; host and device vectors, two right-hand sides."""
+    import torch
+
+    import marie_gb300 as mg
+
+    fN, Mr, Mc, Gram, idx, b = system(L=16, dx=3e-3, radius=0.02)
+    rng = np.random.default_rng(8)
+    J = np.asfortranarray(rng.standard_normal((idx.size, 2)) + 1j * rng.standard_normal((idx.size, 2)))
+    op = mg.Operator.from_array(fN, precision="mixed", nrhs_max=2).bind_mv_AN(Mr, Mc, Gram, transp, idx)
+    ref = np.stack([vo.mv_AN(J[:, c], fN, Mr, Mc, Gram, transp, idx) for c in range(2)], axis=1)
+    scale = np.max(np.abs(ref))
+    out64 = op.apply_mv_AN(J, "fp64")
+    np.testing.assert_array_equal(out64, mg.mv_AN(J, op, Mr, Mc, Gram, transp, idx, precision="fp64"))
+    assert np.max(np.abs(out64 - ref)) / scale < 1e-12
+    out32 = op.apply_mv_AN(J, "fp32")
+    assert np.max(np.abs(out32 - ref)) / scale < 1e-5
+    Jd = torch.from_numpy(J[:, 0].copy()).to(cuda)
+    outd = op.apply_mv_AN(Jd, "fp32")
+    assert outd.is_cuda
+    np.testing.assert_array_equal(outd.cpu().numpy(), out32[:, 0])
+    op.close()
