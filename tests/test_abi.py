@@ -51,3 +51,19 @@ def test_version_and_error_string_without_gpu():
     lib = _lib.load()
     assert lib.marie_version() >= 1
     assert isinstance(lib.marie_last_error(), bytes)
+
+
+def test_plan_settings_reject_a_null_plan_without_gpu():
+    """The schedule setters and the bound-matvec entry point check their plan
+    before touching the device (MARIE_EINVAL = -1 for a NULL plan)."""
+    import ctypes as C
+
+    from marie_gb300 import _lib
+
+    lib = _lib.load()
+    assert lib.marie_plan_set_batch_groups(None, 2) == _lib.MARIE_EINVAL
+    assert lib.marie_plan_set_graph_refinement(None, 1) == _lib.MARIE_EINVAL
+    assert lib.marie_plan_set_inner_restart(None, 20) == _lib.MARIE_EINVAL
+    buf = (C.c_double * 4)()
+    assert lib.marie_plan_apply_mv_AN(None, buf, buf, 1, _lib.MARIE_FP32) == _lib.MARIE_EINVAL
+    assert b"NULL" in lib.marie_last_error()
