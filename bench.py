@@ -210,8 +210,9 @@ def run_gpu(args, world, rank, local):
         op.set_schedule(1, 0, 0)
         # refinement steps and restart cycles driven from the host (plain
         # graphs): ncu does not profile kernels inside conditional graphs;
-        # the kernels and their results are those of the one-launch solve
-        op.set_graph_refinement(False)
+        # the kernels and their results are those of the one-launch solve.
+        # --graph-form keeps the one-launch form (for ncu --graph-profiling graph)
+        op.set_graph_refinement(args.graph_form)
         for _ in range(args.warmup + args.steps):
             res = solve(op, Ed, erd, r)
         torch.cuda.synchronize()
@@ -714,6 +715,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--solve-only", action="store_true", help="run the mixed solves only (for profilers)")
+    ap.add_argument("--graph-form", action="store_true",
+                    help="with --solve-only: the one-launch (conditional graph) form of the solve")
     ap.add_argument("--configs", default="c1,c3,c4,c5",
                     help="other workloads reported as extra keys of the main line ('' for none)")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
