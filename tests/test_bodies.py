@@ -7,7 +7,10 @@ import pytest
 
 from marie_gb300.bodies import Import_RHBM
 
-REF_BODY = "/root/reference/data/bodies/Cube_side10cm.vmm"
+# the reference checkout: MARIE_REFERENCE, else a directory "reference" beside this repository
+_REF_ROOT = os.environ.get("MARIE_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                                              os.pardir, "reference")
+REF_BODY = os.path.join(_REF_ROOT, "data", "bodies", "Cube_side10cm.vmm")
 
 
 def write_body(tmp_path, L=10, M=12, N=9, dx=4e-3, seed=0):
