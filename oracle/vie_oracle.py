@@ -658,9 +658,11 @@ def cubature_nop_batch(Np, w, u, v, r_m, R_faces, ko, dx):
         rq = q1[None, :] + np.outer(u, q2 - q1) + np.outer(v, q4 - q1)
         d = rq[None, None, :, :] - (rp[None, :, None, :] + r_m[:, None, None, :])  # B x Np x Np x 3
         R = np.sqrt(np.sum(d * d, axis=-1))
+        # coincident points of a face with itself give 1/0 here, as in the
+        # C++ core; those entries are replaced by the singular integrals later
         with np.errstate(divide="ignore", invalid="ignore"):
             G = np.exp(-1j * ko * R) / R
-        I[:, io, isrc] = np.sum(W[None] * G, axis=(1, 2))
+            I[:, io, isrc] = np.sum(W[None] * G, axis=(1, 2))
     for (a, b), (c, d_) in MIRROR:
         I[:, a, b] = I[:, c, d_]
     return dx**4 * I
