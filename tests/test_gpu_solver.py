@@ -261,6 +261,15 @@ def test_uneven_bodies_in_one_graph_launch():
         assert list(flg) == list(ref[1]) == [0, 0]
         np.testing.assert_array_equal(rel, ref[2])
         assert list(map(list, it)) == list(map(list, ref[3]))
+    # one plan driven from the host: the bodies go back to one host thread
+    # each (no shared launch), with the same bits
+    bodies[1][3].set_graph_refinement(False)
+    n1 = lib.marie_graph_loops()
+    res2, _ = mg.JVIE_Solver_bodies(bodies, FREQ, tol=1e-8)
+    assert lib.marie_graph_loops() == n1 + 2  # bodies 0 and 2 launch their own graphs
+    for (Je, flg, rel, it), ref in zip(res2, alone):
+        np.testing.assert_array_equal(Je, ref[0])
+        np.testing.assert_array_equal(rel, ref[2])
     for b in bodies:
         b[3].close()
 
