@@ -132,10 +132,9 @@ int marie_mv_AN(marie_plan* plan, const double* JIn0, const double* Mr, const do
  * exit; grids needing more (about 204-252 bytes per voxel in FP32, 396 in FP64)
  * are rejected with MARIE_EINVAL.  Device pointers only.  The call runs on the
  * plan's device and stream (the caller's current device is restored) with the
- * plan's matvec schedule, and waits on the host for that stream before it
- * returns.  The first call for a device looks up the array's address; make it
- * before any stream capture.  Calls share the array, so calls that overlap on
- * the GPU race. */
+ * plan's matvec schedule and blocks the host until that stream is done (it
+ * reads the kernels' error flag), so it cannot be captured into a CUDA graph.
+ * Calls share the array, so calls that overlap on the GPU race. */
 int marie_mv_AN_static(marie_plan* plan, const double* JIn0, const double* Mr,
                        const double* Mc, double Gram, int transp, const int64_t* idx,
                        int64_t n_idx, double* JOut, int precision);

@@ -14,12 +14,12 @@
 // device buffers; the plan (operator and twiddles) is created beforehand.
 //
 // Set-up: the first call for a device looks up the array's device address with
-// cudaGetSymbolAddress, with that device (the plan's) current, and caches it;
-// make that first call before any stream capture.  A call runs on the plan's
-// device and stream whatever device is current, and restores the caller's
-// current device before it returns.  Each call waits for its stream on the host
-// (it reads the status of the index check, then finishes the product) before
-// returning.  Every call shares the one array and it keeps the previous call's
+// cudaGetSymbolAddress, with that device (the plan's) current, and caches it.
+// A call runs on the plan's device and stream whatever device is current, and
+// restores the caller's current device before it returns.  Each call blocks
+// the host until its stream is done (it reads the status of the index check,
+// then finishes the product), so the entry point cannot be captured into a
+// CUDA graph.  Every call shares the one array and it keeps the previous call's
 // contents, so each call resets what must start clean (the error flag and the
 // index map); two calls that overlap on the GPU (other streams, other threads,
 // other plans on the same device) race on it.  The passes run with the plan's
