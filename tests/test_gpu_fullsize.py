@@ -1,9 +1,11 @@
 """The 128^3 workload at full size (12-ellipsoid phantom at 2 mm, 256^3 FFT,
 about 1.36 M DOFs, 298 MHz), checked through properties that hold at any
-size, since the oracle's matvec is too slow to compare element by element
-here: the adjoint identity of the two mv_AN flags, the transpose as the Mc
-similarity (N complex symmetric), linearity, FP32 products against FP64
-ones, and the FP64 residual of the currents JVIE_Solver returns."""
+size (its element-by-element parity with the oracle is in
+test_gpu_config_parity.py): the adjoint identity of the two mv_AN flags, the
+transpose as the Mc similarity (N complex symmetric), linearity, FP32
+products against FP64 ones, and the FP64 residual of the currents
+JVIE_Solver returns.  The largest grid (512 x 384 x 320 FFT) gets the same
+identities and an element-by-element comparison with the oracle's mv_AN."""
 import numpy as np
 import pytest
 
@@ -109,7 +111,8 @@ def test_solutions_meet_the_tolerance_in_fp64_full_size(c2, solver):
 def test_largest_grid_adjoint_and_precision():
     """The largest workload's grid, 256 x 192 x 160 voxels (512 x 384 x 320
     FFT), with a 15 cm sphere (5.3 M DOFs): adjoint identity in FP64 and
-    FP32, and FP32 products within 1e-5 of FP64, repeated.  This grid once
+    FP32, FP32 products within 1e-5 of FP64, repeated, and the product
+    element by element against the oracle's mv_AN.  This grid once
     showed the fused passes' first clusters, started early by programmatic
     dependent launch, reading the spectrum before the z pass had written it
     (wrong leading DOFs in three calls out of four)."""
@@ -133,5 +136,14 @@ def test_largest_grid_adjoint_and_precision():
             ref = _A(op, S, x, flag, "fp64")
             for _ in range(4):
                 assert relerr(_A(op, S, x, flag, "fp32"), ref) < 1e-5, flag
+        # element by element against the oracle's mv_AN (mv_AN.m:40-146) on
+        # the device-assembled operator: FP64 1e-12, FP32 1e-5 of max|out|
+        import os
+
+        fN = op.to_array()
+        orc = vo.mv_AN(x, fN, S["Mr"], S["Mc"], S["Gram"], "notransp", S["idxS3"], workers=os.cpu_count())
+        del fN
+        assert relerr(_A(op, S, x, "notransp", "fp64"), orc) < 1e-12
+        assert relerr(_A(op, S, x, "notransp", "fp32"), orc) < 1e-5
     finally:
         op.close()
