@@ -123,10 +123,10 @@ def test_batched_excitations_match_single_solves(precision, precond):
             assert list(iters[e]) == list(its)
             assert np.max(np.abs(Jb[..., e] - Js)) <= 1e-9 * np.max(np.abs(Js))
         else:
-            # the batch refines with the tightest inner tolerance of its members,
-            # so iteration counts may differ; both meet the FP64 residual bar
-            assert relres[e] <= 1e-8
-            assert np.linalg.norm(Jb[..., e] - Js) <= 1e-6 * np.linalg.norm(Js)
+            # each system of the batch refines with its own inner tolerances,
+            # so it takes the single solve's steps: the same bits
+            assert list(iters[e]) == list(its) and relres[e] == rs <= 1e-8
+            np.testing.assert_array_equal(Jb[..., e], Js)
     if precision == "fp64":
         fN = op.to_array()
         for e in range(3):
